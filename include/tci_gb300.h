@@ -1,0 +1,234 @@
+/*
+ * tci_gb300.h -- C ABI of the GB300-native TCI2 two-site sweep library
+ * (libtci_gpu.so).
+ *
+ * Drop-in boundary for TensorCrossInterpolation.jl's TCI2 path: a Julia host
+ * binds these entry points with ccall; Python tests bind
+ * them with ctypes.  Conventions:
+ *   - multi-indices are 1-based local indices, as in the reference
+ *     (MultiIndex = Vector{Int}, abstracttensortrain.jl:6-7), passed as
+ *     row-major int64 arrays (one multi-index per row);
+ *   - matrices and site tensors are column-major (Julia layout);
+ *   - host buffers are owned by the caller; device state lives behind opaque
+ *     handles owned by the library;
+ *   - every entry point returns 0 or a TCI_ERR_* code; tci_last_error() gives
+ *     the message of the last failure on the calling thread.  The codes map to
+ *     the exceptions the reference throws (ArgumentError, DimensionMismatch,
+ *     ErrorException).
+ * There is no CPU fallback: without a usable CUDA device every entry point
+ * that computes returns TCI_ERR_CUDA.
+ */
+#ifndef TCI_GB300_H
+#define TCI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+enum {
+  TCI_OK = 0,
+  TCI_ERR_ARG = 1,       /* ArgumentError (e.g. tensorci2.jl:750-754, :197-199 family) */
+  TCI_ERR_DIM = 2,       /* DimensionMismatch (tensorci2.jl:197-199) */
+  TCI_ERR_NAN = 3,       /* ErrorException("lu.L contains NaNs") (matrixlu.jl:164-169),
+                            "NaN in tensor T[b]" (tensorci2.jl:439-441) */
+  TCI_ERR_SINGULAR = 4,  /* singular pivot matrix in setsitetensor! (tensorci2.jl:391) */
+  TCI_ERR_GENERIC = 5,   /* other ErrorException (e.g. "maxsamplevalue is zero!") */
+  TCI_ERR_CUDA = 6,      /* CUDA runtime failure or no device */
+  TCI_ERR_OOM = 7,       /* device memory budget exceeded */
+  TCI_ERR_TIMEOUT = 8,   /* a bounded device wait gave up */
+  TCI_ERR_TOO_LARGE = 9  /* a matrix exceeds the kernel's on-chip plan */
+};
+
+/* Registered device functions f (tci_f_lookup names). */
+enum {
+  TCI_F_LORENTZ = 1, /* "lorentz": coeff / (1 + sum v^2)          params [coeff]            */
+  TCI_F_SERVED = 2,  /* "served" : 1/(1+a v.v) + b exp(-g|v-c|^2)  params [a, b, g, c_1..c_L] */
+  TCI_F_QTT1D = 3,   /* "qtt1d"  : quantics 1-D                    params [kind]             */
+  TCI_F_QTT2D = 4,   /* "qtt2d"  : quantics 2-D, d = 4             params []                 */
+  TCI_F_DENSE = 5    /* "dense"  : table lookup                    params [L, strides, data] */
+};
+
+/* Sweep strategies (sweepstrategies.jl:1-6). */
+enum { TCI_SWEEP_BACKANDFORTH = 0, TCI_SWEEP_FORWARD = 1, TCI_SWEEP_BACKWARD = 2 };
+
+/* Keyword arguments of optimize! (tensorci2.jl:700-720).  maxbonddim <= 0
+ * means typemax(Int).  `seed` seeds the host RNG that replaces
+ * Random.default_rng() in DefaultGlobalPivotFinder (globalpivotfinder.jl:156). */
+typedef struct tci_opts {
+  double tolerance;            /* :703, default 1e-8 */
+  int64_t maxbonddim;          /* :705 */
+  int64_t maxiter;             /* :706, default 20 */
+  int32_t sweepstrategy;       /* :707 */
+  int32_t normalizeerror;      /* :711 */
+  int32_t ncheckhistory;       /* :712 */
+  int32_t maxnglobalpivot;     /* :714 */
+  int32_t nsearchglobalpivot;  /* :715 */
+  int32_t strictlynested;      /* :717 */
+  int32_t checkconvglobalpivot;/* :719 */
+  int32_t pad_;
+  double tolmarginglobalsearch;/* :716 */
+  uint64_t seed;
+} tci_opts;
+
+typedef struct tci_ctx tci_ctx;
+typedef struct tci_solve tci_solve;
+typedef struct tci_server tci_server;
+
+/* Fill `o` with the reference's defaults (tensorci2.jl:700-720). */
+void tci_opts_default(tci_opts* o);
+
+/* Library / device set-up.  hbm_budget = 0: no limit beyond the device. */
+int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out);
+int tci_ctx_destroy(tci_ctx* ctx);
+const char* tci_last_error(void);
+/* Name -> id of a registered device function ("lorentz", "served", ...). */
+int tci_f_lookup(const char* name, int* fid);
+
+/* ---- TensorCI2 (tensorci2.jl:6-72) ------------------------------------- */
+/* TensorCI2{Float64}(f, localdims, initialpivots) (tensorci2.jl:42-53).
+ * pivots: np x L row-major, 1-based. */
+int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid,
+                     const double* fparams, int64_t nparams, const int64_t* pivots, int64_t np,
+                     tci_solve** out);
+int tci_solve_destroy(tci_solve* s);
+
+/* crossinterpolate2(Float64, f, localdims, initialpivots; opts...)
+ * (tensorci2.jl:943-953): constructor + optimize!. */
+int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid,
+                          const double* fparams, int64_t nparams, const int64_t* pivots,
+                          int64_t np, const tci_opts* opts, tci_solve** out);
+
+/* optimize!(tci, f; opts...) (tensorci2.jl:700-850). */
+int tci_optimize(tci_solve* s, const tci_opts* opts);
+
+/* updatepivots!(tci, b, f, leftorthogonal; reltol, abstol, maxbonddim)
+ * (tensorci2.jl:510-607), pivotsearch=:full, no extra index sets; b 1-based. */
+int tci_updatepivots(tci_solve* s, int32_t b, int32_t leftorthogonal, double reltol,
+                     double abstol, int64_t maxbonddim);
+
+/* sweep2site!(tci, f, niter; iter1, abstol, maxbonddim, sweepstrategy,
+ * strictlynested, fillsitetensors) (tensorci2.jl:855-916). */
+int tci_sweep2site(tci_solve* s, int32_t niter, int32_t iter1, double abstol, int64_t maxbonddim,
+                   int32_t sweepstrategy, int32_t strictlynested, int32_t fillsitetensors);
+
+/* sweep1site!(tci, f, :forward/:backward; reltol, abstol, maxbonddim,
+ * updatetensors) (tensorci2.jl:402-461). */
+int tci_sweep1site(tci_solve* s, int32_t forward, double reltol, double abstol,
+                   int64_t maxbonddim, int32_t updatetensors);
+
+/* fillsitetensors!(tci, f) (globalsearch.jl:97-103). */
+int tci_fillsitetensors(tci_solve* s);
+
+/* addglobalpivots!(tci, pivots) (tensorci2.jl:193-213). */
+int tci_addglobalpivots(tci_solve* s, const int64_t* pivots, int64_t np);
+
+/* addglobalpivots1sitesweep!(tci, f, pivots; reltol, abstol, maxbonddim)
+ * (tensorci2.jl:219-229). */
+int tci_addglobalpivots1sitesweep(tci_solve* s, const int64_t* pivots, int64_t np, double reltol,
+                                  double abstol, int64_t maxbonddim);
+
+/* Accessors.  linkdims (tensorci2.jl:83-85): L-1 values. */
+int tci_solve_length(const tci_solve* s, int32_t* L);
+int tci_linkdims(const tci_solve* s, int64_t* out);
+double tci_maxsamplevalue(const tci_solve* s);
+/* Iset[b], Jset[b] for 1-based site b: I is nI x (b-1), J is nJ x (L-b), row-major,
+ * 1-based.  Pass NULL arrays to query nI/nJ only. */
+int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t* J, int64_t* nJ);
+/* Site tensor b (1-based), column-major r_{b-1} x d_b x r_b; dims[3] out.
+ * Pass NULL `out` to query dims.  Fails if site tensors are invalidated. */
+int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims);
+/* pivoterrors (length *npe) and bonderrors (L-1) (tensorci2.jl:13-16). */
+int tci_get_errors(const tci_solve* s, double* pivoterrors, int64_t* npe, double* bonderrors);
+/* ranks, errors (normalised) and number of global pivots per iteration of the
+ * last optimize! (tensorci2.jl:849). */
+int tci_get_history(const tci_solve* s, int64_t* ranks, double* errors, int64_t* nglobal,
+                    int64_t* niter);
+/* Number of function evaluations performed on the device so far. */
+int64_t tci_solve_nfeval(const tci_solve* s);
+
+/* ---- TensorTrain (abstracttensortrain.jl:124-199) ---------------------- */
+/* evaluate(tt, indexset) for np points (np x L, 1-based) of the solve's train, FP64. */
+int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out);
+/* sum(tt) (abstracttensortrain.jl:191-199), FP64. */
+int tci_sum(tci_solve* s, double* out);
+
+/* Batch evaluation of a registered f at np points (np x L, 1-based) on the
+ * device: the BatchEvaluator call of batcheval.jl:67-83 with M = L. */
+int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,
+              const int64_t* localdims, const int64_t* points, int64_t np, double* out);
+
+/* convergencecriterion (tensorci2.jl:609-628); host only, returns 1 or 0. */
+int tci_convergencecriterion(const int64_t* ranks, const double* errors, const int64_t* nglobalpivots,
+                             int64_t n, double tolerance, int64_t maxbonddim, int64_t ncheckhistory,
+                             int32_t checkconvglobalpivot);
+
+/* ---- batched solves and serving ---------------------------------------- */
+/* One request of a batch: crossinterpolate2 with initial pivot all ones. */
+typedef struct tci_request {
+  int32_t L, fid;
+  const int64_t* localdims;
+  const double* fparams;
+  int64_t nparams;
+  tci_opts opts;
+} tci_request;
+
+/* Solve `n` requests together: every engine step batches the current sweep
+ * stage of all live solves into one launch.  max_live caps concurrent solves
+ * (0 = all).  out[i] receives solve i (caller destroys). */
+int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* reqs,
+                                  int64_t max_live, tci_solve** out);
+
+/* Continuous-batching server over a request stream with arrival times
+ * (seconds from start).  Requests are admitted as they arrive while live
+ * solves and the HBM estimate allow (L*d^2*r_max^2 doubles per solve);
+ * completed solves are released.  latency[i] = completion - arrival,
+ * rank[i] = final rank.  Returns total wall seconds in *wall. */
+int tci_serve_run(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival,
+                  int64_t max_live, double* latency, int64_t* rank, double* wall);
+
+/* ---- rrLU (matrixlu.jl:194-225) ---------------------------------------- */
+/* rrlu(A; maxrank, reltol, abstol, leftorthogonal) on a host matrix (m x n,
+ * column-major; copied).  rowperm (m), colperm (n): full 1-based permutations;
+ * L (m x npivot) and U (npivot x n) column-major with capacities m*min(m,n) and
+ * min(m,n)*n; either may be NULL.  maxrank <= 0 means typemax(Int). */
+int tci_rrlu(tci_ctx* ctx, const double* A, int64_t m, int64_t n, int64_t maxrank, double reltol,
+             double abstol, int32_t leftorthogonal, int64_t* rowperm, int64_t* colperm, double* L,
+             double* U, int64_t* npivot, double* error);
+
+/* Many independent rrLUs (host buffers).  Matrix i is at A + offsets[i]
+ * (column-major ms[i] x ns[i]).  Outputs: npivots[i], errors[i] and the first
+ * npivot entries of the 1-based row/col pivot lists at piv + piv_offsets[i]
+ * (rows then cols, 2*min(maxrank, m, n) capacity each matrix). */
+int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t* offsets,
+                     const int64_t* ms, const int64_t* ns, int64_t maxrank, double reltol,
+                     double abstol, int32_t leftorthogonal, int64_t* piv, const int64_t* piv_offsets,
+                     int64_t* npivots, double* errors);
+
+/* ---- context utilities --------------------------------------------------- */
+/* cudaStream_t of the context, as an integer. */
+uintptr_t tci_ctx_stream(tci_ctx* ctx);
+int tci_ctx_synchronize(tci_ctx* ctx);
+/* Engine counters since the last reset: steps, kernel launches, tasks, kernel
+ * milliseconds (CUDA events around each step kernel on the context stream),
+ * function evaluations and rank-1 update elements. */
+typedef struct tci_stats {
+  int64_t steps, launches, tasks;
+  double kernel_ms;
+  int64_t feval, lu_updates;
+  int64_t h2d_bytes, d2h_bytes;
+} tci_stats;
+int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
+
+/* Measured FP64 throughput of the current device (operations per second) for
+ * separate multiply+subtract and for fused multiply-add; the roofline
+ * denominator of the FP64-bound kernels.  No reference counterpart. */
+int tci_fp64_peak(uintptr_t stream, double* ops_separate, double* ops_fused);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TCI_GB300_H */

@@ -1,0 +1,390 @@
+"""ctypes bindings of the CPU oracle (test infrastructure only).
+
+The oracle is a C++ restatement of TensorCrossInterpolation.jl's TCI2 path
+(oracle/tci_oracle.cpp).  Only the tests, the smoke check and the CPU-baseline
+legs of bench.py use this module, as the checker or the timed CPU baseline.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+F_LORENTZ, F_SERVED, F_QTT1D, F_QTT2D, F_DENSE = 1, 2, 3, 4, 5
+FUNCTION_IDS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5}
+
+I64P = ctypes.POINTER(ctypes.c_int64)
+F64P = ctypes.POINTER(ctypes.c_double)
+I32P = ctypes.POINTER(ctypes.c_int32)
+
+
+class Opts(ctypes.Structure):
+    """optimize! keyword arguments (tensorci2.jl:700-720)."""
+    _fields_ = [
+        ("tolerance", ctypes.c_double),
+        ("maxbonddim", ctypes.c_int64),
+        ("maxiter", ctypes.c_int64),
+        ("sweepstrategy", ctypes.c_int32),
+        ("normalizeerror", ctypes.c_int32),
+        ("ncheckhistory", ctypes.c_int32),
+        ("maxnglobalpivot", ctypes.c_int32),
+        ("nsearchglobalpivot", ctypes.c_int32),
+        ("strictlynested", ctypes.c_int32),
+        ("checkconvglobalpivot", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("tolmarginglobalsearch", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
+
+
+def make_opts(tolerance=1e-8, maxbonddim=None, maxiter=20, sweepstrategy="backandforth",
+              normalizeerror=True, ncheckhistory=3, maxnglobalpivot=5, nsearchglobalpivot=5,
+              tolmarginglobalsearch=10.0, strictlynested=False, checkconvglobalpivot=True, seed=0):
+    o = Opts()
+    o.tolerance = tolerance
+    o.maxbonddim = 0 if maxbonddim is None else int(maxbonddim)
+    o.maxiter = int(maxiter)
+    o.sweepstrategy = SWEEP[sweepstrategy]
+    o.normalizeerror = int(bool(normalizeerror))
+    o.ncheckhistory = int(ncheckhistory)
+    o.maxnglobalpivot = int(maxnglobalpivot)
+    o.nsearchglobalpivot = int(nsearchglobalpivot)
+    o.strictlynested = int(bool(strictlynested))
+    o.checkconvglobalpivot = int(bool(checkconvglobalpivot))
+    o.tolmarginglobalsearch = float(tolmarginglobalsearch)
+    o.seed = int(seed)
+    return o
+
+
+def build():
+    src = os.path.join(HERE, "tci_oracle.cpp")
+    if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", HERE])
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_rrlu.argtypes = [F64P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_int, I64P, I64P, F64P, F64P, I64P, F64P]
+        L.orc_luci.argtypes = [F64P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
+                               ctypes.c_double, ctypes.c_int, F64P, F64P, I64P]
+        L.orc_rrlu_batched.argtypes = [ctypes.c_int64, F64P, I64P, I64P, I64P, ctypes.c_int64,
+                                       ctypes.c_double, ctypes.c_double, ctypes.c_int, I64P, I64P,
+                                       I64P, F64P, ctypes.c_int]
+        L.orc_feval.argtypes = [ctypes.c_int, F64P, ctypes.c_int64, ctypes.c_int, I64P, ctypes.c_int64,
+                                F64P]
+        L.orc_tci_new.restype = ctypes.c_void_p
+        L.orc_tci_new.argtypes = [ctypes.c_int, I64P, ctypes.c_int, F64P, ctypes.c_int64, I64P,
+                                  ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+        L.orc_crossinterpolate2.restype = ctypes.c_void_p
+        L.orc_crossinterpolate2.argtypes = [ctypes.c_int, I64P, ctypes.c_int, F64P, ctypes.c_int64, I64P,
+                                            ctypes.c_int64, ctypes.POINTER(Opts),
+                                            ctypes.POINTER(ctypes.c_int)]
+        L.orc_tci_free.argtypes = [ctypes.c_void_p]
+        L.orc_tci_optimize.argtypes = [ctypes.c_void_p, ctypes.POINTER(Opts)]
+        L.orc_tci_updatepivots.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int64]
+        L.orc_tci_sweep2site.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                         ctypes.c_int64, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_tci_sweep1site.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                         ctypes.c_int64, ctypes.c_int]
+        L.orc_tci_fillsitetensors.argtypes = [ctypes.c_void_p]
+        L.orc_tci_addglobalpivots.argtypes = [ctypes.c_void_p, I64P, ctypes.c_int64]
+        L.orc_tci_addglobalpivots1sitesweep.argtypes = [ctypes.c_void_p, I64P, ctypes.c_int64,
+                                                        ctypes.c_double, ctypes.c_double,
+                                                        ctypes.c_int64]
+        L.orc_tci_L.argtypes = [ctypes.c_void_p]
+        L.orc_tci_maxsample.argtypes = [ctypes.c_void_p]
+        L.orc_tci_maxsample.restype = ctypes.c_double
+        L.orc_tci_nfeval.argtypes = [ctypes.c_void_p]
+        L.orc_tci_nfeval.restype = ctypes.c_int64
+        L.orc_tci_linkdims.argtypes = [ctypes.c_void_p, I64P]
+        L.orc_tci_sets.argtypes = [ctypes.c_void_p, ctypes.c_int, I64P, I64P, I64P, I64P]
+        L.orc_tci_core.argtypes = [ctypes.c_void_p, ctypes.c_int, F64P, I64P]
+        L.orc_tci_errors.argtypes = [ctypes.c_void_p, F64P, I64P, F64P]
+        L.orc_tci_history.argtypes = [ctypes.c_void_p, I64P, F64P, I64P, I64P]
+        L.orc_tci_evaluate.argtypes = [ctypes.c_void_p, I64P, ctypes.c_int64, F64P]
+        L.orc_tci_sum.argtypes = [ctypes.c_void_p]
+        L.orc_tci_sum.restype = ctypes.c_double
+        L.orc_tt_evaluate.argtypes = [ctypes.c_int, I64P, I64P, F64P, I64P, ctypes.c_int64, F64P]
+        L.orc_tt_sum.argtypes = [ctypes.c_int, I64P, I64P, F64P]
+        L.orc_tt_sum.restype = ctypes.c_double
+        L.orc_convergencecriterion.argtypes = [I64P, F64P, I64P, ctypes.c_int64, ctypes.c_double,
+                                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
+        L.orc_solve_batch.argtypes = [ctypes.c_int64, I32P, I64P, I64P, I32P, F64P, I64P, I64P, F64P,
+                                      I64P, ctypes.POINTER(Opts), I64P, F64P, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"oracle error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc:
+        raise OracleError(rc, lib().orc_last_error().decode())
+
+
+def rrlu(A, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True):
+    """rrlu (matrixlu.jl:217-225).  Returns dict with 0-based permutations."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    k = min(m, n)
+    rp = np.zeros(m, np.int64)
+    cp = np.zeros(n, np.int64)
+    Lb = np.zeros(max(m * k, 1))
+    Ub = np.zeros(max(k * n, 1))
+    npiv = ctypes.c_int64()
+    err = ctypes.c_double()
+    flat = np.ascontiguousarray(A.reshape(-1, order="F"))
+    rc = lib().orc_rrlu(_p(flat, F64P), m, n, 0 if maxrank is None else int(maxrank), reltol, abstol,
+                        int(leftorthogonal), _p(rp, I64P), _p(cp, I64P), _p(Lb, F64P), _p(Ub, F64P),
+                        ctypes.byref(npiv), ctypes.byref(err))
+    K = npiv.value
+    res = dict(rowpermutation=rp, colpermutation=cp, npivot=K, error=err.value,
+               L=Lb[: m * K].reshape((m, K), order="F").copy(),
+               U=Ub[: K * n].reshape((K, n), order="F").copy(), leftorthogonal=leftorthogonal, rc=rc)
+    _check(rc)
+    return res
+
+
+def luci(A, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True):
+    """MatrixLUCI left/right (matrixluci.jl:70-84)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    k = min(m, n)
+    left = np.zeros(max(m * k, 1))
+    right = np.zeros(max(k * n, 1))
+    npiv = ctypes.c_int64()
+    flat = np.ascontiguousarray(A.reshape(-1, order="F"))
+    _check(lib().orc_luci(_p(flat, F64P), m, n, 0 if maxrank is None else int(maxrank), reltol, abstol,
+                          int(leftorthogonal), _p(left, F64P), _p(right, F64P), ctypes.byref(npiv)))
+    K = npiv.value
+    return (left[: m * K].reshape((m, K), order="F"), right[: K * n].reshape((K, n), order="F"))
+
+
+def pivoterrors(res):
+    """pivoterrors(lu) (matrixlu.jl:409-411)."""
+    K = res["npivot"]
+    if res["leftorthogonal"]:
+        d = np.abs(np.diag(res["U"][:K, :K]))
+    else:
+        d = np.abs(np.diag(res["L"][:K, :K]))
+    return np.concatenate([d, [res["error"]]])
+
+
+def left(res):
+    """left(lu; permute=true) (matrixlu.jl:374-382)."""
+    out = np.empty_like(res["L"])
+    out[res["rowpermutation"], :] = res["L"]
+    return out
+
+
+def right(res):
+    """right(lu; permute=true) (matrixlu.jl:384-392)."""
+    out = np.empty_like(res["U"])
+    out[:, res["colpermutation"]] = res["U"]
+    return out
+
+
+def feval(fid, params, points):
+    pts = np.ascontiguousarray(points, dtype=np.int64)
+    prm = np.ascontiguousarray(params if params is not None else [], dtype=np.float64)
+    out = np.zeros(pts.shape[0])
+    lib().orc_feval(int(fid), _p(prm, F64P) if prm.size else None, prm.size, pts.shape[1], _p(pts, I64P),
+                    pts.shape[0], _p(out, F64P))
+    return out
+
+
+class OracleTCI:
+    """TensorCI2 state held by the oracle (tensorci2.jl:6-40)."""
+
+    def __init__(self, handle, L):
+        self.h = ctypes.c_void_p(handle)
+        self.L = L
+
+    def __del__(self):
+        try:
+            lib().orc_tci_free(self.h)
+        except Exception:
+            pass
+
+    @classmethod
+    def new(cls, localdims, fid, params=(), initialpivots=None):
+        L = len(localdims)
+        d = np.ascontiguousarray(localdims, dtype=np.int64)
+        prm = np.ascontiguousarray(params, dtype=np.float64)
+        piv = np.ascontiguousarray(initialpivots if initialpivots is not None else [np.ones(L)],
+                                   dtype=np.int64)
+        rc = ctypes.c_int()
+        h = lib().orc_tci_new(L, _p(d, I64P), int(fid), _p(prm, F64P) if prm.size else None, prm.size,
+                              _p(piv, I64P), piv.shape[0], ctypes.byref(rc))
+        obj = cls(h, L)
+        _check(rc.value)
+        return obj
+
+    def optimize(self, **kw):
+        o = make_opts(**kw)
+        _check(lib().orc_tci_optimize(self.h, ctypes.byref(o)))
+
+    def updatepivots(self, b, leftorthogonal=True, reltol=1e-14, abstol=0.0, maxbonddim=None):
+        _check(lib().orc_tci_updatepivots(self.h, b, int(leftorthogonal), reltol, abstol,
+                                          0 if maxbonddim is None else int(maxbonddim)))
+
+    def sweep2site(self, niter=2, iter1=1, abstol=1e-8, maxbonddim=None, sweepstrategy="backandforth",
+                   strictlynested=False, fillsitetensors=True):
+        _check(lib().orc_tci_sweep2site(self.h, niter, iter1, abstol, 0 if maxbonddim is None else maxbonddim,
+                                        SWEEP[sweepstrategy], int(strictlynested), int(fillsitetensors)))
+
+    def sweep1site(self, forward=True, reltol=1e-14, abstol=0.0, maxbonddim=None, updatetensors=True):
+        _check(lib().orc_tci_sweep1site(self.h, int(forward), reltol, abstol,
+                                        0 if maxbonddim is None else maxbonddim, int(updatetensors)))
+
+    def fillsitetensors(self):
+        _check(lib().orc_tci_fillsitetensors(self.h))
+
+    def addglobalpivots(self, pivots):
+        piv = np.ascontiguousarray(pivots, dtype=np.int64).reshape(-1, self.L)
+        _check(lib().orc_tci_addglobalpivots(self.h, _p(piv, I64P), piv.shape[0]))
+
+    def addglobalpivots1sitesweep(self, pivots, reltol=1e-14, abstol=0.0, maxbonddim=None):
+        piv = np.ascontiguousarray(pivots, dtype=np.int64).reshape(-1, self.L)
+        _check(lib().orc_tci_addglobalpivots1sitesweep(self.h, _p(piv, I64P), piv.shape[0], reltol, abstol,
+                                                       0 if maxbonddim is None else maxbonddim))
+
+    @property
+    def maxsamplevalue(self):
+        return lib().orc_tci_maxsample(self.h)
+
+    @property
+    def nfeval(self):
+        return lib().orc_tci_nfeval(self.h)
+
+    def linkdims(self):
+        out = np.zeros(self.L - 1, np.int64)
+        lib().orc_tci_linkdims(self.h, _p(out, I64P))
+        return out
+
+    def rank(self):
+        return int(self.linkdims().max())
+
+    def sets(self, b):
+        """(Iset[b], Jset[b]) for 1-based site b, as int arrays of 1-based indices."""
+        nI, nJ = ctypes.c_int64(), ctypes.c_int64()
+        lib().orc_tci_sets(self.h, b, None, ctypes.byref(nI), None, ctypes.byref(nJ))
+        I = np.zeros((nI.value, b - 1), np.int64)
+        J = np.zeros((nJ.value, self.L - b), np.int64)
+        lib().orc_tci_sets(self.h, b, _p(I, I64P), ctypes.byref(nI), _p(J, I64P), ctypes.byref(nJ))
+        return I, J
+
+    def core(self, b):
+        dims = np.zeros(3, np.int64)
+        lib().orc_tci_core(self.h, b, None, _p(dims, I64P))
+        out = np.zeros(int(np.prod(dims)))
+        lib().orc_tci_core(self.h, b, _p(out, F64P) if out.size else None, _p(dims, I64P))
+        return out.reshape(tuple(dims), order="F")
+
+    def cores(self):
+        return [self.core(b) for b in range(1, self.L + 1)]
+
+    def errors(self):
+        n = ctypes.c_int64()
+        lib().orc_tci_errors(self.h, None, ctypes.byref(n), None)
+        pe = np.zeros(n.value)
+        be = np.zeros(self.L - 1)
+        lib().orc_tci_errors(self.h, _p(pe, F64P) if pe.size else None, ctypes.byref(n), _p(be, F64P))
+        return pe, be
+
+    def history(self):
+        n = ctypes.c_int64()
+        lib().orc_tci_history(self.h, None, None, None, ctypes.byref(n))
+        r = np.zeros(n.value, np.int64)
+        e = np.zeros(n.value)
+        g = np.zeros(n.value, np.int64)
+        if n.value:
+            lib().orc_tci_history(self.h, _p(r, I64P), _p(e, F64P), _p(g, I64P), ctypes.byref(n))
+        return r, e, g
+
+    def evaluate(self, points):
+        pts = np.ascontiguousarray(points, dtype=np.int64).reshape(-1, self.L)
+        out = np.zeros(pts.shape[0])
+        lib().orc_tci_evaluate(self.h, _p(pts, I64P), pts.shape[0], _p(out, F64P))
+        return out
+
+    def sum(self):
+        return lib().orc_tci_sum(self.h)
+
+
+def crossinterpolate2(localdims, fid, params=(), initialpivots=None, **kw):
+    """crossinterpolate2 (tensorci2.jl:943-953) -> (OracleTCI, ranks, errors)."""
+    L = len(localdims)
+    d = np.ascontiguousarray(localdims, dtype=np.int64)
+    prm = np.ascontiguousarray(params, dtype=np.float64)
+    piv = np.ascontiguousarray(initialpivots if initialpivots is not None else [np.ones(L)], dtype=np.int64)
+    o = make_opts(**kw)
+    rc = ctypes.c_int()
+    h = lib().orc_crossinterpolate2(L, _p(d, I64P), int(fid), _p(prm, F64P) if prm.size else None,
+                                    prm.size, _p(piv, I64P), piv.shape[0], ctypes.byref(o),
+                                    ctypes.byref(rc))
+    t = OracleTCI(h, L)
+    _check(rc.value)
+    r, e, _ = t.history()
+    return t, r, e
+
+
+def convergencecriterion(ranks, errors, nglobalpivots, tolerance, maxbonddim, ncheckhistory,
+                         checkconvglobalpivot=True):
+    r = np.ascontiguousarray(ranks, np.int64)
+    e = np.ascontiguousarray(errors, np.float64)
+    g = np.ascontiguousarray(nglobalpivots, np.int64)
+    return bool(lib().orc_convergencecriterion(_p(r, I64P), _p(e, F64P), _p(g, I64P), r.size, tolerance,
+                                               maxbonddim, ncheckhistory, int(checkconvglobalpivot)))
+
+
+def tt_evaluate(cores, points):
+    L = len(cores)
+    link = np.array([c.shape[0] for c in cores] + [cores[-1].shape[2]], np.int64)
+    d = np.array([c.shape[1] for c in cores], np.int64)
+    flat = np.ascontiguousarray(np.concatenate([c.reshape(-1, order="F") for c in cores]))
+    pts = np.ascontiguousarray(points, np.int64).reshape(-1, L)
+    out = np.zeros(pts.shape[0])
+    lib().orc_tt_evaluate(L, _p(link, I64P), _p(d, I64P), _p(flat, F64P), _p(pts, I64P), pts.shape[0],
+                          _p(out, F64P))
+    return out
+
+
+def tt_sum(cores):
+    L = len(cores)
+    link = np.array([c.shape[0] for c in cores] + [cores[-1].shape[2]], np.int64)
+    d = np.array([c.shape[1] for c in cores], np.int64)
+    flat = np.ascontiguousarray(np.concatenate([c.reshape(-1, order="F") for c in cores]))
+    return lib().orc_tt_sum(L, _p(link, I64P), _p(d, I64P), _p(flat, F64P))
+
+
+def dense_params(table):
+    """Parameter block of the DENSE function for a column-major table."""
+    table = np.asarray(table, dtype=np.float64)
+    dims = table.shape
+    strides = np.cumprod((1,) + dims[:-1])
+    return np.concatenate([[len(dims)], strides.astype(np.float64), table.reshape(-1, order="F")])

@@ -1,0 +1,600 @@
+// C ABI of libtci_gpu.so (include/tci_gb300.h): thin wrappers that build the
+// solve state, run the coroutine algorithm on the context's engine and copy
+// results into caller buffers.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <optional>
+#include <thread>
+
+#include "engine.h"
+
+using namespace tci;
+
+struct tci_ctx {
+  Engine eng;
+  std::mutex mu;
+  explicit tci_ctx(int dev) : eng(dev) {}
+};
+
+struct tci_solve {
+  tci_ctx* ctx = nullptr;
+  Solve s;
+};
+
+namespace {
+
+int fail(int code, const std::string& msg) {
+  set_error(code, msg);
+  return code;
+}
+
+std::vector<std::vector<uint8_t>> to_pivots(const int64_t* piv, int64_t np, int L, const std::vector<int>& d,
+                                            int* rc) {
+  std::vector<std::vector<uint8_t>> out;
+  *rc = 0;
+  for (int64_t p = 0; p < np; ++p) {
+    std::vector<uint8_t> v(L);
+    for (int q = 0; q < L; ++q) {
+      int64_t x = piv[p * L + q];
+      if (x < 1 || x > d[q]) {
+        *rc = fail(TCI_ERR_ARG, "pivot index out of range");
+        return {};
+      }
+      v[q] = (uint8_t)(x - 1);
+    }
+    out.push_back(v);
+  }
+  return out;
+}
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// HBM estimate used for admission: L * d^2 * r_max^2 doubles.
+double solve_estimate_bytes(const tci_request& r) {
+  double dmax = 1;
+  for (int q = 0; q < r.L; ++q) dmax = std::max<double>(dmax, (double)r.localdims[q]);
+  double rmax = r.opts.maxbonddim > 0 ? (double)r.opts.maxbonddim : 1e9;
+  double full = 1;  // d^(L/2) bound on the rank
+  for (int q = 0; q < r.L / 2; ++q) full = std::min(full * dmax, 1e9);
+  rmax = std::min(rmax, full);
+  return (double)r.L * dmax * dmax * rmax * rmax * 8.0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void tci_opts_default(tci_opts* o) {
+  std::memset(o, 0, sizeof(*o));
+  o->tolerance = 1e-8;
+  o->maxbonddim = 0;
+  o->maxiter = 20;
+  o->sweepstrategy = TCI_SWEEP_BACKANDFORTH;
+  o->normalizeerror = 1;
+  o->ncheckhistory = 3;
+  o->maxnglobalpivot = 5;
+  o->nsearchglobalpivot = 5;
+  o->strictlynested = 0;
+  o->checkconvglobalpivot = 1;
+  o->tolmarginglobalsearch = 10.0;
+  o->seed = 0;
+}
+
+const char* tci_last_error(void) { return last_message(); }
+
+int tci_f_lookup(const char* name, int* fid) {
+  static const struct {
+    const char* n;
+    int id;
+  } tab[] = {{"lorentz", TCI_F_LORENTZ}, {"served", TCI_F_SERVED}, {"qtt1d", TCI_F_QTT1D},
+             {"qtt2d", TCI_F_QTT2D},     {"dense", TCI_F_DENSE}};
+  for (auto& e : tab)
+    if (std::strcmp(e.n, name) == 0) {
+      *fid = e.id;
+      return 0;
+    }
+  return fail(TCI_ERR_ARG, std::string("unknown function ") + name);
+}
+
+int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
+  *out = nullptr;
+  auto* c = new tci_ctx(device);
+  int rc = c->eng.init();
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  if (hbm_budget == 0) {
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    hbm_budget = (size_t)(0.8 * (double)fr);
+  }
+  c->eng.hbm_budget = hbm_budget;
+  *out = c;
+  return 0;
+}
+
+int tci_ctx_destroy(tci_ctx* ctx) {
+  delete ctx;
+  return 0;
+}
+
+uintptr_t tci_ctx_stream(tci_ctx* ctx) { return (uintptr_t)ctx->eng.stream(); }
+
+int tci_ctx_synchronize(tci_ctx* ctx) {
+  cudaError_t e = cudaStreamSynchronize(ctx->eng.stream());
+  return e == cudaSuccess ? 0 : fail(TCI_ERR_CUDA, cudaGetErrorString(e));
+}
+
+int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
+  *out = ctx->eng.stats;
+  if (reset) ctx->eng.stats = tci_stats{};
+  return 0;
+}
+
+// ---------------------------------------------------------------- solves
+static int make_solve(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid, const double* fparams,
+                      int64_t nparams, tci_solve** out) {
+  auto* h = new tci_solve();
+  h->ctx = ctx;
+  int rc = solve_init(h->s, L, localdims, fid, fparams, nparams, nullptr, 0);
+  if (rc) {
+    delete h;
+    *out = nullptr;
+    return rc;
+  }
+  *out = h;
+  return 0;
+}
+
+int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid, const double* fparams,
+                     int64_t nparams, const int64_t* pivots, int64_t np, tci_solve** out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  int rc = make_solve(ctx, L, localdims, fid, fparams, nparams, out);
+  if (rc) return rc;
+  auto piv = to_pivots(pivots, np, L, (*out)->s.d, &rc);
+  if (!rc) {
+    CoTask t = co_construct(ctx->eng, (*out)->s, piv);
+    rc = ctx->eng.run(t);
+  }
+  if (rc) {
+    ctx->eng.release_cores((*out)->s);
+    delete *out;
+    *out = nullptr;
+  }
+  return rc;
+}
+
+int tci_solve_destroy(tci_solve* s) {
+  if (!s) return 0;
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  s->ctx->eng.release_cores(s->s);
+  delete s;
+  return 0;
+}
+
+int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid,
+                          const double* fparams, int64_t nparams, const int64_t* pivots, int64_t np,
+                          const tci_opts* opts, tci_solve** out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  int rc = make_solve(ctx, L, localdims, fid, fparams, nparams, out);
+  if (rc) return rc;
+  std::vector<int64_t> ones;
+  if (!pivots || np == 0) {
+    ones.assign(L, 1);
+    pivots = ones.data();
+    np = 1;
+  }
+  auto piv = to_pivots(pivots, np, L, (*out)->s.d, &rc);
+  if (!rc) {
+    tci_opts o;
+    if (opts)
+      o = *opts;
+    else
+      tci_opts_default(&o);
+    CoTask t = co_crossinterpolate2(ctx->eng, (*out)->s, piv, o);
+    rc = ctx->eng.run(t);
+  }
+  if (rc) {
+    ctx->eng.release_cores((*out)->s);
+    delete *out;
+    *out = nullptr;
+  }
+  return rc;
+}
+
+int tci_optimize(tci_solve* s, const tci_opts* opts) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  tci_opts o;
+  if (opts)
+    o = *opts;
+  else
+    tci_opts_default(&o);
+  CoTask t = co_optimize(s->ctx->eng, s->s, o);
+  return s->ctx->eng.run(t);
+}
+
+int tci_updatepivots(tci_solve* s, int32_t b, int32_t leftorthogonal, double reltol, double abstol,
+                     int64_t maxbonddim) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  if (b < 1 || b > s->s.L - 1) return fail(TCI_ERR_ARG, "bond index out of range");
+  CoTask t = co_updatepivots(s->ctx->eng, s->s, b - 1, leftorthogonal != 0, reltol, abstol,
+                             maxbonddim <= 0 ? TYPEMAX : maxbonddim, nullptr, nullptr);
+  return s->ctx->eng.run(t);
+}
+
+int tci_sweep2site(tci_solve* s, int32_t niter, int32_t iter1, double abstol, int64_t maxbonddim,
+                   int32_t sweepstrategy, int32_t strictlynested, int32_t fillsitetensors) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  CoTask t = co_sweep2site(s->ctx->eng, s->s, niter, iter1, abstol, maxbonddim <= 0 ? TYPEMAX : maxbonddim,
+                           sweepstrategy, strictlynested != 0, fillsitetensors != 0);
+  return s->ctx->eng.run(t);
+}
+
+int tci_sweep1site(tci_solve* s, int32_t forward, double reltol, double abstol, int64_t maxbonddim,
+                   int32_t updatetensors) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  CoTask t = co_sweep1site(s->ctx->eng, s->s, forward != 0, reltol, abstol,
+                           maxbonddim <= 0 ? TYPEMAX : maxbonddim, updatetensors != 0);
+  return s->ctx->eng.run(t);
+}
+
+int tci_fillsitetensors(tci_solve* s) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  CoTask t = co_fillsitetensors(s->ctx->eng, s->s);
+  return s->ctx->eng.run(t);
+}
+
+int tci_addglobalpivots(tci_solve* s, const int64_t* pivots, int64_t np) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  int rc = 0;
+  auto piv = to_pivots(pivots, np, s->s.L, s->s.d, &rc);
+  if (rc) return rc;
+  rc = addglobalpivots(s->s, piv);
+  if (!rc && !piv.empty()) s->ctx->eng.release_cores(s->s);
+  return rc;
+}
+
+int tci_addglobalpivots1sitesweep(tci_solve* s, const int64_t* pivots, int64_t np, double reltol,
+                                  double abstol, int64_t maxbonddim) {
+  int rc = tci_addglobalpivots(s, pivots, np);
+  if (rc) return rc;
+  // makecanonical! (tensorci2.jl:463-474)
+  rc = tci_sweep1site(s, 1, 0.0, 0.0, 0, 0);
+  if (!rc) rc = tci_sweep1site(s, 0, reltol, abstol, maxbonddim, 0);
+  if (!rc) rc = tci_sweep1site(s, 1, reltol, abstol, maxbonddim, 1);
+  return rc;
+}
+
+int tci_solve_length(const tci_solve* s, int32_t* L) {
+  *L = s->s.L;
+  return 0;
+}
+
+int tci_linkdims(const tci_solve* s, int64_t* out) {
+  for (int b = 0; b < s->s.L - 1; ++b) out[b] = (int64_t)s->s.Iset[b + 1].n;
+  return 0;
+}
+
+double tci_maxsamplevalue(const tci_solve* s) { return s->s.maxsample; }
+
+int64_t tci_solve_nfeval(const tci_solve* s) { return s->s.nfeval; }
+
+int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t* J, int64_t* nJ) {
+  if (b < 1 || b > s->s.L) return fail(TCI_ERR_ARG, "site index out of range");
+  const IndexSet& Is = s->s.Iset[b - 1];
+  const IndexSet& Js = s->s.Jset[b - 1];
+  *nI = (int64_t)Is.n;
+  *nJ = (int64_t)Js.n;
+  if (I)
+    for (size_t i = 0; i < Is.n; ++i)
+      for (int q = 0; q < Is.len; ++q) I[i * Is.len + q] = (int64_t)Is.at(i)[q] + 1;
+  if (J)
+    for (size_t j = 0; j < Js.n; ++j)
+      for (int q = 0; q < Js.len; ++q) J[j * Js.len + q] = (int64_t)Js.at(j)[q] + 1;
+  return 0;
+}
+
+int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
+  if (b < 1 || b > s->s.L) return fail(TCI_ERR_ARG, "site index out of range");
+  if (!s->s.cores_valid) return fail(TCI_ERR_GENERIC, "site tensors are not available");
+  const Core& c = s->s.cores[b - 1];
+  dims[0] = c.d0;
+  dims[1] = c.d1;
+  dims[2] = c.d2;
+  if (out && c.elems()) {
+    cudaError_t e = cudaMemcpyAsync(out, c.p, c.elems() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    s->ctx->eng.stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->eng.stream());
+    if (e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(e));
+    s->ctx->eng.stats.d2h_bytes += (int64_t)(c.elems() * sizeof(double));
+  }
+  return 0;
+}
+
+int tci_get_errors(const tci_solve* s, double* pivoterrors, int64_t* npe, double* bonderrors) {
+  *npe = (int64_t)s->s.pivoterrors.size();
+  if (pivoterrors) std::copy(s->s.pivoterrors.begin(), s->s.pivoterrors.end(), pivoterrors);
+  if (bonderrors) std::copy(s->s.bonderrors.begin(), s->s.bonderrors.end(), bonderrors);
+  return 0;
+}
+
+int tci_get_history(const tci_solve* s, int64_t* ranks, double* errors, int64_t* nglobal, int64_t* niter) {
+  *niter = (int64_t)s->s.ranks.size();
+  if (ranks) std::copy(s->s.ranks.begin(), s->s.ranks.end(), ranks);
+  if (errors) std::copy(s->s.errors.begin(), s->s.errors.end(), errors);
+  if (nglobal) std::copy(s->s.nglobal.begin(), s->s.nglobal.end(), nglobal);
+  return 0;
+}
+
+int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  int rc = 0;
+  auto piv = to_pivots(points, np, s->s.L, s->s.d, &rc);
+  if (rc) return rc;
+  std::vector<uint8_t> pts;
+  pts.reserve((size_t)np * s->s.L);
+  for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
+  // evaluate in chunks so the result record stays modest
+  const int64_t chunk = 1 << 16;
+  for (int64_t b = 0; b < np; b += chunk) {
+    int64_t n = std::min(chunk, np - b);
+    std::vector<uint8_t> sub(pts.begin() + b * s->s.L, pts.begin() + (b + n) * s->s.L);
+    CoTask t = co_evaluate(s->ctx->eng, s->s, sub, n, nullptr, out + b);
+    rc = s->ctx->eng.run(t);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int tci_sum(tci_solve* s, double* out) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  CoTask t = co_sum(s->ctx->eng, s->s, out);
+  return s->ctx->eng.run(t);
+}
+
+// ---------------------------------------------------------------- batches / serving
+namespace {
+struct Job {
+  tci_solve* solve = nullptr;
+  std::optional<CoTask> task;
+  bool started = false, done = false;
+  double arrival = 0, t_start = 0, t_done = 0;
+  int rc = 0;
+};
+
+// Drive jobs with continuous batching.  arrival==nullptr: all available at t=0.
+int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
+          std::vector<Job>& jobs, bool keep) {
+  Engine& e = ctx->eng;
+  jobs.clear();
+  jobs.resize((size_t)n);
+  if (max_live <= 0) max_live = n;
+  const double t0 = now_s();
+  int64_t next = 0, live = 0, finished = 0;
+  double live_bytes = 0;
+  std::vector<double> est(n);
+  for (int64_t i = 0; i < n; ++i) est[i] = solve_estimate_bytes(reqs[i]);
+  int first_rc = 0;
+  auto finish = [&](Job& j, int64_t i) {
+    j.done = true;
+    j.t_done = now_s() - t0;
+    j.rc = j.task->h.promise().rc;
+    if (j.rc && !first_rc) first_rc = j.rc;
+    j.task.reset();
+    --live;
+    ++finished;
+    live_bytes -= est[i];
+    if (!keep) e.release_cores(j.solve->s);
+  };
+  while (finished < n) {
+    double t = now_s() - t0;
+    while (next < n && live < max_live && (!arrival || arrival[next] <= t) &&
+           (live == 0 || live_bytes + est[next] <= (double)e.hbm_budget)) {
+      Job& j = jobs[next];
+      j.arrival = arrival ? arrival[next] : 0.0;
+      j.t_start = t;
+      const tci_request& r = reqs[next];
+      int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
+      std::vector<std::vector<uint8_t>> piv;
+      if (!rc) piv.push_back(std::vector<uint8_t>(r.L, 0));
+      if (rc) {
+        j.started = j.done = true;
+        j.rc = rc;
+        if (!first_rc) first_rc = rc;
+        ++finished;
+        ++next;
+        continue;
+      }
+      j.task.emplace(co_crossinterpolate2(e, j.solve->s, piv, r.opts));
+      j.started = true;
+      ++live;
+      live_bytes += est[next];
+      j.task->h.resume();
+      if (j.task->h.done()) finish(j, next);
+      ++next;
+    }
+    if (e.idle()) {
+      if (finished >= n) break;
+      if (live == 0 && next < n && arrival) {
+        double wait = arrival[next] - (now_s() - t0);
+        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+        continue;
+      }
+      if (live > 0) return fail(TCI_ERR_GENERIC, "engine stalled with live solves");
+      continue;
+    }
+    int rc = e.step();
+    if (rc) return rc;
+    for (int64_t i = 0; i < next; ++i) {
+      Job& j = jobs[i];
+      if (j.started && !j.done && j.task && j.task->h.done()) finish(j, i);
+    }
+  }
+  return first_rc;
+}
+}  // namespace
+
+int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* reqs, int64_t max_live,
+                                  tci_solve** out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::vector<Job> jobs;
+  int rc = drive(ctx, n, reqs, nullptr, max_live, jobs, true);
+  for (int64_t i = 0; i < n; ++i) out[i] = jobs[i].solve;
+  return rc;
+}
+
+int tci_serve_run(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
+                  double* latency, int64_t* rank, double* wall) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::vector<Job> jobs;
+  double t0 = now_s();
+  int rc = drive(ctx, n, reqs, arrival, max_live, jobs, false);
+  if (wall) *wall = now_s() - t0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (latency) latency[i] = jobs[i].t_done - jobs[i].arrival;
+    if (rank) rank[i] = jobs[i].solve ? solve_rank(jobs[i].solve->s) : -1;
+    if (jobs[i].solve) delete jobs[i].solve;
+  }
+  return rc;
+}
+
+// ---------------------------------------------------------------- f and host helpers
+int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,
+              const int64_t* localdims, const int64_t* points, int64_t np, double* out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  Solve s;
+  int rc = solve_init(s, L, localdims, fid, fparams, nparams, nullptr, 0);
+  if (rc) return rc;
+  auto piv = to_pivots(points, np, L, s.d, &rc);
+  if (rc) return rc;
+  const int64_t chunk = 1 << 16;
+  for (int64_t b = 0; b < np; b += chunk) {
+    int64_t n = std::min(chunk, np - b);
+    std::vector<uint8_t> pts;
+    pts.reserve((size_t)n * L);
+    for (int64_t i = b; i < b + n; ++i) pts.insert(pts.end(), piv[i].begin(), piv[i].end());
+    CoTask t = co_evaluate(ctx->eng, s, pts, n, out + b, nullptr);
+    rc = ctx->eng.run(t);
+    if (rc) return rc;
+  }
+  return 0;
+}
+
+int tci_convergencecriterion(const int64_t* ranks, const double* errors, const int64_t* nglobalpivots,
+                             int64_t n, double tolerance, int64_t maxbonddim, int64_t ncheckhistory,
+                             int32_t checkconvglobalpivot) {
+  std::vector<i64> r(ranks, ranks + n), g(nglobalpivots, nglobalpivots + n);
+  std::vector<double> e(errors, errors + n);
+  return convergencecriterion(r, e, g, tolerance, maxbonddim, ncheckhistory, checkconvglobalpivot != 0) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- rrLU
+int tci_rrlu(tci_ctx* ctx, const double* A, int64_t m, int64_t n, int64_t maxrank, double reltol,
+             double abstol, int32_t leftorthogonal, int64_t* rowperm, int64_t* colperm, double* L, double* U,
+             int64_t* npivot, double* error) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (m < 0 || n < 0 || m > INT32_MAX || n > INT32_MAX || m * n > INT32_MAX)
+    return fail(TCI_ERR_ARG, "matrix size out of range");
+  Engine& e = ctx->eng;
+  Req r;
+  r.t.kind = TCI_TASK_RRLU;
+  r.t.m = (int32_t)m;
+  r.t.n = (int32_t)n;
+  int64_t kmax = std::min<int64_t>(maxrank <= 0 ? INT64_MAX : maxrank, std::min(m, n));
+  r.t.maxrank = (int32_t)kmax;
+  r.t.kcap = (int32_t)kmax;
+  r.t.reltol = reltol;
+  r.t.abstol = abstol;
+  r.t.leftorth = leftorthogonal ? 1 : 0;
+  r.t.post = TCI_POST_FACTORS;
+  r.ain_host = A;
+  // factors (m*n doubles) followed by the full permutations (m + n int32)
+  size_t out_elems = (size_t)(m * n) + ((size_t)(m + n) * 4 + 7) / 8;
+  double* dout = e.alloc_core(out_elems);
+  if (!dout) return fail(TCI_ERR_OOM, "device memory");
+  r.t.core_out = dout;
+  std::vector<Req*> reqs{&r};
+  int rc = e.run_tasks(reqs);
+  if (rc) {
+    e.free_core(dout);
+    return rc;
+  }
+  const tci_result_head* h = r.head();
+  const int K = h->npivot;
+  std::vector<double> F(out_elems);
+  cudaError_t ce = cudaMemcpyAsync(F.data(), dout, out_elems * 8, cudaMemcpyDeviceToHost, e.stream());
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e.stream());
+  e.free_core(dout);
+  if (ce != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  const int32_t* perms = (const int32_t*)(F.data() + m * n);
+  if (rowperm)
+    for (int64_t i = 0; i < m; ++i) rowperm[i] = perms[i] + 1;
+  if (colperm)
+    for (int64_t j = 0; j < n; ++j) colperm[j] = perms[m + j] + 1;
+  // L = tril(A[:, 1:K]), U = triu(A[1:K, :]), unit diagonal on L or U (matrixlu.jl:162-174)
+  if (L)
+    for (int64_t j = 0; j < K; ++j)
+      for (int64_t i = 0; i < m; ++i)
+        L[i + j * m] = i < j ? 0.0 : (i == j && leftorthogonal ? 1.0 : F[i + j * m]);
+  if (U)
+    for (int64_t j = 0; j < n; ++j)
+      for (int64_t i = 0; i < K; ++i)
+        U[i + j * K] = i > j ? 0.0 : (i == j && !leftorthogonal ? 1.0 : F[i + j * m]);
+  if (npivot) *npivot = K;
+  if (error) *error = h->error;
+  if (h->status & TCI_ST_NAN) return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  return 0;
+}
+
+int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t* offsets, const int64_t* ms,
+                     const int64_t* ns, int64_t maxrank, double reltol, double abstol, int32_t leftorthogonal,
+                     int64_t* piv, const int64_t* piv_offsets, int64_t* npivots, double* errors) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  Engine& e = ctx->eng;
+  std::vector<Req> rs((size_t)nmat);
+  std::vector<Req*> ptrs;
+  for (int64_t i = 0; i < nmat; ++i) {
+    Req& r = rs[i];
+    if (ms[i] * ns[i] > INT32_MAX) return fail(TCI_ERR_ARG, "matrix size out of range");
+    r.t.kind = TCI_TASK_RRLU;
+    r.t.m = (int32_t)ms[i];
+    r.t.n = (int32_t)ns[i];
+    int64_t kmax = std::min<int64_t>(maxrank <= 0 ? INT64_MAX : maxrank, std::min(ms[i], ns[i]));
+    r.t.maxrank = (int32_t)kmax;
+    r.t.kcap = (int32_t)kmax;
+    r.t.reltol = reltol;
+    r.t.abstol = abstol;
+    r.t.leftorth = leftorthogonal ? 1 : 0;
+    r.t.post = TCI_POST_NONE;
+    r.ain_host = A + offsets[i];
+    ptrs.push_back(&r);
+  }
+  int rc = e.run_tasks(ptrs);
+  if (rc) return rc;
+  int bad = 0;
+  for (int64_t i = 0; i < nmat; ++i) {
+    const Req& r = rs[i];
+    const tci_result_head* h = r.head();
+    npivots[i] = h->npivot;
+    errors[i] = h->error;
+    if (h->status & TCI_ST_NAN) bad = 1;
+    if (piv) {
+      int64_t* o = piv + piv_offsets[i];
+      for (int k = 0; k < h->npivot; ++k) {
+        o[k] = r.rowperm()[k] + 1;
+        o[r.t.kcap + k] = r.colperm()[k] + 1;
+      }
+    }
+  }
+  if (bad) return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,1003 @@
+// Host engine: index sets, the batched step loop and the TCI2 algorithm written
+// as coroutines.  The algorithm follows tensorci2.jl step by step (citations at
+// each function); every Pi evaluation, LU and site-tensor computation is a GPU
+// task, and the only host work is integer bookkeeping of the pivot index sets,
+// the convergence test and the random start points of the global pivot search.
+#include "engine.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+
+cudaError_t tci_step_configure();
+size_t tci_step_smem_bytes();
+cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
+                            int* counter_dev, int grid, cudaStream_t stream);
+
+namespace tci {
+
+namespace {
+thread_local Error g_err;
+const double QNAN = std::numeric_limits<double>::quiet_NaN();
+
+double jmax(double a, double b) {
+  if (a != a || b != b) return QNAN;
+  return a > b ? a : b;
+}
+inline size_t a16(size_t x) { return (x + 15) & ~(size_t)15; }
+inline size_t a8(size_t x) { return (x + 7) & ~(size_t)7; }
+
+uint64_t hash_bytes(const uint8_t* p, int len) {
+  uint64_t h = 1469598103934665603ULL;
+  for (int i = 0; i < len; ++i) h = (h ^ p[i]) * 1099511628211ULL;
+  return h ^ (h >> 29);
+}
+}  // namespace
+
+void set_error(int code, const std::string& msg) {
+  g_err.code = code;
+  g_err.msg = msg;
+}
+int last_code() { return g_err.code; }
+const char* last_message() { return g_err.msg.c_str(); }
+
+static int fail(int code, const std::string& msg) {
+  set_error(code, msg);
+  return code;
+}
+
+// ---------------------------------------------------------------- index sets
+bool IndexSet::contains(const uint8_t* v) const {
+  for (size_t i = 0; i < n; ++i)
+    if (len == 0 || std::memcmp(at(i), v, (size_t)len) == 0) return true;
+  return false;
+}
+
+IndexSet kron_right(const IndexSet& I, int d) {
+  IndexSet o;
+  o.len = I.len + 1;
+  o.data.reserve(I.n * d * o.len);
+  std::vector<uint8_t> buf(o.len);
+  for (int j = 0; j < d; ++j)
+    for (size_t i = 0; i < I.n; ++i) {
+      if (I.len) std::memcpy(buf.data(), I.at(i), I.len);
+      buf[I.len] = (uint8_t)j;
+      o.push(buf.data());
+    }
+  return o;
+}
+
+IndexSet kron_left(int d, const IndexSet& J) {
+  IndexSet o;
+  o.len = J.len + 1;
+  o.data.reserve(J.n * d * o.len);
+  std::vector<uint8_t> buf(o.len);
+  for (size_t j = 0; j < J.n; ++j)
+    for (int i = 0; i < d; ++i) {
+      buf[0] = (uint8_t)i;
+      if (J.len) std::memcpy(buf.data() + 1, J.at(j), J.len);
+      o.push(buf.data());
+    }
+  return o;
+}
+
+IndexSet set_union(const IndexSet& a, const IndexSet& b) {
+  IndexSet o;
+  o.len = a.len;
+  if (a.len == 0) {  // entries are all the empty multi-index
+    if (a.n + b.n > 0) o.n = 1;
+    return o;
+  }
+  size_t cap = 16;
+  while (cap < 2 * (a.n + b.n) + 1) cap <<= 1;
+  std::vector<int64_t> table(cap, -1);
+  o.data.reserve((a.n + b.n) * a.len);
+  for (const IndexSet* src : {&a, &b})
+    for (size_t i = 0; i < src->n; ++i) {
+      const uint8_t* v = src->at(i);
+      size_t h = hash_bytes(v, a.len) & (cap - 1);
+      bool found = false;
+      while (table[h] >= 0) {
+        if (std::memcmp(o.at((size_t)table[h]), v, a.len) == 0) {
+          found = true;
+          break;
+        }
+        h = (h + 1) & (cap - 1);
+      }
+      if (!found) {
+        table[h] = (int64_t)o.n;
+        o.push(v);
+      }
+    }
+  return o;
+}
+
+IndexSet select(const IndexSet& s, const int32_t* idx, int k) {
+  IndexSet o;
+  o.len = s.len;
+  if (s.len == 0) {
+    o.n = (size_t)k;
+    return o;
+  }
+  o.data.reserve((size_t)k * s.len);
+  for (int i = 0; i < k; ++i) o.push(s.at((size_t)idx[i]));
+  return o;
+}
+
+// ---------------------------------------------------------------- GpuOp
+void GpuOp::await_suspend(std::coroutine_handle<> h) { eng->enqueue(reqs, h, this); }
+int GpuOp::await_resume() const noexcept { return status; }
+
+// ---------------------------------------------------------------- Engine
+Engine::Engine(int device) : device_(device) {}
+
+Engine::~Engine() {
+  if (stream_) cudaStreamSynchronize(stream_);
+  if (hblob_) cudaFreeHost(hblob_);
+  if (hres_) cudaFreeHost(hres_);
+  if (dblob_) cudaFree(dblob_);
+  if (dres_) cudaFree(dres_);
+  if (dwork_) cudaFree(dwork_);
+  if (dcounter_) cudaFree(dcounter_);
+  if (ev0_) cudaEventDestroy(ev0_);
+  if (ev1_) cudaEventDestroy(ev1_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+#define CUDA_TRY(x)                                                             \
+  do {                                                                          \
+    cudaError_t _e = (x);                                                       \
+    if (_e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(_e));   \
+  } while (0)
+
+int Engine::init() {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+    return fail(TCI_ERR_CUDA, "no CUDA device available");
+  if (device_ < 0 || device_ >= ndev) return fail(TCI_ERR_ARG, "invalid device index");
+  CUDA_TRY(cudaSetDevice(device_));
+  CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&ev0_));
+  CUDA_TRY(cudaEventCreate(&ev1_));
+  CUDA_TRY(tci_step_configure());
+  smem_bytes = tci_step_smem_bytes();
+  CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device_));
+  CUDA_TRY(cudaMalloc(&dcounter_, 64));
+  cudaMemPool_t pool;
+  CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, device_));
+  uint64_t thr = UINT64_MAX;
+  CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  return 0;
+}
+
+double* Engine::alloc_core(size_t elems) {
+  if (elems == 0) elems = 1;
+  void* p = nullptr;
+  if (cudaMallocAsync(&p, elems * sizeof(double), stream_) != cudaSuccess) return nullptr;
+  return (double*)p;
+}
+void Engine::free_core(double* p) {
+  if (p) cudaFreeAsync(p, stream_);
+}
+void Engine::release_cores(Solve& s) {
+  for (auto& c : s.cores) {
+    if (c.p) free_core(c.p);
+    c = Core();
+  }
+  s.cores_valid = false;
+}
+
+void Engine::enqueue(std::vector<Req*>& reqs, std::coroutine_handle<> h, GpuOp* op) {
+  Waiter w{h, op, pending_.size(), reqs.size()};
+  for (Req* r : reqs) pending_.push_back(r);
+  waiters_.push_back(w);
+}
+
+int Engine::ensure(size_t blob, size_t res, size_t work) {
+  if (blob > hblob_cap_) {
+    size_t cap = std::max(blob, hblob_cap_ * 2);
+    if (hblob_) cudaFreeHost(hblob_);
+    hblob_ = nullptr;
+    CUDA_TRY(cudaHostAlloc(&hblob_, cap, cudaHostAllocDefault));
+    hblob_cap_ = cap;
+  }
+  if (blob > dblob_cap_) {
+    size_t cap = std::max(blob, dblob_cap_ * 2);
+    if (dblob_) cudaFree(dblob_);
+    dblob_ = nullptr;
+    CUDA_TRY(cudaMalloc(&dblob_, cap));
+    dblob_cap_ = cap;
+  }
+  if (res > hres_cap_) {
+    size_t cap = std::max(res, hres_cap_ * 2);
+    if (hres_) cudaFreeHost(hres_);
+    hres_ = nullptr;
+    CUDA_TRY(cudaHostAlloc(&hres_, cap, cudaHostAllocDefault));
+    hres_cap_ = cap;
+  }
+  if (res > dres_cap_) {
+    size_t cap = std::max(res, dres_cap_ * 2);
+    if (dres_) cudaFree(dres_);
+    dres_ = nullptr;
+    CUDA_TRY(cudaMalloc(&dres_, cap));
+    dres_cap_ = cap;
+  }
+  if (work > dwork_cap_) {
+    size_t cap = std::max(work, dwork_cap_ * 2);
+    if (dwork_) cudaFree(dwork_);
+    dwork_ = nullptr;
+    CUDA_TRY(cudaMalloc(&dwork_, cap * sizeof(double)));
+    dwork_cap_ = cap;
+  }
+  return 0;
+}
+
+// Shared-memory plan of a task; mirrors the SmemCursor use in step_kernel.cu.
+// Returns false if the task cannot run.
+static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
+  const size_t m = (size_t)t.m, n = (size_t)t.n;
+  work_elems = 0;
+  switch (t.kind) {
+    case TCI_TASK_RRLU: {
+      size_t rest = a16(m * 4) + a16(n * 4);
+      if (!t.ain) rest += 2 * a16(m * 8) + 2 * a16(n * 8);
+      if (a16(m * n * 8) + rest <= smem) {
+        t.smem_mode = 1;
+        return true;
+      }
+      t.smem_mode = 0;
+      work_elems = m * n;
+      return rest <= smem;
+    }
+    case TCI_TASK_SITE: {
+      const size_t r = (size_t)t.r;
+      size_t rest = 2 * a16(r * 4) + 4 * a16(r * 8) + 2 * a16(m * 8);
+      size_t want_rows = std::min<size_t>(std::max<size_t>(m, 1), 64);
+      if (a16(r * r * 8) + rest + want_rows * (r * 8 + 8) <= smem) {
+        t.smem_mode = 1;
+        return true;
+      }
+      t.smem_mode = 0;
+      work_elems = r * r;
+      return rest + (r * 8 + 8) <= smem;
+    }
+    case TCI_TASK_CORE:
+      t.smem_mode = 1;
+      return 2 * a16(m * 8) + 2 * a16(n * 8) <= smem;
+    case TCI_TASK_EVAL:
+      t.smem_mode = 1;
+      return (size_t)(TCI_STEP_THREADS / 32) * 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
+    case TCI_TASK_SUM:
+      t.smem_mode = 1;
+      return 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
+    default:
+      return false;
+  }
+}
+
+static size_t result_bytes(const tci_task& t) {
+  size_t h = sizeof(tci_result_head);
+  switch (t.kind) {
+    case TCI_TASK_RRLU:
+    case TCI_TASK_SITE:
+      return a16(h + 2 * a8((size_t)t.kcap * 4) + (size_t)t.kcap * 8);
+    case TCI_TASK_EVAL:
+      return a16(h + 2 * (size_t)t.m * 8);
+    default:
+      return a16(h);
+  }
+}
+
+static int64_t task_cost(const tci_task& t) {
+  const int64_t m = t.m, n = t.n;
+  switch (t.kind) {
+    case TCI_TASK_RRLU:
+      return m * n * (40 + 2 * std::min<int64_t>(t.kcap, 64));
+    case TCI_TASK_SITE:
+      return (int64_t)t.r * t.r * (40 + 2 * t.r) + m * t.r * (40 + 2 * t.r);
+    case TCI_TASK_CORE:
+      return m * n * 40;
+    case TCI_TASK_EVAL:
+      return m * (40 + (int64_t)t.L * t.r * t.r);
+    default:
+      return 1;
+  }
+}
+
+int Engine::step() {
+  if (pending_.empty()) return 0;
+  std::vector<Req*> batch;
+  batch.swap(pending_);
+  std::vector<Waiter> waiters;
+  waiters.swap(waiters_);
+  const size_t nt = batch.size();
+
+  // ---- layout
+  size_t off = a16(nt * sizeof(tci_task));
+  const size_t off_order = off;
+  off = a16(off + nt * sizeof(int));
+  std::vector<size_t> o_params(nt), o_rows(nt), o_cols(nt), o_prows(nt), o_cores(nt), o_ain(nt);
+  std::vector<size_t> o_res(nt), o_work(nt);
+  size_t res_total = 0, work_total = 0;
+  // Plan every task; a task that cannot run fails its own waiter only.
+  std::vector<char> bad(nt, 0);
+  std::vector<size_t> wel(nt, 0);
+  bool anybad = false;
+  for (size_t i = 0; i < nt; ++i)
+    if (!plan_task(batch[i]->t, smem_bytes, wel[i])) {
+      bad[i] = 1;
+      anybad = true;
+    }
+  if (anybad) {
+    std::vector<Req*> good;
+    std::vector<Waiter> goodw, badw;
+    for (auto& w : waiters) {
+      bool wb = false;
+      for (size_t k = w.first; k < w.first + w.count; ++k) wb |= bad[k] != 0;
+      if (wb) {
+        badw.push_back(w);
+      } else {
+        Waiter g = w;
+        g.first = good.size();
+        for (size_t k = w.first; k < w.first + w.count; ++k) good.push_back(batch[k]);
+        goodw.push_back(g);
+      }
+    }
+    set_error(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
+    for (auto& w : badw) {
+      w.op->status = TCI_ERR_TOO_LARGE;
+      w.h.resume();
+    }
+    for (Req* r : good) pending_.push_back(r);
+    for (auto& w : goodw) waiters_.push_back(w);
+    return 0;
+  }
+  for (size_t i = 0; i < nt; ++i) {
+    Req& r = *batch[i];
+    const size_t we = wel[i];
+    o_params[i] = off;
+    off = a16(off + (size_t)r.t.nparams * 8);
+    o_rows[i] = off;
+    off = a16(off + r.rows_bytes);
+    o_cols[i] = off;
+    off = a16(off + r.cols_bytes);
+    o_prows[i] = off;
+    off = a16(off + r.prows_bytes);
+    o_cores[i] = off;
+    off = a16(off + (size_t)r.ncores * sizeof(tci_core_ref));
+    o_ain[i] = off;
+    if (r.ain_host) off = a16(off + (size_t)r.t.m * r.t.n * 8);
+    o_res[i] = res_total;
+    r.res_bytes = result_bytes(r.t);
+    res_total += r.res_bytes;
+    o_work[i] = work_total;
+    work_total += we;
+  }
+  const size_t blob_total = off;
+  int rc = ensure(blob_total, res_total, work_total);
+  if (rc) {
+    for (auto& w : waiters) w.op->status = rc;
+    for (auto& w : waiters) w.h.resume();
+    return rc;
+  }
+
+  // ---- pack
+  tci_task* tasks = (tci_task*)hblob_;
+  for (size_t i = 0; i < nt; ++i) {
+    Req& r = *batch[i];
+    tci_task t = r.t;
+    t.params = (int64_t)o_params[i];
+    t.rows = (int64_t)o_rows[i];
+    t.cols = (int64_t)o_cols[i];
+    t.prows = (int64_t)o_prows[i];
+    t.cores = r.ncores ? (int64_t)o_cores[i] : 0;
+    t.res = (int64_t)o_res[i];
+    t.work = t.smem_mode ? nullptr : dwork_ + o_work[i];
+    if (r.ain_host) t.ain = (const double*)(dblob_ + o_ain[i]);
+    t.cost = task_cost(t);
+    tasks[i] = t;
+    if (t.nparams) std::memcpy(hblob_ + o_params[i], r.params, (size_t)t.nparams * 8);
+    if (r.rows_bytes) std::memcpy(hblob_ + o_rows[i], r.rows, r.rows_bytes);
+    if (r.cols_bytes) std::memcpy(hblob_ + o_cols[i], r.cols, r.cols_bytes);
+    if (r.prows_bytes) std::memcpy(hblob_ + o_prows[i], r.prows, r.prows_bytes);
+    if (r.ncores) std::memcpy(hblob_ + o_cores[i], r.cores, (size_t)r.ncores * sizeof(tci_core_ref));
+    if (r.ain_host) std::memcpy(hblob_ + o_ain[i], r.ain_host, (size_t)r.t.m * r.t.n * 8);
+  }
+  int* order = (int*)(hblob_ + off_order);
+  std::iota(order, order + nt, 0);
+  std::stable_sort(order, order + nt, [&](int a, int b) { return tasks[a].cost > tasks[b].cost; });
+
+  // ---- upload, launch, download
+  CUDA_TRY(cudaMemcpyAsync(dblob_, hblob_, blob_total, cudaMemcpyHostToDevice, stream_));
+  const int grid = std::max(1, std::min<int>((int)nt, num_sms));
+  if (timing) CUDA_TRY(cudaEventRecord(ev0_, stream_));
+  CUDA_TRY(tci_step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid,
+                           stream_));
+  if (timing) CUDA_TRY(cudaEventRecord(ev1_, stream_));
+  CUDA_TRY(cudaMemcpyAsync(hres_, dres_, res_total, cudaMemcpyDeviceToHost, stream_));
+  CUDA_TRY(cudaStreamSynchronize(stream_));
+  if (timing) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    stats.kernel_ms += ms;
+  }
+  stats.steps += 1;
+  stats.launches += 1;
+  stats.tasks += (int64_t)nt;
+  stats.h2d_bytes += (int64_t)blob_total;
+  stats.d2h_bytes += (int64_t)res_total;
+
+  for (size_t i = 0; i < nt; ++i) {
+    Req& r = *batch[i];
+    r.res = hres_ + o_res[i];
+    const tci_task& t = r.t;
+    switch (t.kind) {
+      case TCI_TASK_RRLU: {
+        if (!t.ain) stats.feval += (int64_t)t.m * t.n;
+        int64_t K = r.head()->npivot;
+        for (int64_t k = 1; k < K; ++k) stats.lu_updates += (int64_t)(t.m - k) * (t.n - k);
+      } break;
+      case TCI_TASK_SITE:
+        stats.feval += (int64_t)t.r * t.r + (int64_t)t.m * t.r;
+        for (int64_t k = 1; k < t.r; ++k) stats.lu_updates += (int64_t)(t.r - k) * (t.r - k);
+        break;
+      case TCI_TASK_CORE:
+        stats.feval += (int64_t)t.m * t.n;
+        break;
+      case TCI_TASK_EVAL:
+        stats.feval += t.m;
+        break;
+      default:
+        break;
+    }
+  }
+  for (auto& w : waiters) {
+    w.op->status = 0;
+    w.h.resume();
+  }
+  return 0;
+}
+
+static CoTask co_tasks(Engine& e, std::vector<Req*> reqs) {
+  GpuOp op{&e, reqs};
+  co_await op;
+  co_return op.status;
+}
+
+int Engine::run_tasks(std::vector<Req*>& reqs) {
+  CoTask t = co_tasks(*this, reqs);
+  return run(t);
+}
+
+int Engine::run(CoTask& t) {
+  t.h.resume();
+  while (!t.h.done()) {
+    if (idle()) return fail(TCI_ERR_GENERIC, "engine stalled");
+    int rc = step();
+    if (rc && !t.h.done() && idle()) return rc;
+  }
+  return t.h.promise().rc;
+}
+
+// ---------------------------------------------------------------- TCI2 pieces
+static void updatemaxsample(Solve& s, double maxabs) {
+  // updatemaxsample!/maxabs (tensorci2.jl:397-399, util.jl:1-10)
+  s.maxsample = jmax(std::fabs(s.maxsample), maxabs);
+}
+
+// updatebonderror!/updatepivoterror!/updateerrors! (tensorci2.jl:132-169)
+static void updateerrors(Solve& s, int b, const double* diag, int K, double err) {
+  s.bonderrors[b] = err;
+  size_t ne = (size_t)K + 1;
+  size_t n = std::max(s.pivoterrors.size(), ne);
+  std::vector<double> out(n);
+  for (size_t i = 0; i < n; ++i) {
+    double a = i < s.pivoterrors.size() ? s.pivoterrors[i] : 0.0;
+    double c = i < (size_t)K ? diag[i] : (i == (size_t)K ? err : 0.0);
+    out[i] = jmax(a, c);
+  }
+  s.pivoterrors.swap(out);
+}
+
+static void fill_f(Req& r, const Solve& s) {
+  r.t.fid = s.fid;
+  r.t.nparams = (int32_t)s.params.size();
+  r.t.L = s.L;
+  r.params = s.params.data();
+}
+
+static int clamp_rank(i64 maxrank, size_t m, size_t n) {
+  i64 k = std::min<i64>(maxrank, (i64)std::min(m, n));
+  return (int)std::max<i64>(k, 0);
+}
+
+i64 solve_rank(const Solve& s) {
+  i64 r = 0;
+  for (int b = 1; b < s.L; ++b) r = std::max<i64>(r, (i64)s.Iset[b].n);
+  return r;
+}
+
+int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
+               int64_t nparams, const int64_t*, int64_t) {
+  if (L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
+  if (fid < TCI_F_LORENTZ || fid > TCI_F_DENSE) return fail(TCI_ERR_ARG, "unknown function id");
+  s.L = L;
+  s.d.assign(localdims, localdims + L);
+  for (int x : s.d)
+    if (x < 1 || x > 256) return fail(TCI_ERR_ARG, "local dimensions must be in 1..256");
+  if (fid == TCI_F_SERVED && nparams < 3 + L) return fail(TCI_ERR_ARG, "served f needs 3+L params");
+  if (fid == TCI_F_QTT2D)
+    for (int x : s.d)
+      if (x != 4) return fail(TCI_ERR_ARG, "qtt2d needs local dimension 4");
+  if (fid == TCI_F_QTT1D)
+    for (int x : s.d)
+      if (x != 2) return fail(TCI_ERR_ARG, "qtt1d needs local dimension 2");
+  if (fid == TCI_F_DENSE) {
+    if (nparams < 1 + L || (int)params[0] != L) return fail(TCI_ERR_ARG, "dense f parameter block");
+    int64_t total = 1;
+    for (int x : s.d) total *= x;
+    if (nparams < 1 + L + total) return fail(TCI_ERR_ARG, "dense f table too short");
+  }
+  s.fid = fid;
+  s.params.assign(params, params + nparams);
+  s.Iset.assign(L, IndexSet());
+  s.Jset.assign(L, IndexSet());
+  for (int b = 0; b < L; ++b) {
+    s.Iset[b].len = b;
+    s.Jset[b].len = L - 1 - b;
+  }
+  s.cores.assign(L, Core());
+  s.bonderrors.assign(L - 1, 0.0);
+  s.pivoterrors.clear();
+  return 0;
+}
+
+// addglobalpivots! (tensorci2.jl:193-213); pivots are 0-based byte vectors.
+int addglobalpivots(Solve& s, const std::vector<std::vector<uint8_t>>& pivots) {
+  for (const auto& p : pivots)
+    if ((int)p.size() != s.L)
+      return fail(TCI_ERR_DIM, "Please specify a pivot as one index per leg of the MPS.");
+  for (const auto& p : pivots)
+    for (int b = 0; b < s.L; ++b) {
+      s.Iset[b].push_unique(p.data());
+      s.Jset[b].push_unique(p.data() + b + 1);
+    }
+  return 0;
+}
+
+static void invalidate(Engine& e, Solve& s) { e.release_cores(s); }
+
+// TensorCI2{ValueType}(func, localdims, initialpivots) (tensorci2.jl:42-53)
+CoTask co_construct(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots) {
+  if (pivots.empty()) co_return fail(TCI_ERR_ARG, "initialpivots must not be empty");
+  int rc = addglobalpivots(s, pivots);
+  if (rc) co_return rc;
+  std::vector<uint8_t> pts;
+  for (const auto& p : pivots) pts.insert(pts.end(), p.begin(), p.end());
+  Req r;
+  r.t.kind = TCI_TASK_EVAL;
+  fill_f(r, s);
+  r.t.m = (int32_t)pivots.size();
+  r.t.nl = s.L;
+  r.rows = pts.data();
+  r.rows_bytes = pts.size();
+  GpuOp op{&e, {&r}};
+  co_await op;
+  if (op.status) co_return op.status;
+  double ms = -std::numeric_limits<double>::infinity();
+  for (int i = 0; i < r.t.m; ++i) ms = jmax(ms, std::fabs(r.fvals()[i]));
+  s.nfeval += r.t.m;
+  s.maxsample = ms;
+  if (!(std::fabs(ms) > 0.0)) co_return fail(TCI_ERR_GENERIC, "maxsamplevalue is zero!");
+  invalidate(e, s);
+  co_return 0;
+}
+
+// updatepivots! with pivotsearch=:full (tensorci2.jl:510-551, 599-607).  The
+// site tensors left(luci)/right(luci) of :601-604 are not formed: the next
+// updatepivots! (:524) or fillsitetensors! replaces them before any use.
+CoTask co_updatepivots(Engine& e, Solve& s, int b, bool leftorth, double reltol, double abstol,
+                       i64 maxbonddim, const IndexSet* extraI, const IndexSet* extraJ) {
+  invalidate(e, s);
+  IndexSet emptyI, emptyJ;
+  emptyI.len = b + 1;
+  emptyJ.len = s.L - 1 - b;
+  IndexSet Ic = set_union(kron_right(s.Iset[b], s.d[b]), extraI ? *extraI : emptyI);
+  IndexSet Jc = set_union(kron_left(s.d[b + 1], s.Jset[b + 1]), extraJ ? *extraJ : emptyJ);
+  Req r;
+  r.t.kind = TCI_TASK_RRLU;
+  fill_f(r, s);
+  r.t.m = (int32_t)Ic.n;
+  r.t.n = (int32_t)Jc.n;
+  r.t.nl = Ic.len;
+  r.t.nr = Jc.len;
+  r.t.maxrank = clamp_rank(maxbonddim, Ic.n, Jc.n);
+  r.t.kcap = r.t.maxrank;
+  r.t.reltol = reltol;
+  r.t.abstol = abstol;
+  r.t.leftorth = leftorth ? 1 : 0;
+  r.t.post = TCI_POST_NONE;
+  r.rows = Ic.data.data();
+  r.rows_bytes = Ic.data.size();
+  r.cols = Jc.data.data();
+  r.cols_bytes = Jc.data.size();
+  GpuOp op{&e, {&r}};
+  co_await op;
+  if (op.status) co_return op.status;
+  const tci_result_head* h = r.head();
+  s.nfeval += (i64)Ic.n * (i64)Jc.n;
+  updatemaxsample(s, h->maxabs);
+  if (h->status & TCI_ST_NAN) co_return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  const int K = h->npivot;
+  s.Iset[b + 1] = select(Ic, r.rowperm(), K);
+  s.Jset[b] = select(Jc, r.colperm(), K);
+  updateerrors(s, b, r.diag(), K, h->error);
+  co_return 0;
+}
+
+bool forwardsweep(int strategy, i64 iter) { return strategy == 1 || (strategy == 0 && (iter % 2) == 1); }
+
+// fillsitetensors! (globalsearch.jl:97-103) -> setsitetensor!(tci, f, b)
+// (tensorci2.jl:367-394) for all b in one step.
+CoTask co_fillsitetensors(Engine& e, Solve& s) {
+  const int L = s.L;
+  for (int b = 0; b < L - 1; ++b)
+    if (s.Iset[b + 1].n != s.Jset[b].n)
+      co_return fail(TCI_ERR_GENERIC, "Pivot matrix at bond " + std::to_string(b + 1) + " is not square!");
+  invalidate(e, s);
+  std::vector<IndexSet> Is(L);
+  std::vector<Req> reqs(L);
+  std::vector<Req*> ptrs;
+  for (int b = 0; b < L; ++b) {
+    Is[b] = kron_right(s.Iset[b], s.d[b]);
+    Req& r = reqs[b];
+    fill_f(r, s);
+    r.t.m = (int32_t)Is[b].n;
+    r.t.nl = Is[b].len;
+    r.t.nr = s.Jset[b].len;
+    r.rows = Is[b].data.data();
+    r.rows_bytes = Is[b].data.size();
+    r.cols = s.Jset[b].data.data();
+    r.cols_bytes = s.Jset[b].data.size();
+    Core& c = s.cores[b];
+    c.d0 = (i64)s.Iset[b].n;
+    c.d1 = s.d[b];
+    if (b == L - 1) {
+      r.t.kind = TCI_TASK_CORE;
+      r.t.n = (int32_t)s.Jset[b].n;
+      c.d2 = (i64)s.Jset[b].n;
+    } else {
+      r.t.kind = TCI_TASK_SITE;
+      r.t.r = (int32_t)s.Jset[b].n;
+      r.t.n = r.t.r;
+      r.t.maxrank = r.t.r;
+      r.t.kcap = r.t.r;
+      r.t.leftorth = 1;
+      r.prows = s.Iset[b + 1].data.data();
+      r.prows_bytes = s.Iset[b + 1].data.size();
+      c.d2 = (i64)s.Iset[b + 1].n;
+    }
+    c.p = e.alloc_core(c.elems());
+    if (!c.p) co_return fail(TCI_ERR_OOM, "device memory for site tensors");
+    r.t.core_out = c.p;
+    ptrs.push_back(&r);
+  }
+  GpuOp op{&e, ptrs};
+  co_await op;
+  if (op.status) co_return op.status;
+  for (int b = 0; b < L; ++b) {
+    const tci_result_head* h = reqs[b].head();
+    updatemaxsample(s, h->maxabs);
+    s.nfeval += (i64)reqs[b].t.m * (reqs[b].t.kind == TCI_TASK_SITE ? reqs[b].t.r : reqs[b].t.n);
+    if (h->status & TCI_ST_SINGULAR) co_return fail(TCI_ERR_SINGULAR, "SingularException in setsitetensor!");
+    if (h->status & TCI_ST_NAN) co_return fail(TCI_ERR_NAN, "Error: NaN in tensor T[" + std::to_string(b + 1) + "]");
+  }
+  s.cores_valid = true;
+  co_return 0;
+}
+
+// sweep2site! (tensorci2.jl:855-916)
+CoTask co_sweep2site(Engine& e, Solve& s, int niter, int iter1, double abstol, i64 maxbonddim,
+                     int strategy, bool strictlynested, bool fillsite) {
+  invalidate(e, s);
+  const int n = s.L;
+  for (int iter = iter1; iter < iter1 + niter; ++iter) {
+    std::vector<IndexSet> extraI, extraJ;
+    bool use_extra = !strictlynested && s.has_hist;
+    if (use_extra) {
+      extraI = s.Ihist;
+      extraJ = s.Jhist;
+    }
+    s.Ihist = s.Iset;
+    s.Jhist = s.Jset;
+    s.has_hist = true;
+    s.pivoterrors.clear();
+    if (forwardsweep(strategy, iter)) {
+      for (int b = 0; b < n - 1; ++b)
+        CO_TRY(co_updatepivots(e, s, b, true, 1e-14, abstol, maxbonddim,
+                               use_extra ? &extraI[b + 1] : nullptr, use_extra ? &extraJ[b] : nullptr));
+    } else {
+      for (int b = n - 2; b >= 0; --b)
+        CO_TRY(co_updatepivots(e, s, b, false, 1e-14, abstol, maxbonddim,
+                               use_extra ? &extraI[b + 1] : nullptr, use_extra ? &extraJ[b] : nullptr));
+    }
+  }
+  if (fillsite) CO_TRY(co_fillsitetensors(e, s));
+  co_return 0;
+}
+
+// sweep1site! (tensorci2.jl:402-461)
+CoTask co_sweep1site(Engine& e, Solve& s, bool forward, double reltol, double abstol, i64 maxbonddim,
+                     bool updatetensors) {
+  s.pivoterrors.clear();
+  invalidate(e, s);
+  const int L = s.L;
+  for (int step = 0; step < L - 1; ++step) {
+    const int b = forward ? step : L - 1 - step;
+    IndexSet Is = forward ? kron_right(s.Iset[b], s.d[b]) : s.Iset[b];
+    IndexSet Js = forward ? s.Jset[b] : kron_left(s.d[b], s.Jset[b]);
+    Req r;
+    r.t.kind = TCI_TASK_RRLU;
+    fill_f(r, s);
+    r.t.m = (int32_t)Is.n;
+    r.t.n = (int32_t)Js.n;
+    r.t.nl = Is.len;
+    r.t.nr = Js.len;
+    r.t.maxrank = clamp_rank(maxbonddim, Is.n, Js.n);
+    r.t.kcap = r.t.maxrank;
+    r.t.reltol = reltol;
+    r.t.abstol = abstol;
+    r.t.leftorth = forward ? 1 : 0;
+    r.t.post = updatetensors ? (forward ? TCI_POST_LEFT : TCI_POST_RIGHT) : TCI_POST_NONE;
+    r.rows = Is.data.data();
+    r.rows_bytes = Is.data.size();
+    r.cols = Js.data.data();
+    r.cols_bytes = Js.data.size();
+    double* out = nullptr;
+    size_t cap = 0;
+    if (updatetensors) {
+      cap = forward ? (size_t)Is.n * r.t.kcap : (size_t)r.t.kcap * Js.n;
+      out = e.alloc_core(cap);
+      if (!out) co_return fail(TCI_ERR_OOM, "device memory for site tensors");
+      r.t.core_out = out;
+    }
+    GpuOp op{&e, {&r}};
+    co_await op;
+    if (op.status) co_return op.status;
+    const tci_result_head* h = r.head();
+    s.nfeval += (i64)Is.n * (i64)Js.n;
+    updatemaxsample(s, h->maxabs);
+    if (h->status & TCI_ST_NAN) {
+      if (out) e.free_core(out);
+      co_return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+    }
+    const int K = h->npivot;
+    if (forward) {
+      s.Iset[b + 1] = select(Is, r.rowperm(), K);
+      s.Jset[b] = select(Js, r.colperm(), K);
+    } else {
+      s.Iset[b] = select(Is, r.rowperm(), K);
+      s.Jset[b - 1] = select(Js, r.colperm(), K);
+    }
+    if (updatetensors) {
+      Core& c = s.cores[b];
+      c.p = out;
+      c.d0 = (i64)s.Iset[b].n;
+      c.d1 = s.d[b];
+      c.d2 = (i64)s.Jset[b].n;
+    }
+    updateerrors(s, forward ? b : b - 1, r.diag(), K, h->error);
+  }
+  if (updatetensors) {
+    const int b = forward ? L - 1 : 0;
+    IndexSet Is = kron_right(s.Iset[b], s.d[b]);
+    Req r;
+    r.t.kind = TCI_TASK_CORE;
+    fill_f(r, s);
+    r.t.m = (int32_t)Is.n;
+    r.t.n = (int32_t)s.Jset[b].n;
+    r.t.nl = Is.len;
+    r.t.nr = s.Jset[b].len;
+    r.rows = Is.data.data();
+    r.rows_bytes = Is.data.size();
+    r.cols = s.Jset[b].data.data();
+    r.cols_bytes = s.Jset[b].data.size();
+    Core& c = s.cores[b];
+    c.d0 = (i64)s.Iset[b].n;
+    c.d1 = s.d[b];
+    c.d2 = (i64)s.Jset[b].n;
+    c.p = e.alloc_core(c.elems());
+    if (!c.p) co_return fail(TCI_ERR_OOM, "device memory for site tensors");
+    r.t.core_out = c.p;
+    GpuOp op{&e, {&r}};
+    co_await op;
+    if (op.status) co_return op.status;
+    s.nfeval += (i64)Is.n * (i64)s.Jset[b].n;
+    s.cores_valid = true;
+  }
+  co_return 0;
+}
+
+static void core_table(const Solve& s, std::vector<tci_core_ref>& tab, int& rmax) {
+  tab.resize(s.L);
+  rmax = 1;
+  for (int b = 0; b < s.L; ++b) {
+    const Core& c = s.cores[b];
+    tab[b].p = c.p;
+    tab[b].r0 = (int32_t)c.d0;
+    tab[b].d = (int32_t)c.d1;
+    tab[b].r1 = (int32_t)c.d2;
+    tab[b].pad = 0;
+    rmax = std::max<int>(rmax, (int)std::max(c.d0, c.d2));
+  }
+}
+
+// f and the train at points (np x L, 0-based bytes).  ttout may be null.
+CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np, double* fout,
+                   double* ttout) {
+  if (ttout && !s.cores_valid) co_return fail(TCI_ERR_GENERIC, "site tensors are not available");
+  std::vector<tci_core_ref> tab;
+  int rmax = 1;
+  Req r;
+  r.t.kind = TCI_TASK_EVAL;
+  fill_f(r, s);
+  r.t.m = (int32_t)np;
+  r.t.nl = s.L;
+  r.rows = pts.data();
+  r.rows_bytes = pts.size();
+  if (ttout) {
+    core_table(s, tab, rmax);
+    r.cores = tab.data();
+    r.ncores = s.L;
+    r.t.r = rmax;
+  }
+  GpuOp op{&e, {&r}};
+  co_await op;
+  if (op.status) co_return op.status;
+  if (fout) std::memcpy(fout, r.fvals(), (size_t)np * 8);
+  if (ttout) std::memcpy(ttout, r.ttvals(), (size_t)np * 8);
+  co_return 0;
+}
+
+CoTask co_sum(Engine& e, Solve& s, double* out) {
+  if (!s.cores_valid) co_return fail(TCI_ERR_GENERIC, "site tensors are not available");
+  std::vector<tci_core_ref> tab;
+  int rmax = 1;
+  core_table(s, tab, rmax);
+  Req r;
+  r.t.kind = TCI_TASK_SUM;
+  r.t.L = s.L;
+  r.t.r = rmax;
+  r.cores = tab.data();
+  r.ncores = s.L;
+  GpuOp op{&e, {&r}};
+  co_await op;
+  if (op.status) co_return op.status;
+  *out = r.head()->error;
+  co_return 0;
+}
+
+// DefaultGlobalPivotFinder (globalpivotfinder.jl:143-195): nsearch random start
+// points, a line scan along every site, the point of largest |f - tt| kept when
+// it exceeds abstol * tolmarginglobalsearch.  All f and train evaluations of one
+// search run as one EVAL task.
+CoTask co_globalpivots(Engine& e, Solve& s, double abstol, int nsearch, int maxnglobalpivot,
+                       double tolmargin, std::vector<std::vector<uint8_t>>* found) {
+  found->clear();
+  if (nsearch <= 0) co_return 0;
+  const int L = s.L;
+  std::vector<std::vector<uint8_t>> starts(nsearch, std::vector<uint8_t>(L));
+  for (int q = 0; q < nsearch; ++q)
+    for (int p = 0; p < L; ++p) starts[q][p] = (uint8_t)(tci_rng_uniform1(&s.rng, (uint64_t)s.d[p]) - 1);
+  i64 per = 0;
+  for (int p = 0; p < L; ++p) per += s.d[p];
+  const i64 np = per * nsearch;
+  std::vector<uint8_t> pts((size_t)np * L);
+  size_t k = 0;
+  for (int q = 0; q < nsearch; ++q)
+    for (int p = 0; p < L; ++p)
+      for (int v = 0; v < s.d[p]; ++v) {
+        std::memcpy(&pts[k * L], starts[q].data(), L);
+        pts[k * L + p] = (uint8_t)v;
+        ++k;
+      }
+  std::vector<double> fv(np), tv(np);
+  CO_TRY(co_evaluate(e, s, pts, np, fv.data(), tv.data()));
+  s.nfeval += np;
+  k = 0;
+  for (int q = 0; q < nsearch; ++q) {
+    double best_error = 0.0;
+    size_t best = SIZE_MAX;
+    for (int p = 0; p < L; ++p)
+      for (int v = 0; v < s.d[p]; ++v) {
+        double err = std::fabs(fv[k] - tv[k]);
+        if (err > best_error) {
+          best_error = err;
+          best = k;
+        }
+        ++k;
+      }
+    if (best_error > abstol * tolmargin) {
+      std::vector<uint8_t> bp(L);
+      if (best == SIZE_MAX)
+        bp = starts[q];
+      else
+        std::memcpy(bp.data(), &pts[best * L], L);
+      found->push_back(bp);
+    }
+  }
+  if ((int)found->size() > maxnglobalpivot) found->resize(maxnglobalpivot);
+  co_return 0;
+}
+
+// convergencecriterion (tensorci2.jl:609-628)
+bool convergencecriterion(const std::vector<i64>& ranks, const std::vector<double>& errors,
+                          const std::vector<i64>& ngp, double tolerance, i64 maxbonddim,
+                          i64 ncheckhistory, bool checkconvglobalpivot) {
+  if ((i64)errors.size() < ncheckhistory) return false;
+  const i64 n = ncheckhistory;
+  if (n <= 0) return false;
+  bool allerr = true, allg = true, allmax = true;
+  i64 mn = INT64_MAX;
+  for (i64 i = (i64)ranks.size() - n; i < (i64)ranks.size(); ++i) {
+    allmax &= ranks[i] >= maxbonddim;
+    mn = std::min(mn, ranks[i]);
+  }
+  for (i64 i = (i64)errors.size() - n; i < (i64)errors.size(); ++i) allerr &= errors[i] < tolerance;
+  for (i64 i = (i64)ngp.size() - n; i < (i64)ngp.size(); ++i) allg &= ngp[i] == 0;
+  return (allerr && (checkconvglobalpivot ? allg : true) && mn == ranks.back()) || allmax;
+}
+
+// optimize! (tensorci2.jl:700-850) with DefaultGlobalPivotFinder.
+CoTask co_optimize(Engine& e, Solve& s, tci_opts o) {
+  const double tol = o.tolerance;
+  const i64 maxbonddim = o.maxbonddim <= 0 ? TYPEMAX : o.maxbonddim;
+  if (o.nsearchglobalpivot > 0 && o.nsearchglobalpivot < o.maxnglobalpivot)
+    co_return fail(TCI_ERR_GENERIC, "nsearchglobalpivot < maxnglobalpivot!");
+  if (maxbonddim >= TYPEMAX && tol <= 0)
+    co_return fail(TCI_ERR_ARG,
+                   "Specify either tolerance > 0 or some maxbonddim; otherwise, the convergence "
+                   "criterion is not reachable!");
+  tci_rng_seed(&s.rng, o.seed);
+  s.opts = o;
+  s.ranks.clear();
+  s.errors.clear();
+  s.nglobal.clear();
+  std::vector<std::vector<uint8_t>> gp;
+  for (i64 iter = 1; iter <= o.maxiter; ++iter) {
+    double errnorm = o.normalizeerror ? s.maxsample : 1.0;
+    double abstol = tol * errnorm;
+    CO_TRY(co_sweep2site(e, s, 2, 1, abstol, maxbonddim, o.sweepstrategy, o.strictlynested != 0, true));
+    double perr = *std::max_element(s.bonderrors.begin(), s.bonderrors.end());
+    s.errors.push_back(perr);
+    CO_TRY(co_globalpivots(e, s, abstol, o.nsearchglobalpivot, o.maxnglobalpivot, o.tolmarginglobalsearch,
+                           &gp));
+    int rc = addglobalpivots(s, gp);
+    if (rc) co_return rc;
+    if (!gp.empty()) invalidate(e, s);
+    s.nglobal.push_back((i64)gp.size());
+    s.ranks.push_back(solve_rank(s));
+    if (convergencecriterion(s.ranks, s.errors, s.nglobal, abstol, maxbonddim, o.ncheckhistory,
+                             o.checkconvglobalpivot != 0))
+      break;
+  }
+  double errnorm = o.normalizeerror ? s.maxsample : 1.0;
+  double abstol = tol * errnorm;
+  CO_TRY(co_sweep1site(e, s, true, 1e-14, abstol, maxbonddim, true));
+  for (int b = 0; b < s.L - 1; ++b)  // _sanitycheck (globalsearch.jl:106-112)
+    if (s.Iset[b + 1].n != s.Jset[b].n)
+      co_return fail(TCI_ERR_GENERIC, "Pivot matrix at bond " + std::to_string(b + 1) + " is not square!");
+  for (auto& x : s.errors) x = x / errnorm;
+  co_return 0;
+}
+
+// crossinterpolate2 (tensorci2.jl:943-953)
+CoTask co_crossinterpolate2(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots, tci_opts o) {
+  CO_TRY(co_construct(e, s, std::move(pivots)));
+  CO_TRY(co_optimize(e, s, o));
+  co_return 0;
+}
+
+}  // namespace tci

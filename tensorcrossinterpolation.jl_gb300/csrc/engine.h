@@ -1,0 +1,237 @@
+// Host engine of the TCI2 sweep: solve state, index sets, the coroutine
+// machinery that lets each solve be written as straight-line code, and the
+// step loop that batches the GPU tasks of all live solves into one launch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <coroutine>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/tci_gb300.h"
+#include "tci_rng.h"
+#include "tci_tasks.h"
+
+namespace tci {
+
+using i64 = int64_t;
+const i64 TYPEMAX = INT64_MAX;
+
+// Error with the reference's exception message.
+struct Error {
+  int code = 0;
+  std::string msg;
+};
+void set_error(int code, const std::string& msg);
+int last_code();
+
+// A set of multi-indices of equal length, stored flat (0-based uint8 values).
+// Order of insertion is kept (the reference's Vector{MultiIndex}).
+struct IndexSet {
+  int len = 0;
+  size_t n = 0;
+  std::vector<uint8_t> data;
+  const uint8_t* at(size_t i) const { return data.data() + i * (size_t)len; }
+  void push(const uint8_t* v) {
+    data.insert(data.end(), v, v + len);
+    ++n;
+  }
+  bool contains(const uint8_t* v) const;
+  void push_unique(const uint8_t* v) {
+    if (!contains(v)) push(v);
+  }
+};
+IndexSet kron_right(const IndexSet& I, int d);   // kronecker(Iset, d) (tensorci2.jl:315-320)
+IndexSet kron_left(int d, const IndexSet& J);    // kronecker(d, Jset) (tensorci2.jl:322-327)
+IndexSet set_union(const IndexSet& a, const IndexSet& b);  // Base.union
+IndexSet select(const IndexSet& s, const int32_t* idx, int k);
+
+// ------------------------------------------------------------ coroutines
+struct CoTask {
+  struct promise_type {
+    std::coroutine_handle<> cont;
+    int rc = 0;
+    CoTask get_return_object() {
+      return CoTask{std::coroutine_handle<promise_type>::from_promise(*this)};
+    }
+    std::suspend_always initial_suspend() noexcept { return {}; }
+    struct Final {
+      bool await_ready() noexcept { return false; }
+      std::coroutine_handle<> await_suspend(std::coroutine_handle<promise_type> h) noexcept {
+        auto c = h.promise().cont;
+        return c ? c : std::noop_coroutine();
+      }
+      void await_resume() noexcept {}
+    };
+    Final final_suspend() noexcept { return {}; }
+    void return_value(int v) { rc = v; }
+    void unhandled_exception() { rc = TCI_ERR_GENERIC; }
+  };
+  std::coroutine_handle<promise_type> h;
+  explicit CoTask(std::coroutine_handle<promise_type> hh) : h(hh) {}
+  CoTask(CoTask&& o) noexcept : h(o.h) { o.h = {}; }
+  CoTask(const CoTask&) = delete;
+  ~CoTask() {
+    if (h) h.destroy();
+  }
+  bool await_ready() { return false; }
+  std::coroutine_handle<> await_suspend(std::coroutine_handle<> parent) {
+    h.promise().cont = parent;
+    return h;
+  }
+  int await_resume() { return h.promise().rc; }
+};
+
+#define CO_TRY(expr)              \
+  do {                            \
+    int _rc = co_await (expr);    \
+    if (_rc) co_return _rc;       \
+  } while (0)
+
+// One GPU task as the host sees it.
+struct Req {
+  tci_task t{};
+  const uint8_t* rows = nullptr;
+  size_t rows_bytes = 0;
+  const uint8_t* cols = nullptr;
+  size_t cols_bytes = 0;
+  const uint8_t* prows = nullptr;
+  size_t prows_bytes = 0;
+  const double* params = nullptr;
+  const tci_core_ref* cores = nullptr;
+  int ncores = 0;
+  const double* ain_host = nullptr;  // packed into the upload blob
+  const char* res = nullptr;         // host copy of the result record after the step
+  size_t res_bytes = 0;
+  const tci_result_head* head() const { return (const tci_result_head*)res; }
+  const int32_t* rowperm() const { return (const int32_t*)(res + sizeof(tci_result_head)); }
+  const int32_t* colperm() const {
+    return (const int32_t*)(res + sizeof(tci_result_head) + ((size_t)t.kcap * 4 + 7) / 8 * 8);
+  }
+  const double* diag() const {
+    return (const double*)(res + sizeof(tci_result_head) + 2 * (((size_t)t.kcap * 4 + 7) / 8 * 8));
+  }
+  const double* fvals() const { return (const double*)(res + sizeof(tci_result_head)); }
+  const double* ttvals() const { return fvals() + t.m; }
+};
+
+class Engine;
+
+struct GpuOp {
+  Engine* eng;
+  std::vector<Req*> reqs;
+  bool await_ready() const noexcept { return reqs.empty(); }
+  void await_suspend(std::coroutine_handle<> h);
+  int await_resume() const noexcept;
+  int status = 0;
+};
+
+// Device copy of one site tensor.
+struct Core {
+  double* p = nullptr;
+  i64 d0 = 0, d1 = 0, d2 = 0;
+  size_t elems() const { return (size_t)(d0 * d1 * d2); }
+};
+const char* last_message();
+
+struct Solve {
+  int L = 0;
+  std::vector<int> d;
+  int fid = 0;
+  std::vector<double> params;
+  std::vector<IndexSet> Iset, Jset;       // Iset[b]: length b; Jset[b]: length L-1-b
+  std::vector<IndexSet> Ihist, Jhist;     // last snapshot pushed by sweep2site!
+  bool has_hist = false;
+  std::vector<Core> cores;
+  bool cores_valid = false;
+  std::vector<double> pivoterrors, bonderrors;
+  double maxsample = 0.0;
+  std::vector<i64> ranks, nglobal;
+  std::vector<double> errors;
+  i64 nfeval = 0;
+  tci_rng rng;
+  tci_opts opts{};
+  // bookkeeping for serving
+  int rc = 0;
+  std::string msg;
+  double t_arrival = 0, t_done = 0;
+  i64 id = -1;
+};
+
+class Engine {
+ public:
+  explicit Engine(int device);
+  ~Engine();
+  int init();
+  cudaStream_t stream() const { return stream_; }
+
+  // Queue tasks for the next step and remember the coroutine to resume.
+  void enqueue(std::vector<Req*>& reqs, std::coroutine_handle<> h, GpuOp* op);
+  bool idle() const { return pending_.empty(); }
+  // Run one batched step: pack, upload, launch, download, resume.
+  int step();
+  // Drive a single coroutine (and any others already queued) to completion.
+  int run(CoTask& t);
+
+  // Device memory for site tensors (stream-ordered pool).
+  double* alloc_core(size_t elems);
+  void free_core(double* p);
+  void release_cores(Solve& s);
+  // Run a list of tasks outside any solve (rrLU entry points).
+  int run_tasks(std::vector<Req*>& reqs);
+
+  tci_stats stats{};
+  bool timing = true;
+  size_t smem_bytes = 0;
+  int num_sms = 0;
+  size_t hbm_budget = 0;
+
+ private:
+  struct Waiter {
+    std::coroutine_handle<> h;
+    GpuOp* op;
+    size_t first, count;
+  };
+  int ensure(size_t blob, size_t res, size_t work);
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+  std::vector<Req*> pending_;
+  std::vector<Waiter> waiters_;
+  char* hblob_ = nullptr;
+  size_t hblob_cap_ = 0;
+  char* dblob_ = nullptr;
+  size_t dblob_cap_ = 0;
+  char* hres_ = nullptr;
+  size_t hres_cap_ = 0;
+  char* dres_ = nullptr;
+  size_t dres_cap_ = 0;
+  double* dwork_ = nullptr;
+  size_t dwork_cap_ = 0;
+  int* dcounter_ = nullptr;
+};
+
+// ------------------------------------------------------------ TCI2 algorithm
+int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
+               int64_t nparams, const int64_t* pivots, int64_t np);
+CoTask co_construct(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots);
+CoTask co_optimize(Engine& e, Solve& s, tci_opts o);
+CoTask co_crossinterpolate2(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots, tci_opts o);
+CoTask co_updatepivots(Engine& e, Solve& s, int b, bool leftorth, double reltol, double abstol,
+                       i64 maxbonddim, const IndexSet* extraI, const IndexSet* extraJ);
+CoTask co_sweep2site(Engine& e, Solve& s, int niter, int iter1, double abstol, i64 maxbonddim,
+                     int strategy, bool strictlynested, bool fillsite);
+CoTask co_sweep1site(Engine& e, Solve& s, bool forward, double reltol, double abstol, i64 maxbonddim,
+                     bool updatetensors);
+CoTask co_fillsitetensors(Engine& e, Solve& s);
+CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np, double* fout,
+                   double* ttout);
+int addglobalpivots(Solve& s, const std::vector<std::vector<uint8_t>>& pivots);
+i64 solve_rank(const Solve& s);
+bool convergencecriterion(const std::vector<i64>& ranks, const std::vector<double>& errors,
+                          const std::vector<i64>& ngp, double tolerance, i64 maxbonddim,
+                          i64 ncheckhistory, bool checkconvglobalpivot);
+CoTask co_sum(Engine& e, Solve& s, double* out);
+
+}  // namespace tci

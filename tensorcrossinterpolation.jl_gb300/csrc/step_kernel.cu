@@ -1,0 +1,752 @@
+// The TCI2 sweep step kernel (sm_103a): batched evaluation of f over Pi,
+// full-pivot rank-revealing LU, and the per-bond post-processing, fused so that
+// a Pi matrix that fits in shared memory never leaves the SM.
+//
+// One CTA takes one task at a time from an atomic queue (tasks are ordered
+// largest first on the host).  Task kinds (tci_tasks.h):
+//   RRLU : Pi[i,j] = f(rows[i] ++ cols[j]) (filltensor, tensorci2.jl:290-312,
+//          batcheval.jl:32-61) or a given matrix, then rrLU exactly as
+//          _optimizerrlu!/addpivot! (matrixlu.jl:98-181), then optionally
+//          left/right of MatrixLUCI (matrixluci.jl:40-84).
+//   SITE : setsitetensor!(tci, f, b) (tensorci2.jl:367-394): the pivot matrix P
+//          is factored by the same full-pivot LU and T = Pi1 * inv(P) is solved
+//          row by row.
+//   CORE : core = Pi1 (tensorci2.jl:379-383, :449-459).
+//   EVAL : f and the tensor train at points (globalpivotfinder.jl:167-177,
+//          abstracttensortrain.jl:124-132).
+//
+// Bit-exactness of the pivots: the rank-1 update is a separate IEEE multiply and
+// subtract (__dmul_rn/__dsub_rn, as the reference's loop at matrixlu.jl:128-134
+// is compiled without FMA), scaling is an IEEE division (matrixlu.jl:119-123),
+// and the argmax compares abs2 = v*v with strict '>' and breaks ties towards the
+// first element in column-major order of the physically permuted matrix
+// (matrixlu.jl:16-31).  The comparison of v*v is skipped for elements whose |v|
+// is more than 16 ulps below the running maximum, where v*v is provably smaller.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tci_functions.h"
+#include "tci_tasks.h"
+
+namespace {
+
+constexpr int NT = TCI_STEP_THREADS;
+constexpr int NW = NT / 32;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr uint64_t ABS_MASK = 0x7fffffffffffffffULL;
+constexpr uint64_t NAN_FLOOR = 0x7ff0000000000000ULL;  // bits above this are NaN
+constexpr uint64_t SQ_SMALL = (uint64_t)(1023 - 500) << 52;  // below: squares may be subnormal
+constexpr uint64_t SQ_BIG = (uint64_t)(1023 + 500) << 52;    // above: squares may overflow
+
+struct Ctl {
+  int task;
+  int r, c, K, stop, kmax;
+  int status;
+  double piv, maxerror, err;
+  double red_s[NW + 1];
+  int red_k[NW + 1];
+  unsigned long long red_u[NW + 1];
+};
+
+__device__ __forceinline__ double jmax(double a, double b) {
+  if (a != a || b != b) return __longlong_as_double(0x7ff8000000000000LL);
+  return a > b ? a : b;
+}
+
+// Running argmax of abs2 with first-in-column-major tie breaking.
+struct ArgBest {
+  uint64_t M;
+  double bs;
+  int key;
+  __device__ __forceinline__ void init() {
+    M = 0;
+    bs = -1.0;
+    key = 0x7fffffff;
+  }
+  __device__ __forceinline__ void push(double v, int k) {
+    uint64_t b = (uint64_t)__double_as_longlong(v) & ABS_MASK;
+    if (b > NAN_FLOOR) return;
+    if (b + 16 >= M || M < SQ_SMALL || M >= SQ_BIG) {
+      double s = __dmul_rn(v, v);
+      if (s > bs || (s == bs && k < key)) {
+        bs = s;
+        key = k;
+      }
+      if (b > M) M = b;
+    }
+  }
+};
+
+__device__ __forceinline__ void arg_combine(double& bs, int& key, double obs, int okey) {
+  if (obs > bs || (obs == bs && okey < key)) {
+    bs = obs;
+    key = okey;
+  }
+}
+
+// Block-wide argmax; every thread gets the result.  Ends with a barrier.
+__device__ void block_argmax(const ArgBest& a, Ctl& ctl, double& out_s, int& out_key) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double bs = a.bs;
+  int key = a.key;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    double obs = __shfl_down_sync(FULL, bs, off);
+    int okey = __shfl_down_sync(FULL, key, off);
+    arg_combine(bs, key, obs, okey);
+  }
+  if (lane == 0) {
+    ctl.red_s[warp] = bs;
+    ctl.red_k[warp] = key;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    bs = lane < NW ? ctl.red_s[lane] : -1.0;
+    key = lane < NW ? ctl.red_k[lane] : 0x7fffffff;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      double obs = __shfl_down_sync(FULL, bs, off);
+      int okey = __shfl_down_sync(FULL, key, off);
+      arg_combine(bs, key, obs, okey);
+    }
+    if (lane == 0) {
+      ctl.red_s[NW] = bs;
+      ctl.red_k[NW] = key;
+    }
+  }
+  __syncthreads();
+  out_s = ctl.red_s[NW];
+  out_key = ctl.red_k[NW];
+  __syncthreads();
+}
+
+// Block-wide max of unsigned 64-bit values (|v| bit patterns: NaN sorts above Inf).
+__device__ unsigned long long block_max_u64(unsigned long long v, Ctl& ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(FULL, v, off);
+    v = o > v ? o : v;
+  }
+  if (lane == 0) ctl.red_u[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < NW ? ctl.red_u[lane] : 0ULL;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      unsigned long long o = __shfl_down_sync(FULL, v, off);
+      v = o > v ? o : v;
+    }
+    if (lane == 0) ctl.red_u[NW] = v;
+  }
+  __syncthreads();
+  unsigned long long r = ctl.red_u[NW];
+  __syncthreads();
+  return r;
+}
+
+__device__ int block_or(int v, Ctl& ctl) {
+  int r = __syncthreads_or(v);
+  return r;
+}
+
+__device__ __forceinline__ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Row / column partial sums of the registered f (tci_functions.h).
+__device__ void compute_states(int fid, const double* params, const uint8_t* idx, int count, int len,
+                               int site0, double* s0, double* s1) {
+  for (int i = threadIdx.x; i < count; i += NT) {
+    double a0 = 0.0, a1 = 0.0;
+    const uint8_t* v = idx + (size_t)i * len;
+    for (int p = 0; p < len; ++p) tci_f_term(fid, params, site0 + p, v[p], &a0, &a1);
+    s0[i] = a0;
+    s1[i] = a1;
+  }
+}
+
+// Result record pointers.
+struct ResPtrs {
+  tci_result_head* head;
+  int* rowp;
+  int* colp;
+  double* diag;
+};
+__device__ ResPtrs res_ptrs(char* resb, const tci_task& T) {
+  ResPtrs p;
+  char* base = resb + T.res;
+  p.head = (tci_result_head*)base;
+  const int kcap = T.kcap;
+  size_t off = sizeof(tci_result_head);
+  p.rowp = (int*)(base + off);
+  off += align_up((size_t)kcap * 4, 8);
+  p.colp = (int*)(base + off);
+  off += align_up((size_t)kcap * 4, 8);
+  p.diag = (double*)(base + off);
+  return p;
+}
+
+// The rrLU main loop (matrixlu.jl:141-181) on A (m x n, leading dim lda) with the
+// first argmax already in ctl.r/ctl.c.  rowperm/colperm are full permutations.
+__device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
+                          bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int kmax = min(maxrank, min(m, n));
+  if (tid == 0) {
+    ctl.K = 0;
+    ctl.maxerror = 0.0;
+    ctl.err = __longlong_as_double(0x7ff8000000000000LL);
+    ctl.kmax = kmax;
+  }
+  __syncthreads();
+  int K = 0;
+  while (K < kmax) {
+    if (tid == 0) {
+      const int r = ctl.r, c = ctl.c;
+      double piv = A[r + (size_t)c * lda];
+      double e = fabs(piv);
+      ctl.err = e;
+      int stop = ((e < reltol * ctl.maxerror || e < abstol) && K > 0) ? 1 : 0;
+      ctl.stop = stop;
+      if (!stop) {
+        ctl.maxerror = jmax(ctl.maxerror, e);
+        ctl.piv = piv;
+        diag_out[K] = e;
+        int t = rowperm[K];
+        rowperm[K] = rowperm[r];
+        rowperm[r] = t;
+        t = colperm[K];
+        colperm[K] = colperm[c];
+        colperm[c] = t;
+      }
+    }
+    __syncthreads();
+    if (ctl.stop) break;
+    const int r = ctl.r, c = ctl.c;
+    const double piv = ctl.piv;
+    // swaprow! (matrixlu.jl:98-104): whole rows K and r
+    if (r != K)
+      for (int j = tid; j < n; j += NT) {
+        double* col = A + (size_t)j * lda;
+        double a = col[K];
+        col[K] = col[r];
+        col[r] = a;
+      }
+    __syncthreads();
+    // swapcol! (matrixlu.jl:106-112) and, for leftorthogonal, A[K+1:end, K] ./= A[K, K]
+    {
+      double* ck = A + (size_t)K * lda;
+      double* cc = A + (size_t)c * lda;
+      for (int i = tid; i < m; i += NT) {
+        double a = ck[i];
+        if (c != K) {
+          double b = cc[i];
+          cc[i] = a;
+          a = b;
+        }
+        if (leftorth && i > K) a = __ddiv_rn(a, piv);
+        ck[i] = a;
+      }
+    }
+    __syncthreads();
+    if (!leftorth) {  // A[K, K+1:end] ./= A[K, K]
+      for (int j = K + 1 + tid; j < n; j += NT) A[K + (size_t)j * lda] = __ddiv_rn(A[K + (size_t)j * lda], piv);
+      __syncthreads();
+    }
+    ++K;
+    if (K == kmax) break;  // the trailing update after the last pivot is not observable
+    // A[K:, K:] -= x * y^T fused with the argmax of abs2 for the next pivot
+    ArgBest ab;
+    ab.init();
+    const double* x = A + (size_t)(K - 1) * lda;
+    for (int j = K + warp; j < n; j += NW) {
+      double* col = A + (size_t)j * lda;
+      const double y = col[K - 1];
+      const int kb = j * m;
+      for (int i = K + lane; i < m; i += 32) {
+        double v = __dsub_rn(col[i], __dmul_rn(x[i], y));
+        col[i] = v;
+        ab.push(v, kb + i);
+      }
+    }
+    double bs;
+    int key;
+    block_argmax(ab, ctl, bs, key);
+    if (tid == 0) {
+      if (bs < 0.0) {  // every candidate NaN: Julia's loop keeps the first index
+        ctl.r = K;
+        ctl.c = K;
+      } else {
+        ctl.r = key % m;
+        ctl.c = key / m;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) {
+    ctl.K = K;
+    if (K >= min(m, n)) ctl.err = 0.0;
+  }
+  __syncthreads();
+}
+
+// NaN scan of L = tril(A[:, 1:K]) and U = triu(A[1:K, :]) (matrixlu.jl:162-169).
+__device__ int lu_has_nan(const double* A, int lda, int m, int n, int K, Ctl& ctl) {
+  int bad = 0;
+  for (int j = threadIdx.x >> 5; j < n; j += NW) {
+    const double* col = A + (size_t)j * lda;
+    int i0 = j < K ? j : m;  // L part: rows >= j for j < K
+    for (int i = (threadIdx.x & 31); i < m; i += 32) {
+      bool inL = (j < K) && (i >= i0);
+      bool inU = (i < K) && (i <= j);
+      if ((inL || inU) && col[i] != col[i]) bad = 1;
+    }
+  }
+  return block_or(bad, ctl);
+}
+
+// left(MatrixLUCI) for leftorthogonal (colstimespivotinv, matrixluci.jl:48-57):
+// rows K.. of L solved against the unit-lower L11, rows scattered by rowperm.
+// For !leftorthogonal: colmatrix = left(lu) * U[:, 1:K] (matrixluci.jl:40-42).
+__device__ void post_left(double* A, int lda, int m, int n, int K, bool leftorth, const int* rowperm,
+                          double* out) {
+  const int tid = threadIdx.x;
+  if (leftorth) {
+    // X * L11 = L21, processed right to left; one thread per row of L21.
+    for (int p = K + tid; p < m; p += NT) {
+      for (int q = K - 1; q >= 0; --q) {
+        double zq = A[p + (size_t)q * lda];
+        for (int s = 0; s < q; ++s) {
+          double l = A[q + (size_t)s * lda];
+          A[p + (size_t)s * lda] = A[p + (size_t)s * lda] - zq * l;
+        }
+      }
+    }
+    __syncthreads();
+    for (int q = 0; q < K; ++q)
+      for (int p = tid; p < m; p += NT) {
+        double v = p < K ? (p == q ? 1.0 : 0.0) : A[p + (size_t)q * lda];
+        out[rowperm[p] + (size_t)q * m] = v;
+      }
+  } else {
+    // colmatrix: (L with rows scattered) * U11, U11 unit upper; L keeps its diagonal
+    for (int p = tid; p < m; p += NT)
+      for (int q = 0; q < K; ++q) {
+        double s = 0.0;
+        const int tmax = min(p, q);
+        for (int t = 0; t <= tmax; ++t) {
+          double l = A[p + (size_t)t * lda];
+          double u = (t == q) ? 1.0 : A[t + (size_t)q * lda];
+          s = s + l * u;
+        }
+        out[rowperm[p] + (size_t)q * m] = s;
+      }
+  }
+  __syncthreads();
+}
+
+// right(MatrixLUCI): for leftorthogonal rowmatrix = L11 * right(lu)
+// (matrixluci.jl:44-46); otherwise pivotinvtimesrows (matrixluci.jl:59-68).
+__device__ void post_right(double* A, int lda, int m, int n, int K, bool leftorth, const int* colperm,
+                           double* out) {
+  const int tid = threadIdx.x;
+  if (leftorth) {
+    for (int j = tid; j < n; j += NT)
+      for (int q = 0; q < K; ++q) {
+        double s = 0.0;
+        for (int t = 0; t <= q; ++t) {
+          double l = (t == q) ? 1.0 : A[q + (size_t)t * lda];
+          double u = (t <= j) ? A[t + (size_t)j * lda] : 0.0;
+          s = s + l * u;
+        }
+        out[q + (size_t)colperm[j] * K] = s;
+      }
+  } else {
+    // U11 X = U12 with unit-upper U11; one thread per column of U12.
+    for (int j = K + tid; j < n; j += NT) {
+      double* col = A + (size_t)j * lda;
+      for (int q = K - 1; q >= 0; --q) {
+        double xq = col[q];
+        for (int p = 0; p < q; ++p) col[p] = col[p] - A[p + (size_t)q * lda] * xq;
+      }
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += NT)
+      for (int q = 0; q < K; ++q) {
+        double v = j < K ? (q == j ? 1.0 : 0.0) : A[q + (size_t)j * lda];
+        out[q + (size_t)colperm[j] * K] = v;
+      }
+  }
+  __syncthreads();
+}
+
+struct SmemCursor {
+  char* p;
+  __device__ char* take(size_t bytes) {
+    char* r = p;
+    p += align_up(bytes, 16);
+    return r;
+  }
+};
+
+// ---------------------------------------------------------------- RRLU task
+__device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
+  const int m = T.m, n = T.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  ResPtrs rp = res_ptrs(resb, T);
+  SmemCursor cur{smem};
+  double* A = T.smem_mode ? (double*)cur.take((size_t)m * n * 8) : T.work;
+  const int lda = m;
+  int* rowperm = (int*)cur.take((size_t)m * 4);
+  int* colperm = (int*)cur.take((size_t)n * 4);
+  for (int i = tid; i < m; i += NT) rowperm[i] = i;
+  for (int j = tid; j < n; j += NT) colperm[j] = j;
+  ArgBest ab;
+  ab.init();
+  unsigned long long mx = 0;
+  if (T.ain) {
+    for (int j = warp; j < n; j += NW) {
+      const double* src = T.ain + (size_t)j * m;
+      double* dst = A + (size_t)j * lda;
+      for (int i = lane; i < m; i += 32) {
+        double v = src[i];
+        dst[i] = v;
+        ab.push(v, j * m + i);
+        unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+        mx = b > mx ? b : mx;
+      }
+    }
+  } else {
+    const double* prm = (const double*)(blob + T.params);
+    double* rs0 = (double*)cur.take((size_t)m * 8);
+    double* rs1 = (double*)cur.take((size_t)m * 8);
+    double* cs0 = (double*)cur.take((size_t)n * 8);
+    double* cs1 = (double*)cur.take((size_t)n * 8);
+    compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
+    compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
+    __syncthreads();
+    for (int j = warp; j < n; j += NW) {
+      double* dst = A + (size_t)j * lda;
+      const double c0 = cs0[j], c1 = cs1[j];
+      for (int i = lane; i < m; i += 32) {
+        double v = tci_f_finish(T.fid, prm, T.nparams, rs0[i] + c0, rs1[i] + c1);
+        dst[i] = v;
+        ab.push(v, j * m + i);
+        unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+        mx = b > mx ? b : mx;
+      }
+    }
+  }
+  __syncthreads();
+  unsigned long long mxall = block_max_u64(mx, ctl);
+  double bs;
+  int key;
+  block_argmax(ab, ctl, bs, key);
+  if (tid == 0) {
+    if (bs < 0.0 || m == 0 || n == 0) {
+      ctl.r = 0;
+      ctl.c = 0;
+    } else {
+      ctl.r = key % m;
+      ctl.c = key / m;
+    }
+    ctl.status = 0;
+  }
+  __syncthreads();
+  const bool leftorth = T.leftorth != 0;
+  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl);
+  const int K = ctl.K;
+  int nan = lu_has_nan(A, lda, m, n, K, ctl);
+  if (T.post == TCI_POST_LEFT && !nan) post_left(A, lda, m, n, K, leftorth, rowperm, T.core_out);
+  if (T.post == TCI_POST_RIGHT && !nan) post_right(A, lda, m, n, K, leftorth, colperm, T.core_out);
+  if (T.post == TCI_POST_FACTORS)
+    for (int j = warp; j < n; j += NW)
+      for (int i = lane; i < m; i += 32) T.core_out[i + (size_t)j * m] = A[i + (size_t)j * lda];
+  if (tid == 0) {
+    rp.head->status = nan ? TCI_ST_NAN : 0;
+    rp.head->npivot = K;
+    rp.head->error = ctl.err;
+    rp.head->maxabs = __longlong_as_double((long long)mxall);
+    rp.head->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+  }
+  if (T.post == TCI_POST_FACTORS) {
+    // full permutations go after the factors: rowperm (m) then colperm (n)
+    int* fr = (int*)(T.core_out + (size_t)m * n);
+    for (int i = tid; i < m; i += NT) fr[i] = rowperm[i];
+    for (int j = tid; j < n; j += NT) fr[m + j] = colperm[j];
+  }
+  for (int k = tid; k < K; k += NT) {
+    rp.rowp[k] = rowperm[k];
+    rp.colp[k] = colperm[k];
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- SITE task
+// T.r x T.r pivot matrix P = f(prows x cols); Pi1 = f(rows x cols) (m x r).
+__device__ void task_site(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl,
+                          size_t smem_bytes) {
+  const int r = T.r, m = T.m, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  ResPtrs rp = res_ptrs(resb, T);
+  const double* prm = (const double*)(blob + T.params);
+  SmemCursor cur{smem};
+  double* P = T.smem_mode ? (double*)cur.take((size_t)r * r * 8) : T.work;
+  int* rowperm = (int*)cur.take((size_t)r * 4);
+  int* colperm = (int*)cur.take((size_t)r * 4);
+  double* ps0 = (double*)cur.take((size_t)r * 8);
+  double* ps1 = (double*)cur.take((size_t)r * 8);
+  double* cs0 = (double*)cur.take((size_t)r * 8);
+  double* cs1 = (double*)cur.take((size_t)r * 8);
+  double* rs0 = (double*)cur.take((size_t)m * 8);
+  double* rs1 = (double*)cur.take((size_t)m * 8);
+  compute_states(T.fid, prm, (const uint8_t*)(blob + T.prows), r, T.nl, 0, ps0, ps1);
+  compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), r, T.nr, T.nl, cs0, cs1);
+  compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
+  for (int i = tid; i < r; i += NT) {
+    rowperm[i] = i;
+    colperm[i] = i;
+  }
+  __syncthreads();
+  ArgBest ab;
+  ab.init();
+  for (int j = warp; j < r; j += NW)
+    for (int i = lane; i < r; i += 32) {
+      double v = tci_f_finish(T.fid, prm, T.nparams, ps0[i] + cs0[j], ps1[i] + cs1[j]);
+      P[i + (size_t)j * r] = v;
+      ab.push(v, j * r + i);
+    }
+  __syncthreads();
+  double bs;
+  int key;
+  block_argmax(ab, ctl, bs, key);
+  if (tid == 0) {
+    ctl.r = bs < 0.0 ? 0 : key % r;
+    ctl.c = bs < 0.0 ? 0 : key / r;
+  }
+  __syncthreads();
+  rrlu_loop(P, r, r, r, r, 0.0, 0.0, true, rowperm, colperm, rp.diag, ctl);
+  int singular = 0;
+  if (tid == 0) {
+    for (int k = 0; k < r; ++k)
+      if (!(P[k + (size_t)k * r] != 0.0)) singular = 1;
+    if (ctl.K < r) singular = 1;
+    ctl.status = singular ? TCI_ST_SINGULAR : 0;
+  }
+  __syncthreads();
+  // T = Pi1 * inv(P): per row, w = Pi1[row, colperm]; z U = w; s L = z; t[rowperm] = s.
+  size_t used = (size_t)(cur.p - smem);
+  int RB = (int)((smem_bytes > used ? smem_bytes - used : 0) / ((size_t)r * 8 + 8));
+  RB = RB > NT ? NT : RB;
+  RB = RB < 1 ? 1 : RB;
+  double* W = (double*)cur.take((size_t)RB * r * 8);
+  unsigned long long mx = 0;
+  int nanflag = 0;
+  for (int base = 0; base < m; base += RB) {
+    const int rows_here = min(RB, m - base);
+    for (int e = tid; e < rows_here * r; e += NT) {
+      int rr = e % rows_here, q = e / rows_here;
+      int row = base + rr, col = colperm[q];
+      double v = tci_f_finish(T.fid, prm, T.nparams, rs0[row] + cs0[col], rs1[row] + cs1[col]);
+      W[rr + (size_t)q * RB] = v;
+      unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+      mx = b > mx ? b : mx;
+    }
+    __syncthreads();
+    if (ctl.status == 0) {
+      for (int rr = tid; rr < rows_here; rr += NT) {
+        // forward: z U = w (U upper, non-unit)
+        for (int q = 0; q < r; ++q) {
+          double zq = W[rr + (size_t)q * RB] / P[q + (size_t)q * r];
+          W[rr + (size_t)q * RB] = zq;
+          for (int p = q + 1; p < r; ++p) W[rr + (size_t)p * RB] = W[rr + (size_t)p * RB] - zq * P[q + (size_t)p * r];
+        }
+        // backward: s L = z (L unit lower)
+        for (int q = r - 1; q >= 0; --q) {
+          double sq = W[rr + (size_t)q * RB];
+          for (int p = 0; p < q; ++p) W[rr + (size_t)p * RB] = W[rr + (size_t)p * RB] - sq * P[q + (size_t)p * r];
+        }
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < rows_here * r; e += NT) {
+      int rr = e % rows_here, p = e / rows_here;
+      double v = W[rr + (size_t)p * RB];
+      if (v != v) nanflag = 1;
+      T.core_out[(base + rr) + (size_t)rowperm[p] * m] = v;
+    }
+    __syncthreads();
+  }
+  unsigned long long mxall = block_max_u64(mx, ctl);
+  int nan = block_or(nanflag, ctl);
+  if (tid == 0) {
+    rp.head->status = ctl.status | (nan ? TCI_ST_NAN : 0);
+    rp.head->npivot = ctl.K;
+    rp.head->error = ctl.err;
+    rp.head->maxabs = __longlong_as_double((long long)mxall);
+    rp.head->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- CORE task
+__device__ void task_core(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
+  const int m = T.m, n = T.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const double* prm = (const double*)(blob + T.params);
+  SmemCursor cur{smem};
+  double* rs0 = (double*)cur.take((size_t)m * 8);
+  double* rs1 = (double*)cur.take((size_t)m * 8);
+  double* cs0 = (double*)cur.take((size_t)n * 8);
+  double* cs1 = (double*)cur.take((size_t)n * 8);
+  compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
+  compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
+  __syncthreads();
+  unsigned long long mx = 0;
+  for (int j = warp; j < n; j += NW)
+    for (int i = lane; i < m; i += 32) {
+      double v = tci_f_finish(T.fid, prm, T.nparams, rs0[i] + cs0[j], rs1[i] + cs1[j]);
+      T.core_out[i + (size_t)j * m] = v;
+      unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+      mx = b > mx ? b : mx;
+    }
+  unsigned long long mxall = block_max_u64(mx, ctl);
+  if (tid == 0) {
+    tci_result_head* h = (tci_result_head*)(resb + T.res);
+    h->status = 0;
+    h->npivot = 0;
+    h->error = 0.0;
+    h->maxabs = __longlong_as_double((long long)mxall);
+    h->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- EVAL task
+// f and the tensor train at T.m points (rows, L sites each).  One warp per point
+// for the train: out[q] = sum_p v[p] * core[p, i, q], summed in order of p with
+// separate multiply and add, as the oracle's loop.
+__device__ void task_eval(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
+  const int np = T.m, L = T.L, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const double* prm = (const double*)(blob + T.params);
+  const uint8_t* pts = (const uint8_t*)(blob + T.rows);
+  char* base = resb + T.res;
+  double* fout = (double*)(base + sizeof(tci_result_head));
+  double* tout = fout + np;
+  for (int p = tid; p < np; p += NT) {
+    double a0 = 0.0, a1 = 0.0;
+    for (int s = 0; s < L; ++s) tci_f_term(T.fid, prm, s, pts[(size_t)p * L + s], &a0, &a1);
+    fout[p] = tci_f_finish(T.fid, prm, T.nparams, a0, a1);
+  }
+  if (T.cores) {
+    const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
+    const int rmax = T.r;
+    double* va = (double*)smem + (size_t)warp * 2 * rmax;
+    double* vb = va + rmax;
+    for (int p = warp; p < np; p += NW) {
+      if (lane == 0) va[0] = 1.0;
+      __syncwarp();
+      double* v = va;
+      double* w = vb;
+      for (int s = 0; s < L; ++s) {
+        const tci_core_ref c = cr[s];
+        const int i = pts[(size_t)p * L + s];
+        for (int q = lane; q < c.r1; q += 32) {
+          double acc = 0.0;
+          const double* col = c.p + (size_t)c.r0 * (i + (size_t)c.d * q);
+          for (int t = 0; t < c.r0; ++t) acc = __dadd_rn(acc, __dmul_rn(v[t], col[t]));
+          w[q] = acc;
+        }
+        __syncwarp();
+        double* tmp = v;
+        v = w;
+        w = tmp;
+      }
+      if (lane == 0) tout[p] = v[0];
+      __syncwarp();
+    }
+  } else {
+    for (int p = tid; p < np; p += NT) tout[p] = 0.0;
+  }
+  if (tid == 0) {
+    tci_result_head* h = (tci_result_head*)base;
+    h->status = 0;
+    h->npivot = 0;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- SUM task
+// sum(tt) (abstracttensortrain.jl:164-199): v <- v * (sum over the local index
+// of core b), left to right; one thread per output bond index.
+__device__ void task_sum(const tci_task& T, const char* blob, char* resb, char* smem) {
+  const int L = T.L, tid = threadIdx.x;
+  const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
+  double* v = (double*)smem;
+  double* w = v + T.r;
+  if (tid == 0) v[0] = 1.0;
+  __syncthreads();
+  for (int s = 0; s < L; ++s) {
+    const tci_core_ref c = cr[s];
+    for (int q = tid; q < c.r1; q += NT) {
+      double acc = 0.0;
+      for (int p = 0; p < c.r0; ++p) {
+        double sm = 0.0;
+        for (int i = 0; i < c.d; ++i) sm = __dadd_rn(sm, c.p[p + (size_t)c.r0 * (i + (size_t)c.d * q)]);
+        acc = __dadd_rn(acc, __dmul_rn(v[p], sm));
+      }
+      w[q] = acc;
+    }
+    __syncthreads();
+    double* t = v;
+    v = w;
+    w = t;
+  }
+  if (tid == 0) {
+    tci_result_head* h = (tci_result_head*)(resb + T.res);
+    h->status = 0;
+    h->npivot = 0;
+    h->error = v[0];
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(NT, 1)
+    tci_step_kernel(const char* __restrict__ blob, char* __restrict__ resb, const int* __restrict__ order,
+                    int ntasks, int* counter, size_t smem_bytes) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ Ctl ctl;
+  const tci_task* tasks = (const tci_task*)blob;
+  for (;;) {
+    if (threadIdx.x == 0) ctl.task = atomicAdd(counter, 1);
+    __syncthreads();
+    const int ti = ctl.task;
+    __syncthreads();
+    if (ti >= ntasks) break;
+    const tci_task T = tasks[order[ti]];
+    switch (T.kind) {
+      case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl); break;
+      case TCI_TASK_SITE: task_site(T, blob, resb, smem, ctl, smem_bytes); break;
+      case TCI_TASK_CORE: task_core(T, blob, resb, smem, ctl); break;
+      case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
+      case TCI_TASK_SUM: task_sum(T, blob, resb, smem); break;
+      default: break;
+    }
+  }
+}
+
+}  // namespace
+
+// Shared-memory budget of one CTA of the step kernel.
+size_t tci_step_smem_bytes() { return 227 * 1024 - 1024; }
+
+cudaError_t tci_step_configure() {
+  return cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tci_step_smem_bytes());
+}
+
+// Launch one step.  counter must be zero (the launcher clears it on the stream).
+cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
+                            int* counter_dev, int grid, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(counter_dev, 0, sizeof(int), stream);
+  if (e != cudaSuccess) return e;
+  tci_step_kernel<<<grid, NT, tci_step_smem_bytes(), stream>>>(blob_dev, res_dev, order_dev, ntasks,
+                                                              counter_dev, tci_step_smem_bytes());
+  return cudaGetLastError();
+}

@@ -1,0 +1,99 @@
+// Registered device functions f(v) for batched evaluation over Pi matrices.
+//
+// In the reference, f is any Julia callable taking a MultiIndex (a vector of
+// 1-based local indices, abstracttensortrain.jl:6-7) and filltensor calls it
+// once per element of Pi (tensorci2.jl:290-312 -> batcheval.jl:32-61).  Here f
+// is a registered device function.  Every registered f is written as
+//     f(v) = finish( sum_p term_p(v_p) )
+// where the running sums (at most two) are exact in double precision: sums of
+// integers below 2^53, or of distinct powers of two spanning at most 53 bits.
+// Because they are exact, a row prefix and a column suffix of a multi-index can
+// be accumulated separately and added, and the value is bit-identical to the
+// one-pass evaluation the CPU oracle performs.  `v` below is the 0-based local
+// index (the reference's index minus one).
+#pragma once
+#include "tci_math.h"
+
+enum {
+  TCI_F_LORENTZ = 1,  // coeff / (1 + sum_p v_p^2), v 1-based (test_tensorci2.jl:249)
+  TCI_F_SERVED = 2,   // 1/(1 + a sum v^2) + b exp(-g sum (v - c)^2), v and c 1-based
+  TCI_F_QTT1D = 3,    // quantics 1-D, x = sum_i b_i 2^-i
+  TCI_F_QTT2D = 4,    // quantics 2-D, d = 4: x bit = low bit, y bit = high bit
+  TCI_F_DENSE = 5,    // table lookup: f(v) = T[v] (column-major over localdims)
+};
+
+// Parameter layouts (double array `params`):
+//   LORENTZ: [coeff]                      (empty => coeff = 1)
+//   SERVED : [alpha, beta, gamma, c_1 .. c_L]
+//   QTT1D  : [kind]   kind 0: exp(-x) cos(2000 pi x) + 0.5 exp(-(x-0.3)^2/1e-4)
+//                     kind 1: exp(-x)
+//                     kind 2: exp(-x) + 1e-4 exp(-2x)
+//   QTT2D  : []       exp(-((x-.5)^2 + (y-.5)^2)/0.01) cos(400 pi (x + y))
+//   DENSE  : [L, stride_1 .. stride_L, values ...]
+
+#define TCI_TWO_THOUSAND_PI 6283.185307179587   /* 2000*pi rounded to double */
+#define TCI_FOUR_HUNDRED_PI 1256.6370614359173  /* 400*pi rounded to double  */
+
+TCI_HD void tci_f_term(int fid, const double* params, int site, int v,
+                       double* acc0, double* acc1) {
+  switch (fid) {
+    case TCI_F_LORENTZ: {
+      double v1 = (double)(v + 1);
+      *acc0 = *acc0 + v1 * v1;
+    } break;
+    case TCI_F_SERVED: {
+      double v1 = (double)(v + 1);
+      double dv = v1 - params[3 + site];
+      *acc0 = *acc0 + v1 * v1;
+      *acc1 = *acc1 + dv * dv;
+    } break;
+    case TCI_F_QTT1D: {
+      if (v) *acc0 = *acc0 + tci_pow2i(-(site + 1));
+    } break;
+    case TCI_F_QTT2D: {
+      if (v & 1) *acc0 = *acc0 + tci_pow2i(-(site + 1));
+      if (v & 2) *acc1 = *acc1 + tci_pow2i(-(site + 1));
+    } break;
+    case TCI_F_DENSE: {
+      *acc0 = *acc0 + (double)v * params[1 + site];
+    } break;
+    default: break;
+  }
+}
+
+TCI_HD double tci_f_finish(int fid, const double* params, int nparams, double acc0,
+                           double acc1) {
+  switch (fid) {
+    case TCI_F_LORENTZ: {
+      double coeff = nparams > 0 ? params[0] : 1.0;
+      return coeff / (acc0 + 1.0);
+    }
+    case TCI_F_SERVED: {
+      double a = 1.0 / (1.0 + params[0] * acc0);
+      double e = tci_exp(-(params[2] * acc1));
+      return a + params[1] * e;
+    }
+    case TCI_F_QTT1D: {
+      double x = acc0;
+      int kind = nparams > 0 ? (int)params[0] : 0;
+      if (kind == 1) return tci_exp(-x);
+      if (kind == 2) return tci_exp(-x) + 1e-4 * tci_exp(-(2.0 * x));
+      double t1 = tci_exp(-x);
+      double t2 = tci_cos(TCI_TWO_THOUSAND_PI * x);
+      double dx = x - 0.3;
+      double t3 = tci_exp(-(dx * dx) / 1e-4);
+      return t1 * t2 + 0.5 * t3;
+    }
+    case TCI_F_QTT2D: {
+      double dx = acc0 - 0.5, dy = acc1 - 0.5;
+      double g = tci_exp(-(dx * dx + dy * dy) / 0.01);
+      return g * tci_cos(TCI_FOUR_HUNDRED_PI * (acc0 + acc1));
+    }
+    case TCI_F_DENSE: {
+      int L = (int)params[0];
+      return params[1 + L + (int64_t)acc0];
+    }
+    default:
+      return 0.0;
+  }
+}

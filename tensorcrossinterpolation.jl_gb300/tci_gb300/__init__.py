@@ -1,0 +1,653 @@
+"""GB300-native TCI2 two-site sweep, with the reference's Python-facing API.
+
+Mirrors TensorCrossInterpolation.jl's interface for this path:
+``crossinterpolate2``, ``TensorCI2`` (``updatepivots!``, ``sweep2site!``,
+``sweep1site!``, ``optimize!``, ``addglobalpivots!``, ...), ``TensorTrain``
+(``evaluate``, ``sum``) and ``rrlu`` / ``rrLU``.  Everything that computes runs
+in libtci_gpu.so (CUDA kernels for sm_103a behind a C ABI, include/tci_gb300.h).
+There is no CPU fallback: without the library or a GPU every call raises.
+
+Indices are 1-based, as in Julia.  Matrices are numpy arrays; site tensors are
+returned as (r_{b-1}, d_b, r_b) arrays.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtci_gpu.so")
+
+I64P = ctypes.POINTER(ctypes.c_int64)
+F64P = ctypes.POINTER(ctypes.c_double)
+
+TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
+TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
+SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
+FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5}
+
+
+class TCIError(RuntimeError):
+    """A failure reported by the library (code + the reference's message)."""
+
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class ArgumentError(TCIError, ValueError):
+    pass
+
+
+class DimensionMismatch(TCIError, ValueError):
+    pass
+
+
+_EXC = {TCI_ERR_ARG: ArgumentError, TCI_ERR_DIM: DimensionMismatch}
+
+
+class Opts(ctypes.Structure):
+    """tci_opts: keyword arguments of optimize! (tensorci2.jl:700-720)."""
+    _fields_ = [
+        ("tolerance", ctypes.c_double),
+        ("maxbonddim", ctypes.c_int64),
+        ("maxiter", ctypes.c_int64),
+        ("sweepstrategy", ctypes.c_int32),
+        ("normalizeerror", ctypes.c_int32),
+        ("ncheckhistory", ctypes.c_int32),
+        ("maxnglobalpivot", ctypes.c_int32),
+        ("nsearchglobalpivot", ctypes.c_int32),
+        ("strictlynested", ctypes.c_int32),
+        ("checkconvglobalpivot", ctypes.c_int32),
+        ("pad_", ctypes.c_int32),
+        ("tolmarginglobalsearch", ctypes.c_double),
+        ("seed", ctypes.c_uint64),
+    ]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [
+        ("L", ctypes.c_int32),
+        ("fid", ctypes.c_int32),
+        ("localdims", I64P),
+        ("fparams", F64P),
+        ("nparams", ctypes.c_int64),
+        ("opts", Opts),
+    ]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_int64),
+        ("launches", ctypes.c_int64),
+        ("tasks", ctypes.c_int64),
+        ("kernel_ms", ctypes.c_double),
+        ("feval", ctypes.c_int64),
+        ("lu_updates", ctypes.c_int64),
+        ("h2d_bytes", ctypes.c_int64),
+        ("d2h_bytes", ctypes.c_int64),
+    ]
+
+
+# Every exported symbol of include/tci_gb300.h with its ctypes signature.
+_SIGNATURES = {
+    "tci_opts_default": (None, [ctypes.POINTER(Opts)]),
+    "tci_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_last_error": (ctypes.c_char_p, []),
+    "tci_f_lookup": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]),
+    "tci_solve_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_int32, F64P,
+                                        ctypes.c_int64, I64P, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_solve_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_crossinterpolate2": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_int32, F64P,
+                                             ctypes.c_int64, I64P, ctypes.c_int64, ctypes.POINTER(Opts),
+                                             ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_optimize": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Opts)]),
+    "tci_updatepivots": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_int64]),
+    "tci_sweep2site": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_int64, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]),
+    "tci_sweep1site": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                      ctypes.c_int64, ctypes.c_int32]),
+    "tci_fillsitetensors": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_addglobalpivots": (ctypes.c_int, [ctypes.c_void_p, I64P, ctypes.c_int64]),
+    "tci_addglobalpivots1sitesweep": (ctypes.c_int, [ctypes.c_void_p, I64P, ctypes.c_int64, ctypes.c_double,
+                                                     ctypes.c_double, ctypes.c_int64]),
+    "tci_solve_length": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
+    "tci_linkdims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
+    "tci_maxsamplevalue": (ctypes.c_double, [ctypes.c_void_p]),
+    "tci_get_sets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, I64P, I64P, I64P]),
+    "tci_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P, I64P]),
+    "tci_get_errors": (ctypes.c_int, [ctypes.c_void_p, F64P, I64P, F64P]),
+    "tci_get_history": (ctypes.c_int, [ctypes.c_void_p, I64P, F64P, I64P, I64P]),
+    "tci_solve_nfeval": (ctypes.c_int64, [ctypes.c_void_p]),
+    "tci_evaluate": (ctypes.c_int, [ctypes.c_void_p, I64P, ctypes.c_int64, F64P]),
+    "tci_sum": (ctypes.c_int, [ctypes.c_void_p, F64P]),
+    "tci_crossinterpolate2_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(Request),
+                                                     ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_serve_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(Request), F64P,
+                                     ctypes.c_int64, F64P, I64P, F64P]),
+    "tci_rrlu": (ctypes.c_int, [ctypes.c_void_p, F64P, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                ctypes.c_double, ctypes.c_double, ctypes.c_int32, I64P, I64P, F64P, F64P, I64P,
+                                F64P]),
+    "tci_rrlu_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, F64P, I64P, I64P, I64P, ctypes.c_int64,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int32, I64P, I64P, I64P,
+                                        F64P]),
+    "tci_ctx_stream": (ctypes.c_size_t, [ctypes.c_void_p]),
+    "tci_ctx_synchronize": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_ctx_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Stats), ctypes.c_int32]),
+    "tci_feval": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P, ctypes.c_int64, ctypes.c_int32, I64P, I64P,
+                                 ctypes.c_int64, F64P]),
+    "tci_convergencecriterion": (ctypes.c_int, [I64P, F64P, I64P, ctypes.c_int64, ctypes.c_double,
+                                                ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]),
+    "tci_fp64_peak": (ctypes.c_int, [ctypes.c_size_t, F64P, F64P]),
+}
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libtci_gpu.so; raises OSError if it has not been built."""
+    global _lib
+    if _lib is None:
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise OSError(f"{p} not found: build it with tensorcrossinterpolation.jl_gb300/build.py")
+        L = ctypes.CDLL(p)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols():
+    return list(_SIGNATURES)
+
+
+def _check(rc):
+    if rc:
+        msg = load_library().tci_last_error()
+        msg = msg.decode() if msg else ""
+        raise _EXC.get(rc, TCIError)(rc, msg or f"error code {rc}")
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Context:
+    """A device context: one CUDA stream, the batched step engine, its buffers."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        lib = load_library()
+        h = ctypes.c_void_p()
+        _check(lib.tci_ctx_create(int(device), int(hbm_budget), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load_library().tci_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return load_library().tci_ctx_stream(self.h)
+
+    def synchronize(self):
+        _check(load_library().tci_ctx_synchronize(self.h))
+
+    def stats(self, reset=False):
+        s = Stats()
+        load_library().tci_ctx_stats(self.h, ctypes.byref(s), int(bool(reset)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+
+_default_ctx = None
+
+
+def default_context():
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class DeviceFunction:
+    """A registered device function f (the BatchEvaluator plugin point,
+    cachedtensortrain.jl:1 / batcheval.jl:67-83), selected by name."""
+
+    def __init__(self, name, params=()):
+        if name not in FUNCTIONS:
+            raise ArgumentError(TCI_ERR_ARG, f"unknown function {name}")
+        self.name = name
+        self.fid = FUNCTIONS[name]
+        self.params = np.ascontiguousarray(params, dtype=np.float64)
+
+    @staticmethod
+    def dense(table):
+        """f(v) = table[v] for a small dense tensor (column-major)."""
+        table = np.asarray(table, dtype=np.float64)
+        dims = table.shape
+        strides = np.cumprod((1,) + dims[:-1])
+        return DeviceFunction("dense", np.concatenate([[len(dims)], strides, table.reshape(-1, order="F")]))
+
+
+def make_opts(tolerance=None, maxbonddim=None, maxiter=20, sweepstrategy="backandforth", normalizeerror=True,
+              ncheckhistory=3, maxnglobalpivot=5, nsearchglobalpivot=5, tolmarginglobalsearch=10.0,
+              strictlynested=False, checkconvglobalpivot=True, seed=0, pivottolerance=None, verbosity=0,
+              loginterval=10, pivotsearch="full", globalpivotfinder=None):
+    """Map the reference's optimize! keyword arguments to tci_opts."""
+    if pivotsearch != "full":
+        raise ArgumentError(TCI_ERR_ARG, "only pivotsearch=:full is implemented on the device")
+    if globalpivotfinder is not None:
+        raise ArgumentError(TCI_ERR_ARG, "custom global pivot finders are not supported on the device")
+    if pivottolerance is not None:
+        if tolerance is not None and tolerance != pivottolerance:
+            raise ArgumentError(TCI_ERR_ARG, "Got different values for pivottolerance and tolerance in "
+                                "optimize!(TCI2). For TCI2, both of these options have the same meaning. "
+                                "Please assign only `tolerance`.")
+        tolerance = pivottolerance
+    o = Opts()
+    o.tolerance = 1e-8 if tolerance is None else float(tolerance)
+    o.maxbonddim = 0 if maxbonddim is None else int(maxbonddim)
+    o.maxiter = int(maxiter)
+    o.sweepstrategy = SWEEP[sweepstrategy]
+    o.normalizeerror = int(bool(normalizeerror))
+    o.ncheckhistory = int(ncheckhistory)
+    o.maxnglobalpivot = int(maxnglobalpivot)
+    o.nsearchglobalpivot = int(nsearchglobalpivot)
+    o.strictlynested = int(bool(strictlynested))
+    o.checkconvglobalpivot = int(bool(checkconvglobalpivot))
+    o.tolmarginglobalsearch = float(tolmarginglobalsearch)
+    o.seed = int(seed)
+    return o
+
+
+def _pivots_array(pivots, L):
+    return np.ascontiguousarray(np.asarray(pivots, dtype=np.int64).reshape(-1, L))
+
+
+class TensorCI2:
+    """TensorCI2{Float64} (tensorci2.jl:6-40) held on the device."""
+
+    def __init__(self, f, localdims, initialpivots=None, ctx=None, _handle=None):
+        self.ctx = ctx or default_context()
+        self.f = f
+        self.localdims = [int(d) for d in localdims]
+        L = len(self.localdims)
+        if _handle is not None:
+            self.h = _handle
+            return
+        lib = load_library()
+        d = np.ascontiguousarray(self.localdims, dtype=np.int64)
+        piv = _pivots_array(initialpivots if initialpivots is not None else [np.ones(L)], L)
+        h = ctypes.c_void_p()
+        _check(lib.tci_solve_create(self.ctx.h, L, _p(d, I64P), f.fid,
+                                    _p(f.params, F64P) if f.params.size else None, f.params.size,
+                                    _p(piv, I64P), piv.shape[0], ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        try:
+            if self.h:
+                load_library().tci_solve_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def __len__(self):
+        return len(self.localdims)
+
+    # ---- algorithm steps
+    def updatepivots(self, b, leftorthogonal=True, reltol=1e-14, abstol=0.0, maxbonddim=None):
+        """updatepivots! (tensorci2.jl:510-607), b 1-based."""
+        _check(load_library().tci_updatepivots(self.h, int(b), int(bool(leftorthogonal)), reltol, abstol,
+                                               0 if maxbonddim is None else int(maxbonddim)))
+
+    def sweep2site(self, niter=2, iter1=1, abstol=1e-8, maxbonddim=None, sweepstrategy="backandforth",
+                   strictlynested=False, fillsitetensors=True):
+        """sweep2site! (tensorci2.jl:855-916)."""
+        _check(load_library().tci_sweep2site(self.h, niter, iter1, abstol,
+                                             0 if maxbonddim is None else int(maxbonddim), SWEEP[sweepstrategy],
+                                             int(strictlynested), int(fillsitetensors)))
+
+    def sweep1site(self, sweepdirection="forward", reltol=1e-14, abstol=0.0, maxbonddim=None, updatetensors=True):
+        """sweep1site! (tensorci2.jl:402-461)."""
+        if sweepdirection not in ("forward", "backward"):
+            raise ArgumentError(TCI_ERR_ARG, f"Unknown sweep direction {sweepdirection}: choose between "
+                                ":forward, :backward.")
+        _check(load_library().tci_sweep1site(self.h, int(sweepdirection == "forward"), reltol, abstol,
+                                             0 if maxbonddim is None else int(maxbonddim), int(updatetensors)))
+
+    def fillsitetensors(self):
+        _check(load_library().tci_fillsitetensors(self.h))
+
+    def optimize(self, **kw):
+        """optimize! (tensorci2.jl:700-850) -> (ranks, errors)."""
+        o = make_opts(**kw)
+        _check(load_library().tci_optimize(self.h, ctypes.byref(o)))
+        return self.history()[:2]
+
+    def addglobalpivots(self, pivots):
+        piv = _pivots_array(pivots, len(self))
+        _check(load_library().tci_addglobalpivots(self.h, _p(piv, I64P), piv.shape[0]))
+
+    def addglobalpivots1sitesweep(self, pivots, reltol=1e-14, abstol=0.0, maxbonddim=None):
+        piv = _pivots_array(pivots, len(self))
+        _check(load_library().tci_addglobalpivots1sitesweep(self.h, _p(piv, I64P), piv.shape[0], reltol, abstol,
+                                                            0 if maxbonddim is None else int(maxbonddim)))
+
+    # ---- state
+    def linkdims(self):
+        out = np.zeros(len(self) - 1, np.int64)
+        load_library().tci_linkdims(self.h, _p(out, I64P))
+        return out
+
+    def rank(self):
+        return int(self.linkdims().max())
+
+    @property
+    def maxsamplevalue(self):
+        return load_library().tci_maxsamplevalue(self.h)
+
+    @property
+    def nfeval(self):
+        return load_library().tci_solve_nfeval(self.h)
+
+    def sets(self, b):
+        """(Iset[b], Jset[b]) for 1-based site b as int arrays of 1-based indices."""
+        lib = load_library()
+        nI, nJ = ctypes.c_int64(), ctypes.c_int64()
+        _check(lib.tci_get_sets(self.h, b, None, ctypes.byref(nI), None, ctypes.byref(nJ)))
+        I = np.zeros((nI.value, b - 1), np.int64)
+        J = np.zeros((nJ.value, len(self) - b), np.int64)
+        _check(lib.tci_get_sets(self.h, b, _p(I, I64P), ctypes.byref(nI), _p(J, I64P), ctypes.byref(nJ)))
+        return I, J
+
+    @property
+    def Iset(self):
+        return [self.sets(b)[0] for b in range(1, len(self) + 1)]
+
+    @property
+    def Jset(self):
+        return [self.sets(b)[1] for b in range(1, len(self) + 1)]
+
+    def sitetensor(self, b):
+        lib = load_library()
+        dims = np.zeros(3, np.int64)
+        _check(lib.tci_get_core(self.h, b, None, _p(dims, I64P)))
+        out = np.zeros(int(np.prod(dims)))
+        _check(lib.tci_get_core(self.h, b, _p(out, F64P) if out.size else None, _p(dims, I64P)))
+        return out.reshape(tuple(dims), order="F")
+
+    @property
+    def sitetensors(self):
+        return [self.sitetensor(b) for b in range(1, len(self) + 1)]
+
+    def errors(self):
+        lib = load_library()
+        n = ctypes.c_int64()
+        lib.tci_get_errors(self.h, None, ctypes.byref(n), None)
+        pe = np.zeros(n.value)
+        be = np.zeros(len(self) - 1)
+        lib.tci_get_errors(self.h, _p(pe, F64P) if pe.size else None, ctypes.byref(n), _p(be, F64P))
+        return pe, be
+
+    @property
+    def pivoterrors(self):
+        return self.errors()[0]
+
+    @property
+    def bonderrors(self):
+        return self.errors()[1]
+
+    def pivoterror(self):
+        """pivoterror(tci) = maximum(bonderrors) (tensorci2.jl:157-159)."""
+        return float(self.bonderrors.max())
+
+    def history(self):
+        lib = load_library()
+        n = ctypes.c_int64()
+        lib.tci_get_history(self.h, None, None, None, ctypes.byref(n))
+        r = np.zeros(n.value, np.int64)
+        e = np.zeros(n.value)
+        g = np.zeros(n.value, np.int64)
+        if n.value:
+            lib.tci_get_history(self.h, _p(r, I64P), _p(e, F64P), _p(g, I64P), ctypes.byref(n))
+        return r, e, g
+
+    # ---- tensor train
+    def evaluate(self, points):
+        """evaluate(tci, indexset) for one point or an array of points (1-based)."""
+        pts = np.asarray(points, dtype=np.int64)
+        single = pts.ndim == 1
+        pts = np.ascontiguousarray(pts.reshape(-1, len(self)))
+        out = np.zeros(pts.shape[0])
+        _check(load_library().tci_evaluate(self.h, _p(pts, I64P), pts.shape[0], _p(out, F64P)))
+        return float(out[0]) if single else out
+
+    __call__ = evaluate
+
+    def sum(self):
+        out = ctypes.c_double()
+        _check(load_library().tci_sum(self.h, ctypes.byref(out)))
+        return out.value
+
+    def tensortrain(self):
+        return TensorTrain(self.sitetensors)
+
+
+class TensorTrain:
+    """TensorTrain{Float64,3} (tensortrain.jl:17-31) with host-side cores."""
+
+    def __init__(self, sitetensors):
+        for i in range(len(sitetensors) - 1):
+            if sitetensors[i].shape[-1] != sitetensors[i + 1].shape[0]:
+                raise ArgumentError(TCI_ERR_ARG, f"The tensors at {i + 1} and {i + 2} must have consistent "
+                                    "dimensions for a tensor train.")
+        self.sitetensors = [np.asarray(t, dtype=np.float64) for t in sitetensors]
+
+    def __len__(self):
+        return len(self.sitetensors)
+
+    def linkdims(self):
+        return [t.shape[0] for t in self.sitetensors[1:]]
+
+    def rank(self):
+        return max(self.linkdims())
+
+
+def crossinterpolate2(ValueType, f, localdims, initialpivots=None, ctx=None, **kwargs):
+    """crossinterpolate2 (tensorci2.jl:943-953) -> (tci, ranks, errors)."""
+    if ValueType not in (float, np.float64, "Float64"):
+        raise ArgumentError(TCI_ERR_ARG, "only Float64 is supported")
+    ctx = ctx or default_context()
+    lib = load_library()
+    localdims = [int(d) for d in localdims]
+    L = len(localdims)
+    d = np.ascontiguousarray(localdims, dtype=np.int64)
+    piv = _pivots_array(initialpivots if initialpivots is not None else [np.ones(L)], L)
+    o = make_opts(**kwargs)
+    h = ctypes.c_void_p()
+    _check(lib.tci_crossinterpolate2(ctx.h, L, _p(d, I64P), f.fid, _p(f.params, F64P) if f.params.size else None,
+                                     f.params.size, _p(piv, I64P), piv.shape[0], ctypes.byref(o), ctypes.byref(h)))
+    tci = TensorCI2(f, localdims, ctx=ctx, _handle=h)
+    r, e, _ = tci.history()
+    return tci, r, e
+
+
+def make_requests(specs):
+    """specs: list of (f: DeviceFunction, localdims, opts kwargs).  Keeps buffers alive."""
+    keep = []
+    arr = (Request * len(specs))()
+    for i, (f, localdims, kw) in enumerate(specs):
+        d = np.ascontiguousarray(localdims, dtype=np.int64)
+        keep.append(d)
+        keep.append(f.params)
+        arr[i].L = len(localdims)
+        arr[i].fid = f.fid
+        arr[i].localdims = _p(d, I64P)
+        arr[i].fparams = _p(f.params, F64P) if f.params.size else None
+        arr[i].nparams = f.params.size
+        arr[i].opts = make_opts(**kw)
+    return arr, keep
+
+
+def crossinterpolate2_batched(specs, max_live=0, ctx=None):
+    """Solve many crossinterpolate2 problems together (one launch per step for all)."""
+    ctx = ctx or default_context()
+    arr, keep = make_requests(specs)
+    out = (ctypes.c_void_p * len(specs))()
+    rc = load_library().tci_crossinterpolate2_batched(ctx.h, len(specs), arr, int(max_live), out)
+    res = []
+    for i, (f, localdims, _) in enumerate(specs):
+        res.append(TensorCI2(f, localdims, ctx=ctx, _handle=ctypes.c_void_p(out[i])) if out[i] else None)
+    _check(rc)
+    return res
+
+
+def serve(specs, arrival, max_live=0, ctx=None):
+    """Continuous-batching server over a request stream -> (latency, rank, wall)."""
+    ctx = ctx or default_context()
+    arr, keep = make_requests(specs)
+    arrival = np.ascontiguousarray(arrival, dtype=np.float64)
+    lat = np.zeros(len(specs))
+    rank = np.zeros(len(specs), np.int64)
+    wall = ctypes.c_double()
+    _check(load_library().tci_serve_run(ctx.h, len(specs), arr, _p(arrival, F64P), int(max_live), _p(lat, F64P),
+                                        _p(rank, I64P), ctypes.byref(wall)))
+    return lat, rank, wall.value
+
+
+def feval(f, localdims, points, ctx=None):
+    """Evaluate a registered device function at points (n x L, 1-based) on the GPU."""
+    ctx = ctx or default_context()
+    localdims = np.ascontiguousarray(localdims, dtype=np.int64)
+    pts = np.ascontiguousarray(np.asarray(points, dtype=np.int64).reshape(-1, localdims.size))
+    out = np.zeros(pts.shape[0])
+    _check(load_library().tci_feval(ctx.h, f.fid, _p(f.params, F64P) if f.params.size else None, f.params.size,
+                                    localdims.size, _p(localdims, I64P), _p(pts, I64P), pts.shape[0],
+                                    _p(out, F64P)))
+    return out
+
+
+def convergencecriterion(ranks, errors, nglobalpivots, tolerance, maxbonddim, ncheckhistory,
+                         checkconvglobalpivot=True):
+    """convergencecriterion (tensorci2.jl:609-628); host-side logic of the library."""
+    r = np.ascontiguousarray(ranks, np.int64)
+    e = np.ascontiguousarray(errors, np.float64)
+    g = np.ascontiguousarray(nglobalpivots, np.int64)
+    return bool(load_library().tci_convergencecriterion(_p(r, I64P), _p(e, F64P), _p(g, I64P), r.size, tolerance,
+                                                        maxbonddim, ncheckhistory, int(bool(checkconvglobalpivot))))
+
+
+def fp64_peak(ctx=None):
+    """Measured FP64 operations per second: (separate mul+sub, fused)."""
+    ctx = ctx or default_context()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(load_library().tci_fp64_peak(ctx.stream, ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
+
+
+# ---------------------------------------------------------------- rrLU
+class rrLU:
+    """Result of rrlu (matrixlu.jl:71-96): 1-based permutations, L, U."""
+
+    def __init__(self, rowpermutation, colpermutation, L, U, leftorthogonal, npivot, error):
+        self.rowpermutation = rowpermutation
+        self.colpermutation = colpermutation
+        self.L = L
+        self.U = U
+        self.leftorthogonal = leftorthogonal
+        self.npivot = npivot
+        self.error = error
+
+    @property
+    def shape(self):
+        return (self.L.shape[0], self.U.shape[1])
+
+    def rowindices(self):
+        return self.rowpermutation[: self.npivot]
+
+    def colindices(self):
+        return self.colpermutation[: self.npivot]
+
+    def npivots(self):
+        return self.npivot
+
+    def left(self, permute=True):
+        if not permute:
+            return self.L
+        out = np.empty_like(self.L)
+        out[self.rowpermutation - 1, :] = self.L
+        return out
+
+    def right(self, permute=True):
+        if not permute:
+            return self.U
+        out = np.empty_like(self.U)
+        out[:, self.colpermutation - 1] = self.U
+        return out
+
+    def diag(self):
+        K = self.npivot
+        return np.diag(self.U[:K, :K]) if self.leftorthogonal else np.diag(self.L[:K, :K])
+
+    def pivoterrors(self):
+        return np.concatenate([np.abs(self.diag()), [self.error]])
+
+    def lastpivoterror(self):
+        return self.error
+
+
+def rrlu(A, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True, ctx=None):
+    """rrlu(A; maxrank, reltol, abstol, leftorthogonal) (matrixlu.jl:217-225) on the GPU."""
+    ctx = ctx or default_context()
+    A = np.asarray(A, dtype=np.float64)
+    m, n = A.shape
+    k = min(m, n)
+    flat = np.ascontiguousarray(A.reshape(-1, order="F"))
+    rp = np.zeros(m, np.int64)
+    cp = np.zeros(n, np.int64)
+    Lb = np.zeros(max(m * k, 1))
+    Ub = np.zeros(max(k * n, 1))
+    npiv = ctypes.c_int64()
+    err = ctypes.c_double()
+    _check(load_library().tci_rrlu(ctx.h, _p(flat, F64P), m, n, 0 if maxrank is None else int(maxrank), reltol,
+                                   abstol, int(bool(leftorthogonal)), _p(rp, I64P), _p(cp, I64P), _p(Lb, F64P),
+                                   _p(Ub, F64P), ctypes.byref(npiv), ctypes.byref(err)))
+    K = npiv.value
+    return rrLU(rp, cp, Lb[: m * K].reshape((m, K), order="F").copy(), Ub[: K * n].reshape((K, n), order="F").copy(),
+                bool(leftorthogonal), K, err.value)
+
+
+def rrlu_batched(mats, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True, ctx=None):
+    """Many independent rrLUs in one launch -> list of (rows, cols, npivot, error), 1-based."""
+    ctx = ctx or default_context()
+    ms = np.array([a.shape[0] for a in mats], np.int64)
+    ns = np.array([a.shape[1] for a in mats], np.int64)
+    offs = np.concatenate([[0], np.cumsum(ms * ns)[:-1]]).astype(np.int64)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(a, np.float64).reshape(-1, order="F") for a in mats]))
+    kcap = np.minimum(np.minimum(ms, ns), maxrank if maxrank else np.iinfo(np.int64).max)
+    poffs = np.concatenate([[0], np.cumsum(2 * kcap)[:-1]]).astype(np.int64)
+    piv = np.zeros(int(2 * kcap.sum()) + 1, np.int64)
+    npiv = np.zeros(len(mats), np.int64)
+    errs = np.zeros(len(mats))
+    _check(load_library().tci_rrlu_batched(ctx.h, len(mats), _p(flat, F64P), _p(offs, I64P), _p(ms, I64P),
+                                           _p(ns, I64P), 0 if maxrank is None else int(maxrank), reltol, abstol,
+                                           int(bool(leftorthogonal)), _p(piv, I64P), _p(poffs, I64P),
+                                           _p(npiv, I64P), _p(errs, F64P)))
+    out = []
+    for i in range(len(mats)):
+        K = int(npiv[i])
+        o = poffs[i]
+        out.append((piv[o:o + K].copy(), piv[o + kcap[i]:o + kcap[i] + K].copy(), K, float(errs[i])))
+    return out

@@ -1,0 +1,108 @@
+"""Extract the reference's own known-answer data for the TCI2 path into JSON.
+
+Reads the literal matrices of TensorCrossInterpolation.jl's tests as text
+(test/test_matrixlu.jl, test/test_matrixluci.jl) and records, beside each, the
+assertion the reference test makes about it.  Run in a checkout that has the
+reference:
+
+    python tests/golden/make_golden.py /path/to/TensorCrossInterpolation.jl
+
+The output, tests/golden/reference_known_answers.json, is committed; the tests
+never read the reference itself.
+"""
+import json
+import os
+import re
+import sys
+
+
+def parse_matrix_literals(text):
+    """Return {line_number: matrix} for every multi-line `NAME = [ ... ]` literal."""
+    lines = text.splitlines()
+    out = {}
+    i = 0
+    while i < len(lines):
+        m = re.match(r"\s*(\w+)\s*=\s*(?:([0-9.e+-]+)\s*\*\s*)?\[\s*$", lines[i])
+        if m:
+            scale = float(m.group(2)) if m.group(2) else 1.0
+            rows = []
+            j = i + 1
+            while j < len(lines) and lines[j].strip() != "]":
+                row = [float(x) for x in lines[j].replace(";", " ").split()]
+                if row:
+                    rows.append([scale * x for x in row])
+                j += 1
+            out[i + 1] = {"name": m.group(1), "rows": rows}
+            i = j
+        i += 1
+    return out
+
+
+def main(ref):
+    lu_text = open(os.path.join(ref, "test", "test_matrixlu.jl")).read()
+    luci_text = open(os.path.join(ref, "test", "test_matrixluci.jl")).read()
+    lu = parse_matrix_literals(lu_text)
+    luci = parse_matrix_literals(luci_text)
+
+    def find(mats, start, name):
+        for ln, m in sorted(mats.items()):
+            if ln >= start and m["name"] == name:
+                return m["rows"]
+        raise KeyError((start, name))
+
+    cases = [
+        {"source": "test/test_matrixlu.jl:54-69", "A": find(lu, 54, "A"), "kwargs": {},
+         "expect": {"left_right_approx_A": True, "L_unit_lower": True, "U_upper": True}},
+        {"source": "test/test_matrixlu.jl:88-97", "A": find(lu, 88, "A"), "kwargs": {},
+         "expect": {"npivot": 1}},
+        {"source": "test/test_matrixlu.jl:99-121", "A": find(lu, 99, "A"), "kwargs": {"maxrank": 4},
+         "expect": {"npivot": 4, "L_lower": True, "U_upper": True}},
+        {"source": "test/test_matrixlu.jl:167-175", "A": [[1.0, 0.0], [0.0, 1.0]], "kwargs": {},
+         "expect": {"pivoterrors": [1.0, 1.0, 0.0], "lastpivoterror": 0.0}},
+        {"source": "test/test_matrixlu.jl:177-195 (maxrank=2)", "A": find(lu, 177, "A"),
+         "kwargs": {"maxrank": 2}, "expect": {"n_pivoterrors": 3, "lastpivoterror_positive": True}},
+        {"source": "test/test_matrixlu.jl:177-195 (abstol=0.5)", "A": find(lu, 177, "A"),
+         "kwargs": {"abstol": 0.5}, "expect": {"lastpivoterror_below": 0.5}},
+        {"source": "test/test_matrixlu.jl:177-195 (abstol=0)", "A": find(lu, 177, "A"),
+         "kwargs": {"abstol": 0.0}, "expect": {"lastpivoterror": 0.0}},
+        {"source": "test/test_matrixlu.jl:197-211", "A": find(lu, 197, "A"), "kwargs": {"abstol": 1e-3},
+         "expect": {"npivot": 1, "lastpivoterror_positive": True, "max_abs_residual_below": 1e-3}},
+    ]
+    p = find(lu, 141, "p")
+    q = find(lu, 141, "q")
+    lowrank = {"source": "test/test_matrixlu.jl:141-165", "p": p, "q": q, "expect": {"npivot": 3}}
+    luci_case = {"source": "test/test_matrixluci.jl:6-37", "A": find(luci, 6, "A"), "kwargs": {"maxrank": 4},
+                 "expect": {"npivot": 4, "colstimespivotinv_is_leftmatrix": True}}
+    tci = {
+        "pivoterrors": {"source": "test/test_tensorci2.jl:27-39", "diags": [1.0, 1e-5, 0.0],
+                        "localdims": [3, 3], "tolerance": 1e-8, "expect_pivoterrors": [1.0, 1e-5, 0.0]},
+        "lorentz": {"source": "test/test_tensorci2.jl:247-339", "n": 5, "localdim": 10,
+                    "maxbonddim2_linkdims": [2, 2, 2, 2], "globalpivot": [2, 9, 10, 5, 7],
+                    "after_globalpivot_linkdims": [3, 3, 3, 3], "tol3_pivoterror_max": 2e-12,
+                    "initialpivots4": [[1, 1, 1, 1, 1], [10, 8, 10, 4, 4], [5, 4, 8, 9, 3], [7, 7, 10, 5, 9],
+                                       [7, 7, 10, 5, 9]]},
+        "convergencecriterion": {
+            "source": "test/test_tensorci2.jl:504-554",
+            "cases": [
+                {"ranks": [1, 2], "errors": [1e-2, 1e-5], "ngp": [0, 0], "tol": 1e-4, "maxbonddim": 4,
+                 "ncheck": 3, "expect": False},
+                {"ranks": [1, 2, 2, 2], "errors": [1e-2, 1e-5, 1e-5, 1e-5], "ngp": [0, 0, 0, 0], "tol": 1e-4,
+                 "maxbonddim": 4, "ncheck": 3, "expect": True},
+                {"ranks": [1, 2, 2, 2], "errors": [1e-2, 1e-2, 1e-5, 1e-5], "ngp": [0, 0, 0, 0], "tol": 1e-4,
+                 "maxbonddim": 4, "ncheck": 3, "expect": False},
+                {"ranks": [1, 2, 2, 2], "errors": [1e-2, 1e-2, 1e-2, 1e-2], "ngp": [0, 0, 0, 0], "tol": 1e-4,
+                 "maxbonddim": 2, "ncheck": 3, "expect": True},
+                {"ranks": [1, 2, 2, 2], "errors": [1e-2, 1e-2, 1e-2, 1e-2], "ngp": [0, 1, 1, 1], "tol": 1e-4,
+                 "maxbonddim": 2, "ncheck": 3, "expect": True},
+            ]},
+    }
+    out = {"reference": "TensorCrossInterpolation.jl 0.9.19", "rrlu": cases, "rrlu_lowrank": lowrank,
+           "luci": luci_case, "tci2": tci}
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")
+    with open(dst, "w") as fh:
+        json.dump(out, fh, indent=1)
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,177 @@
+"""GPU crossinterpolate2 / TensorCI2 against the CPU oracle.
+
+The registered functions evaluate bit-identically on both sides and the rrLU is
+bit-exact, so pivot index sets and ranks must match exactly.  Site tensors come
+from a different (but stable) solve of T = Pi1 * inv(P) than the reference's
+LAPACK call and are compared to a tolerance; so are evaluate() and sum().
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_sets(tci, ref):
+    L = len(tci)
+    for b in range(1, L + 1):
+        gi, gj = tci.sets(b)
+        ri, rj = ref.sets(b)
+        assert np.array_equal(gi, ri), f"Iset[{b}] differs"
+        assert np.array_equal(gj, rj), f"Jset[{b}] differs"
+
+
+def test_pivoterrors_known_answer(T, golden):
+    g = golden["tci2"]["pivoterrors"]
+    f = T.DeviceFunction.dense(np.diag(g["diags"]))
+    tci, _, _ = T.crossinterpolate2(float, f, g["localdims"], [[1, 1]], tolerance=g["tolerance"])
+    assert list(tci.pivoterrors) == g["expect_pivoterrors"]
+
+
+def test_lorentz_updatepivots_known_answers(T, oracle, golden):
+    g = golden["tci2"]["lorentz"]
+    n, d = g["n"], g["localdim"]
+    f = T.DeviceFunction("lorentz")
+    tci = T.TensorCI2(f, [d] * n)
+    ref = oracle.OracleTCI.new([d] * n, oracle.F_LORENTZ)
+    assert list(tci.linkdims()) == [1] * (n - 1)
+    for p in range(1, n):
+        tci.updatepivots(p, True, reltol=1e-8, maxbonddim=2)
+        ref.updatepivots(p, True, reltol=1e-8, maxbonddim=2)
+    assert list(tci.linkdims()) == g["maxbonddim2_linkdims"]
+    _same_sets(tci, ref)
+    tci.addglobalpivots1sitesweep([g["globalpivot"]], reltol=1e-12)
+    ref.addglobalpivots1sitesweep([g["globalpivot"]], reltol=1e-12)
+    assert list(tci.linkdims()) == g["after_globalpivot_linkdims"]
+    _same_sets(tci, ref)
+    for _ in range(4, 21):
+        for p in range(1, n):
+            tci.updatepivots(p, True, reltol=1e-8)
+            ref.updatepivots(p, True, reltol=1e-8)
+    _same_sets(tci, ref)
+    tci2, _, _ = T.crossinterpolate2(float, f, [d] * n, tolerance=1e-8, maxiter=8, sweepstrategy="forward")
+    assert tci.rank() == tci2.rank()
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-8, 1e-12])
+def test_lorentz5_parity(T, oracle, tol):
+    f = T.DeviceFunction("lorentz")
+    tci, ranks, errors = T.crossinterpolate2(float, f, [10] * 5, tolerance=tol, maxiter=200)
+    ref, rranks, rerrors = oracle.crossinterpolate2([10] * 5, oracle.F_LORENTZ, (), None, tolerance=tol,
+                                                    maxiter=200)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    assert np.array_equal(tci.bonderrors, ref.errors()[1])
+    pts = np.array(list(itertools.product(*[range(1, 4)] * 5)))
+    assert np.allclose(tci.evaluate(pts), 1.0 / (1.0 + (pts ** 2).sum(1)), rtol=max(tol, 1e-12) * 10)
+    for b in range(1, 6):
+        assert np.allclose(tci.sitetensor(b), ref.core(b), rtol=1e-9, atol=1e-12)
+
+
+def test_config1_lorentz8(T, oracle):
+    """8-site Lorentzian, tolerance 1e-8, maxbonddim 200, all-ones pivot: pivots
+    and ranks bit-exact, max error on 1e5 seeded lattice points within tolerance
+    and at most 2x the oracle's, sum to 1e-12 relative."""
+    f = T.DeviceFunction("lorentz")
+    kw = dict(tolerance=1e-8, maxbonddim=200, maxiter=20)
+    tci, ranks, errors = T.crossinterpolate2(float, f, [10] * 8, **kw)
+    ref, rranks, rerrors = oracle.crossinterpolate2([10] * 8, oracle.F_LORENTZ, (), None, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    pts = np.random.default_rng(1234).integers(1, 11, size=(100000, 8))
+    fx = 1.0 / (1.0 + (pts ** 2).sum(1))
+    err_gpu = np.max(np.abs(tci.evaluate(pts) - fx))
+    err_ref = np.max(np.abs(ref.evaluate(pts) - fx))
+    assert err_gpu <= 1e-8 * tci.maxsamplevalue * 10
+    assert err_gpu <= 2 * err_ref + 1e-15
+    s, sr = tci.sum(), ref.sum()
+    assert abs(s - sr) <= 1e-12 * abs(sr)
+
+
+def _served(rng, L, d):
+    a, b, g = 10 ** rng.uniform(-2, 1, size=3)
+    c = rng.integers(1, d + 1, size=L)
+    return [a, b, g] + list(c)
+
+
+def test_served_family_parity(T, oracle):
+    rng = np.random.default_rng(42)
+    for _ in range(6):
+        L = int(rng.integers(4, 12))
+        d = int(rng.integers(2, 12))
+        prm = _served(rng, L, d)
+        tol = 10 ** rng.uniform(-10, -6)
+        mbd = int(rng.choice([32, 64, 128, 256]))
+        tci, ranks, _ = T.crossinterpolate2(float, T.DeviceFunction("served", prm), [d] * L, tolerance=tol,
+                                            maxbonddim=mbd)
+        ref, rranks, _ = oracle.crossinterpolate2([d] * L, oracle.F_SERVED, prm, None, tolerance=tol,
+                                                  maxbonddim=mbd)
+        assert list(ranks) == list(rranks)
+        _same_sets(tci, ref)
+        pts = np.stack([rng.integers(1, d + 1, size=2000) for _ in range(L)], 1)
+        assert np.allclose(tci.evaluate(pts), ref.evaluate(pts), rtol=1e-9, atol=1e-12 * ref.maxsamplevalue)
+
+
+def test_quantics_1d(T, oracle):
+    """Quantics R=40, tolerance 1e-10, maxbonddim 128 (the split-precision
+    config's TCI part)."""
+    f = T.DeviceFunction("qtt1d", [0])
+    kw = dict(tolerance=1e-10, maxbonddim=128, maxiter=20)
+    tci, ranks, _ = T.crossinterpolate2(float, f, [2] * 40, **kw)
+    ref, rranks, _ = oracle.crossinterpolate2([2] * 40, oracle.F_QTT1D, [0], None, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    assert abs(tci.sum() - ref.sum()) <= 1e-12 * abs(ref.sum()) + 1e-15
+
+
+def test_batched_equals_alone(T):
+    """Each solve gives the same pivots alone and in a batch with others."""
+    rng = np.random.default_rng(3)
+    specs = []
+    for _ in range(12):
+        L = int(rng.integers(4, 10))
+        d = int(rng.integers(2, 10))
+        specs.append((T.DeviceFunction("served", _served(rng, L, d)), [d] * L,
+                      dict(tolerance=10 ** rng.uniform(-10, -6), maxbonddim=64)))
+    batch = T.crossinterpolate2_batched(specs, max_live=5)
+    for (f, dims, kw), tb in zip(specs, batch):
+        ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
+        assert list(tb.linkdims()) == list(ta.linkdims())
+        for b in range(1, len(dims) + 1):
+            assert np.array_equal(tb.sets(b)[0], ta.sets(b)[0])
+            assert np.array_equal(tb.sets(b)[1], ta.sets(b)[1])
+        assert np.array_equal(tb.sitetensor(1), ta.sitetensor(1))
+
+
+def test_serve_stream(T):
+    rng = np.random.default_rng(5)
+    specs = []
+    for _ in range(30):
+        L = int(rng.integers(4, 9))
+        d = int(rng.integers(2, 9))
+        specs.append((T.DeviceFunction("served", _served(rng, L, d)), [d] * L,
+                      dict(tolerance=10 ** rng.uniform(-10, -6), maxbonddim=32)))
+    arrival = np.cumsum(rng.exponential(1 / 500.0, size=len(specs)))
+    lat, rank, wall = T.serve(specs, arrival, max_live=16)
+    assert np.all(lat > 0) and np.all(rank >= 1)
+    for i in [0, 7, 29]:
+        f, dims, kw = specs[i]
+        ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
+        assert ta.rank() == rank[i]
+
+
+def test_errors_like_reference(T):
+    f = T.DeviceFunction("lorentz")
+    with pytest.raises(T.ArgumentError):  # tensorci2.jl:750-754
+        T.crossinterpolate2(float, f, [2] * 5, tolerance=0.0)
+    with pytest.raises(T.DimensionMismatch):  # tensorci2.jl:197-199
+        tci = T.TensorCI2(f, [3] * 4)
+        tci.addglobalpivots([[1, 2, 3]])
+    z = T.DeviceFunction.dense(np.zeros((3, 3)))
+    with pytest.raises(T.TCIError, match="maxsamplevalue is zero"):  # tensorci2.jl:50
+        T.TensorCI2(z, [3, 3])
+    bad = np.ones((3, 3))
+    bad[1, 2] = np.nan
+    with pytest.raises(T.TCIError, match="NaN"):
+        T.crossinterpolate2(float, T.DeviceFunction.dense(bad), [3, 3])
