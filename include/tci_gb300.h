@@ -141,6 +141,12 @@ int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t
 /* Site tensor b (1-based), column-major r_{b-1} x d_b x r_b; dims[3] out.
  * Pass NULL `out` to query dims.  Fails if site tensors are invalidated. */
 int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims);
+/* All site tensors of n solves in one device-to-host copy: solve i's tensors,
+ * site by site (each column-major), start at out + out_offsets[i]; offsets must
+ * be contiguous (offset[i+1] = offset[i] + sum of solve i's tensor sizes).
+ * The TensorTrain(tci) conversion (tensortrain.jl:62-64) for a batch. */
+int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
+                          const int64_t* out_offsets);
 /* pivoterrors (length *npe) and bonderrors (L-1) (tensorci2.jl:13-16). */
 int tci_get_errors(const tci_solve* s, double* pivoterrors, int64_t* npe, double* bonderrors);
 /* ranks, errors (normalised) and number of global pivots per iteration of the

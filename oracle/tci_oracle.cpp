@@ -713,13 +713,47 @@ std::vector<MultiIndex> default_global_pivots(TCI2& t, double abstol, int nsearc
     starts.push_back(p);
   }
   std::vector<MultiIndex> found;
+  const auto& C = t.sitetensors;
   for (const auto& point : starts) {
+    // The train at the start point with site q changed is the product
+    // Le_q * C_q[:, v, :] * Re_q of the start's left and right environments
+    // (the same matrix products as evaluate(), associated around site q).
+    std::vector<std::vector<double>> Le(L), Re(L);
+    Le[0].assign(1, 1.0);
+    for (int q = 0; q + 1 < L; ++q) {
+      const Tensor3& T = C[q];
+      const i64 i = point[q] - 1;
+      Le[q + 1].assign((size_t)T.d2, 0.0);
+      for (i64 b = 0; b < T.d2; ++b) {
+        double acc = 0.0;
+        for (i64 a = 0; a < T.d0; ++a) acc = acc + Le[q][a] * T.v[a + T.d0 * (i + T.d1 * b)];
+        Le[q + 1][b] = acc;
+      }
+    }
+    Re[L - 1].assign(1, 1.0);
+    for (int q = L - 1; q > 0; --q) {
+      const Tensor3& T = C[q];
+      const i64 i = point[q] - 1;
+      Re[q - 1].assign((size_t)T.d0, 0.0);
+      for (i64 a = 0; a < T.d0; ++a) {
+        double acc = 0.0;
+        for (i64 b = 0; b < T.d2; ++b) acc = acc + T.v[a + T.d0 * (i + T.d1 * b)] * Re[q][b];
+        Re[q - 1][a] = acc;
+      }
+    }
     MultiIndex cur = point, best = point;
     double best_error = 0.0;
     for (int q = 0; q < L; ++q) {
+      const Tensor3& T = C[q];
       for (int v = 1; v <= t.localdims[q]; ++v) {
         cur[q] = v;
-        double err = std::fabs(t.f(cur) - tt_evaluate(t.sitetensors, cur));
+        double val = 0.0;
+        for (i64 b = 0; b < T.d2; ++b) {
+          double w = 0.0;
+          for (i64 a = 0; a < T.d0; ++a) w = w + Le[q][a] * T.v[a + T.d0 * ((v - 1) + T.d1 * b)];
+          val = val + w * Re[q][b];
+        }
+        double err = std::fabs(t.f(cur) - val);
         t.nfeval += 1;
         if (err > best_error) {
           best_error = err;

@@ -26,6 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = {
     "step_kernel.cu": ["-fmad=false"],
     "peak.cu": [],
+    "gather.cu": [],
 }
 CXX_SOURCES = ["engine.cpp", "capi.cpp"]
 HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h"]

@@ -8,15 +8,22 @@
 #include <mutex>
 #include <optional>
 #include <thread>
+#include <cstdlib>
+#include <algorithm>
 
 #include "engine.h"
 
 using namespace tci;
 
+// A context owns a pool of engines, each with its own stream and buffers.
+// Single-solve entry points use the first; batched solves and the server spread
+// solves over all of them so that one engine's host work and kernel tail
+// overlap the others' kernels.
 struct tci_ctx {
-  Engine eng;
+  std::vector<std::unique_ptr<Engine>> pool;
+  Engine& eng;
   std::mutex mu;
-  explicit tci_ctx(int dev) : eng(dev) {}
+  explicit tci_ctx(std::vector<std::unique_ptr<Engine>>&& p) : pool(std::move(p)), eng(*pool[0]) {}
 };
 
 struct tci_solve {
@@ -104,18 +111,21 @@ int tci_f_lookup(const char* name, int* fid) {
 
 int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
   *out = nullptr;
-  auto* c = new tci_ctx(device);
-  int rc = c->eng.init();
-  if (rc) {
-    delete c;
-    return rc;
+  int neng = 4;
+  if (const char* s = std::getenv("TCI_ENGINES")) neng = std::max(1, std::min(16, std::atoi(s)));
+  std::vector<std::unique_ptr<Engine>> pool;
+  for (int i = 0; i < neng; ++i) {
+    pool.emplace_back(new Engine(device));
+    int rc = pool.back()->init();
+    if (rc) return rc;
   }
+  auto* c = new tci_ctx(std::move(pool));
   if (hbm_budget == 0) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     hbm_budget = (size_t)(0.8 * (double)fr);
   }
-  c->eng.hbm_budget = hbm_budget;
+  for (auto& e : c->pool) e->hbm_budget = hbm_budget;
   *out = c;
   return 0;
 }
@@ -128,13 +138,28 @@ int tci_ctx_destroy(tci_ctx* ctx) {
 uintptr_t tci_ctx_stream(tci_ctx* ctx) { return (uintptr_t)ctx->eng.stream(); }
 
 int tci_ctx_synchronize(tci_ctx* ctx) {
-  cudaError_t e = cudaStreamSynchronize(ctx->eng.stream());
-  return e == cudaSuccess ? 0 : fail(TCI_ERR_CUDA, cudaGetErrorString(e));
+  for (auto& eng : ctx->pool) {
+    cudaError_t e = cudaStreamSynchronize(eng->stream());
+    if (e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return 0;
 }
 
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
-  *out = ctx->eng.stats;
-  if (reset) ctx->eng.stats = tci_stats{};
+  tci_stats t{};
+  for (auto& e : ctx->pool) {
+    const tci_stats& s = e->stats;
+    t.steps += s.steps;
+    t.launches += s.launches;
+    t.tasks += s.tasks;
+    t.kernel_ms += s.kernel_ms;
+    t.feval += s.feval;
+    t.lu_updates += s.lu_updates;
+    t.h2d_bytes += s.h2d_bytes;
+    t.d2h_bytes += s.d2h_bytes;
+    if (reset) e->stats = tci_stats{};
+  }
+  *out = t;
   return 0;
 }
 
@@ -318,6 +343,28 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
   return 0;
 }
 
+int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
+                          const int64_t* out_offsets) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::vector<const double*> src;
+  std::vector<int64_t> len;
+  int64_t expect = -1;
+  for (int64_t i = 0; i < n; ++i) {
+    const Solve& s = solves[i]->s;
+    if (!s.cores_valid) return fail(TCI_ERR_GENERIC, "site tensors are not available");
+    int64_t pos = out_offsets[i];
+    if (expect >= 0 && pos != expect) return fail(TCI_ERR_ARG, "out_offsets must be contiguous");
+    for (const Core& c : s.cores) {
+      src.push_back(c.p);
+      len.push_back((int64_t)c.elems());
+      pos += (int64_t)c.elems();
+    }
+    expect = pos;
+  }
+  if (n == 0) return 0;
+  return ctx->eng.gather_to_host(src, len, out + out_offsets[0]);
+}
+
 int tci_get_errors(const tci_solve* s, double* pivoterrors, int64_t* npe, double* bonderrors) {
   *npe = (int64_t)s->s.pivoterrors.size();
   if (pivoterrors) std::copy(s->s.pivoterrors.begin(), s->s.pivoterrors.end(), pivoterrors);
@@ -369,18 +416,27 @@ struct Job {
   int rc = 0;
 };
 
-// Drive jobs with continuous batching.  arrival==nullptr: all available at t=0.
+// Drive jobs with continuous batching over the context's engine pool.
+// arrival == nullptr: every request is available at t = 0.  Each admitted solve
+// is bound to the engine with the fewest live solves.  The loop completes
+// whichever engine's batch is ready (resuming its solves, which queue their
+// next tasks), relaunches it at once, and admits new requests between steps
+// while the live count and the HBM estimate allow.
 int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
           std::vector<Job>& jobs, bool keep) {
-  Engine& e = ctx->eng;
+  auto& pool = ctx->pool;
+  const int G = (int)pool.size();
   jobs.clear();
   jobs.resize((size_t)n);
   if (max_live <= 0) max_live = n;
   const double t0 = now_s();
   int64_t next = 0, live = 0, finished = 0;
   double live_bytes = 0;
+  const double budget = (double)pool[0]->hbm_budget;
   std::vector<double> est(n);
   for (int64_t i = 0; i < n; ++i) est[i] = solve_estimate_bytes(reqs[i]);
+  std::vector<std::vector<int64_t>> live_on(G);  // live job ids per engine
+  std::vector<int> job_engine(n, 0);
   int first_rc = 0;
   auto finish = [&](Job& j, int64_t i) {
     j.done = true;
@@ -391,19 +447,29 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
     --live;
     ++finished;
     live_bytes -= est[i];
-    if (!keep) e.release_cores(j.solve->s);
+    if (!keep) pool[job_engine[i]]->release_cores(j.solve->s);
+  };
+  auto reap = [&](int g) {
+    auto& lst = live_on[g];
+    size_t w = 0;
+    for (size_t k = 0; k < lst.size(); ++k) {
+      Job& j = jobs[lst[k]];
+      if (j.task && j.task->h.done())
+        finish(j, lst[k]);
+      else
+        lst[w++] = lst[k];
+    }
+    lst.resize(w);
   };
   while (finished < n) {
     double t = now_s() - t0;
     while (next < n && live < max_live && (!arrival || arrival[next] <= t) &&
-           (live == 0 || live_bytes + est[next] <= (double)e.hbm_budget)) {
+           (live == 0 || live_bytes + est[next] <= budget)) {
       Job& j = jobs[next];
       j.arrival = arrival ? arrival[next] : 0.0;
       j.t_start = t;
       const tci_request& r = reqs[next];
       int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
-      std::vector<std::vector<uint8_t>> piv;
-      if (!rc) piv.push_back(std::vector<uint8_t>(r.L, 0));
       if (rc) {
         j.started = j.done = true;
         j.rc = rc;
@@ -412,30 +478,51 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
         ++next;
         continue;
       }
-      j.task.emplace(co_crossinterpolate2(e, j.solve->s, piv, r.opts));
+      int g = 0;
+      for (int k = 1; k < G; ++k)
+        if (live_on[k].size() < live_on[g].size()) g = k;
+      job_engine[next] = g;
+      std::vector<std::vector<uint8_t>> piv(1, std::vector<uint8_t>(r.L, 0));
+      j.task.emplace(co_crossinterpolate2(*pool[g], j.solve->s, piv, r.opts));
       j.started = true;
       ++live;
       live_bytes += est[next];
+      live_on[g].push_back(next);
       j.task->h.resume();
-      if (j.task->h.done()) finish(j, next);
       ++next;
     }
-    if (e.idle()) {
-      if (finished >= n) break;
-      if (live == 0 && next < n && arrival) {
-        double wait = arrival[next] - (now_s() - t0);
-        if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
-        continue;
+    bool progressed = false;
+    for (int g = 0; g < G; ++g) {
+      Engine& e = *pool[g];
+      if (e.inflight() && e.ready()) {
+        int rc = e.complete();
+        if (rc) return rc;
+        progressed = true;
       }
-      if (live > 0) return fail(TCI_ERR_GENERIC, "engine stalled with live solves");
+      reap(g);
+      if (!e.inflight() && !e.idle()) {
+        int rc = e.launch();
+        if (rc) return rc;
+        progressed = true;
+      }
+    }
+    if (progressed || finished >= n) continue;
+    // nothing ready: block on the first batch in flight, or wait for arrivals
+    int busy = -1;
+    for (int g = 0; g < G && busy < 0; ++g)
+      if (pool[g]->inflight()) busy = g;
+    if (busy >= 0) {
+      int rc = pool[busy]->complete();
+      if (rc) return rc;
+      reap(busy);
       continue;
     }
-    int rc = e.step();
-    if (rc) return rc;
-    for (int64_t i = 0; i < next; ++i) {
-      Job& j = jobs[i];
-      if (j.started && !j.done && j.task && j.task->h.done()) finish(j, i);
+    if (live == 0 && next < n && arrival) {
+      double wait = arrival[next] - (now_s() - t0);
+      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
+      continue;
     }
+    if (live > 0) return fail(TCI_ERR_GENERIC, "engine stalled with live solves");
   }
   return first_rc;
 }

@@ -9,12 +9,15 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <cstdio>
+#include <cstdlib>
 #include <numeric>
 
 cudaError_t tci_step_configure();
 size_t tci_step_smem_bytes();
 cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
                             int* counter_dev, int grid, cudaStream_t stream);
+cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
 
 namespace tci {
 
@@ -134,6 +137,7 @@ int GpuOp::await_resume() const noexcept { return status; }
 Engine::Engine(int device) : device_(device) {}
 
 Engine::~Engine() {
+  if (task_log_) std::fflush(task_log_);
   if (stream_) cudaStreamSynchronize(stream_);
   if (hblob_) cudaFreeHost(hblob_);
   if (hres_) cudaFreeHost(hres_);
@@ -143,6 +147,9 @@ Engine::~Engine() {
   if (dcounter_) cudaFree(dcounter_);
   if (ev0_) cudaEventDestroy(ev0_);
   if (ev1_) cudaEventDestroy(ev1_);
+  if (done_) cudaEventDestroy(done_);
+  if (hgat_) cudaFreeHost(hgat_);
+  if (dgat_) cudaFree(dgat_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -161,6 +168,7 @@ int Engine::init() {
   CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&ev0_));
   CUDA_TRY(cudaEventCreate(&ev1_));
+  CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
   CUDA_TRY(tci_step_configure());
   smem_bytes = tci_step_smem_bytes();
   CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device_));
@@ -169,6 +177,13 @@ int Engine::init() {
   CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, device_));
   uint64_t thr = UINT64_MAX;
   CUDA_TRY(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  // Optional per-task trace (step kind m n r npivot cycles smem lut), for tuning.
+  // One stream shared by every engine of the process (lines stay whole).
+  static FILE* shared_log = [] {
+    const char* path = std::getenv("TCI_TASK_LOG");
+    return path ? std::fopen(path, "a") : (FILE*)nullptr;
+  }();
+  task_log_ = shared_log;
   return 0;
 }
 
@@ -272,6 +287,9 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
     case TCI_TASK_SUM:
       t.smem_mode = 1;
       return 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
+    case TCI_TASK_SEARCH:  // t.n = sum of the left and right bond sizes
+      t.smem_mode = 1;
+      return a16((size_t)3 * (t.L + 1) * 4) + (size_t)t.n * 8 <= smem;
     default:
       return false;
   }
@@ -284,6 +302,7 @@ static size_t result_bytes(const tci_task& t) {
     case TCI_TASK_SITE:
       return a16(h + 2 * a8((size_t)t.kcap * 4) + (size_t)t.kcap * 8);
     case TCI_TASK_EVAL:
+    case TCI_TASK_SEARCH:
       return a16(h + 2 * (size_t)t.m * 8);
     default:
       return a16(h);
@@ -301,16 +320,28 @@ static int64_t task_cost(const tci_task& t) {
       return m * n * 40;
     case TCI_TASK_EVAL:
       return m * (40 + (int64_t)t.L * t.r * t.r);
+    case TCI_TASK_SEARCH:
+      return (m + 2 * (int64_t)t.L) * (int64_t)t.r * t.r * 2 + m * 40;
     default:
       return 1;
   }
 }
 
 int Engine::step() {
-  if (pending_.empty()) return 0;
-  std::vector<Req*> batch;
+  int rc = launch();
+  if (rc) return rc;
+  return complete();
+}
+
+bool Engine::ready() const { return !inflight_ || cudaEventQuery(done_) != cudaErrorNotReady; }
+
+int Engine::launch() {
+  if (pending_.empty() || inflight_) return 0;
+  std::vector<Req*>& batch = fl_batch_;
+  batch.clear();
   batch.swap(pending_);
-  std::vector<Waiter> waiters;
+  std::vector<Waiter>& waiters = fl_waiters_;
+  waiters.clear();
   waiters.swap(waiters_);
   const size_t nt = batch.size();
 
@@ -346,13 +377,17 @@ int Engine::step() {
       }
     }
     set_error(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
+    batch.clear();
+    waiters.clear();
+    // pending_/waiters_ were emptied above: requeue the runnable tasks, then let
+    // the failed solves continue (whatever they enqueue lands behind them)
+    for (Req* r : good) pending_.push_back(r);
+    for (auto& w : goodw) waiters_.push_back(w);
     for (auto& w : badw) {
       w.op->status = TCI_ERR_TOO_LARGE;
       w.h.resume();
     }
-    for (Req* r : good) pending_.push_back(r);
-    for (auto& w : goodw) waiters_.push_back(w);
-    return 0;
+    return launch();
   }
   for (size_t i = 0; i < nt; ++i) {
     Req& r = *batch[i];
@@ -374,12 +409,16 @@ int Engine::step() {
     res_total += r.res_bytes;
     o_work[i] = work_total;
     work_total += we;
+    if (r.t.lutcap0 > 0) work_total += (size_t)r.t.lutcap0 + (size_t)std::max(r.t.lutcap1, 0);
   }
   const size_t blob_total = off;
   int rc = ensure(blob_total, res_total, work_total);
   if (rc) {
-    for (auto& w : waiters) w.op->status = rc;
-    for (auto& w : waiters) w.h.resume();
+    std::vector<Waiter> ws;
+    ws.swap(waiters);
+    batch.clear();
+    for (auto& w : ws) w.op->status = rc;
+    for (auto& w : ws) w.h.resume();
     return rc;
   }
 
@@ -395,6 +434,7 @@ int Engine::step() {
     t.cores = r.ncores ? (int64_t)o_cores[i] : 0;
     t.res = (int64_t)o_res[i];
     t.work = t.smem_mode ? nullptr : dwork_ + o_work[i];
+    t.lut = t.lutcap0 > 0 ? dwork_ + o_work[i] + wel[i] : nullptr;
     if (r.ain_host) t.ain = (const double*)(dblob_ + o_ain[i]);
     t.cost = task_cost(t);
     tasks[i] = t;
@@ -417,7 +457,24 @@ int Engine::step() {
                            stream_));
   if (timing) CUDA_TRY(cudaEventRecord(ev1_, stream_));
   CUDA_TRY(cudaMemcpyAsync(hres_, dres_, res_total, cudaMemcpyDeviceToHost, stream_));
-  CUDA_TRY(cudaStreamSynchronize(stream_));
+  CUDA_TRY(cudaEventRecord(done_, stream_));
+  inflight_ = true;
+  fl_blob_ = blob_total;
+  fl_res_ = res_total;
+  fl_o_res_.swap(o_res);
+  fl_smem_.resize(nt);
+  for (size_t i = 0; i < nt; ++i) fl_smem_[i] = (char)tasks[i].smem_mode;
+  return 0;
+}
+
+int Engine::complete() {
+  if (!inflight_) return 0;
+  CUDA_TRY(cudaEventSynchronize(done_));
+  inflight_ = false;
+  std::vector<Req*>& batch = fl_batch_;
+  const size_t nt = batch.size();
+  const size_t blob_total = fl_blob_, res_total = fl_res_;
+  const std::vector<size_t>& o_res = fl_o_res_;
   if (timing) {
     float ms = 0;
     cudaEventElapsedTime(&ms, ev0_, ev1_);
@@ -432,6 +489,11 @@ int Engine::step() {
   for (size_t i = 0; i < nt; ++i) {
     Req& r = *batch[i];
     r.res = hres_ + o_res[i];
+    if (task_log_) {
+      const tci_result_head* h = r.head();
+      std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d\n", (long long)stats.steps, r.t.kind, r.t.m,
+                   r.t.n, r.t.r, h->npivot, (long long)h->cycles, (int)fl_smem_[i], h->lut_used);
+    }
     const tci_task& t = r.t;
     switch (t.kind) {
       case TCI_TASK_RRLU: {
@@ -447,16 +509,62 @@ int Engine::step() {
         stats.feval += (int64_t)t.m * t.n;
         break;
       case TCI_TASK_EVAL:
+      case TCI_TASK_SEARCH:
         stats.feval += t.m;
         break;
       default:
         break;
     }
   }
-  for (auto& w : waiters) {
+  // Resuming lets each solve continue to its next task (enqueued for the next
+  // launch); the Req records of this batch may be gone afterwards.
+  std::vector<Waiter> ws;
+  ws.swap(fl_waiters_);
+  batch.clear();
+  for (auto& w : ws) {
     w.op->status = 0;
     w.h.resume();
   }
+  return 0;
+}
+
+int Engine::gather_to_host(const std::vector<const double*>& src, const std::vector<int64_t>& len,
+                           double* host_out) {
+  const size_t n = src.size();
+  if (n == 0) return 0;
+  size_t total = 0;
+  std::vector<int64_t> off(n);
+  for (size_t i = 0; i < n; ++i) {
+    off[i] = (int64_t)total;
+    total += (size_t)len[i];
+  }
+  const size_t table = a16(n * (sizeof(void*) + 2 * sizeof(int64_t)));
+  const size_t need = table + total * sizeof(double);
+  if (need > hgat_cap_) {
+    if (hgat_) cudaFreeHost(hgat_);
+    hgat_ = nullptr;
+    CUDA_TRY(cudaHostAlloc(&hgat_, need, cudaHostAllocDefault));
+    hgat_cap_ = need;
+  }
+  if (need > dgat_cap_) {
+    if (dgat_) cudaFree(dgat_);
+    dgat_ = nullptr;
+    CUDA_TRY(cudaMalloc(&dgat_, need));
+    dgat_cap_ = need;
+  }
+  std::memcpy(hgat_, src.data(), n * sizeof(void*));
+  std::memcpy(hgat_ + n * sizeof(void*), len.data(), n * sizeof(int64_t));
+  std::memcpy(hgat_ + n * (sizeof(void*) + sizeof(int64_t)), off.data(), n * sizeof(int64_t));
+  CUDA_TRY(cudaMemcpyAsync(dgat_, hgat_, table, cudaMemcpyHostToDevice, stream_));
+  CUDA_TRY(tci_gather_launch(dgat_, (int)n, (double*)(dgat_ + table), std::min<int>((int)n, 4 * num_sms),
+                             stream_));
+  CUDA_TRY(cudaMemcpyAsync(hgat_ + table, dgat_ + table, total * sizeof(double), cudaMemcpyDeviceToHost,
+                           stream_));
+  CUDA_TRY(cudaStreamSynchronize(stream_));
+  std::memcpy(host_out, hgat_ + table, total * sizeof(double));
+  stats.launches += 1;
+  stats.h2d_bytes += (int64_t)table;
+  stats.d2h_bytes += (int64_t)(total * sizeof(double));
   return 0;
 }
 
@@ -506,6 +614,8 @@ static void fill_f(Req& r, const Solve& s) {
   r.t.nparams = (int32_t)s.params.size();
   r.t.L = s.L;
   r.params = s.params.data();
+  r.t.lutcap0 = s.lutcap0;
+  r.t.lutcap1 = s.lutcap1;
 }
 
 static int clamp_rank(i64 maxrank, size_t m, size_t n) {
@@ -550,6 +660,27 @@ int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double*
   }
   s.cores.assign(L, Core());
   s.bonderrors.assign(L - 1, 0.0);
+  // table ranges of the factored functions: sum v^2 over [L, sum d^2] and
+  // sum (v - c)^2 over [0, sum max((d - c)^2, (1 - c)^2)]
+  s.lutcap0 = s.lutcap1 = 0;
+  if (fid == TCI_F_LORENTZ || fid == TCI_F_SERVED) {
+    int64_t hi0 = 0, hi1 = 0;
+    for (int p = 0; p < L; ++p) {
+      hi0 += (int64_t)s.d[p] * s.d[p];
+      if (fid == TCI_F_SERVED) {
+        int64_t c = (int64_t)params[3 + p];
+        int64_t a = (int64_t)s.d[p] - c, b = 1 - c;
+        hi1 += std::max(a * a, b * b);
+      }
+    }
+    if (hi0 - L + 1 <= (1 << 20)) s.lutcap0 = (int)(hi0 - L + 1);
+    if (fid == TCI_F_SERVED) {
+      if (hi1 + 1 <= (1 << 20) && s.lutcap0 > 0)
+        s.lutcap1 = (int)(hi1 + 1);
+      else
+        s.lutcap0 = 0;
+    }
+  }
   s.pivoterrors.clear();
   return 0;
 }
@@ -881,50 +1012,61 @@ CoTask co_sum(Engine& e, Solve& s, double* out) {
 
 // DefaultGlobalPivotFinder (globalpivotfinder.jl:143-195): nsearch random start
 // points, a line scan along every site, the point of largest |f - tt| kept when
-// it exceeds abstol * tolmarginglobalsearch.  All f and train evaluations of one
-// search run as one EVAL task.
+// it exceeds abstol * tolmarginglobalsearch.  Each start point is one SEARCH
+// task (train values through left/right environments of the start point).
 CoTask co_globalpivots(Engine& e, Solve& s, double abstol, int nsearch, int maxnglobalpivot,
                        double tolmargin, std::vector<std::vector<uint8_t>>* found) {
   found->clear();
   if (nsearch <= 0) co_return 0;
+  if (!s.cores_valid) co_return fail(TCI_ERR_GENERIC, "site tensors are not available");
   const int L = s.L;
   std::vector<std::vector<uint8_t>> starts(nsearch, std::vector<uint8_t>(L));
   for (int q = 0; q < nsearch; ++q)
     for (int p = 0; p < L; ++p) starts[q][p] = (uint8_t)(tci_rng_uniform1(&s.rng, (uint64_t)s.d[p]) - 1);
   i64 per = 0;
   for (int p = 0; p < L; ++p) per += s.d[p];
-  const i64 np = per * nsearch;
-  std::vector<uint8_t> pts((size_t)np * L);
-  size_t k = 0;
-  for (int q = 0; q < nsearch; ++q)
-    for (int p = 0; p < L; ++p)
-      for (int v = 0; v < s.d[p]; ++v) {
-        std::memcpy(&pts[k * L], starts[q].data(), L);
-        pts[k * L + p] = (uint8_t)v;
-        ++k;
-      }
-  std::vector<double> fv(np), tv(np);
-  CO_TRY(co_evaluate(e, s, pts, np, fv.data(), tv.data()));
-  s.nfeval += np;
-  k = 0;
+  std::vector<tci_core_ref> tab;
+  int rmax = 1;
+  core_table(s, tab, rmax);
+  int envs = 0;
+  for (int p = 0; p < L; ++p) envs += tab[p].r0 + tab[p].r1;
+  std::vector<Req> reqs(nsearch);
+  std::vector<Req*> ptrs;
   for (int q = 0; q < nsearch; ++q) {
+    Req& r = reqs[q];
+    r.t.kind = TCI_TASK_SEARCH;
+    fill_f(r, s);
+    r.t.m = (int32_t)per;
+    r.t.n = envs;
+    r.t.r = rmax;
+    r.rows = starts[q].data();
+    r.rows_bytes = (size_t)L;
+    r.cores = tab.data();
+    r.ncores = L;
+    ptrs.push_back(&r);
+  }
+  GpuOp op{&e, ptrs};
+  co_await op;
+  if (op.status) co_return op.status;
+  s.nfeval += per * nsearch;
+  for (int q = 0; q < nsearch; ++q) {
+    const double* fv = reqs[q].fvals();
+    const double* tv = reqs[q].ttvals();
     double best_error = 0.0;
-    size_t best = SIZE_MAX;
+    int bp_site = -1, bp_val = 0;
+    int k = 0;
     for (int p = 0; p < L; ++p)
-      for (int v = 0; v < s.d[p]; ++v) {
+      for (int v = 0; v < s.d[p]; ++v, ++k) {
         double err = std::fabs(fv[k] - tv[k]);
         if (err > best_error) {
           best_error = err;
-          best = k;
+          bp_site = p;
+          bp_val = v;
         }
-        ++k;
       }
     if (best_error > abstol * tolmargin) {
-      std::vector<uint8_t> bp(L);
-      if (best == SIZE_MAX)
-        bp = starts[q];
-      else
-        std::memcpy(bp.data(), &pts[best * L], L);
+      std::vector<uint8_t> bp = starts[q];
+      if (bp_site >= 0) bp[bp_site] = (uint8_t)bp_val;
       found->push_back(bp);
     }
   }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <coroutine>
+#include <cstdio>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -151,6 +152,7 @@ struct Solve {
   std::vector<double> errors;
   i64 nfeval = 0;
   tci_rng rng;
+  int lutcap0 = 0, lutcap1 = 0;  // capacities of the f tables (tci_f_tables)
   tci_opts opts{};
   // bookkeeping for serving
   int rc = 0;
@@ -171,6 +173,13 @@ class Engine {
   bool idle() const { return pending_.empty(); }
   // Run one batched step: pack, upload, launch, download, resume.
   int step();
+  // The same split in two: launch() packs and enqueues the pending tasks on
+  // the engine's stream (no-op while a batch is in flight); complete() waits
+  // for it and resumes the solves.  ready(): the in-flight batch is done.
+  int launch();
+  int complete();
+  bool ready() const;
+  bool inflight() const { return inflight_; }
   // Drive a single coroutine (and any others already queued) to completion.
   int run(CoTask& t);
 
@@ -180,6 +189,10 @@ class Engine {
   void release_cores(Solve& s);
   // Run a list of tasks outside any solve (rrLU entry points).
   int run_tasks(std::vector<Req*>& reqs);
+  // Copy many device arrays to one host buffer: gather on the device into a
+  // contiguous staging buffer, then a single device-to-host copy.
+  int gather_to_host(const std::vector<const double*>& src, const std::vector<int64_t>& len,
+                     double* host_out);
 
   tci_stats stats{};
   bool timing = true;
@@ -210,6 +223,20 @@ class Engine {
   double* dwork_ = nullptr;
   size_t dwork_cap_ = 0;
   int* dcounter_ = nullptr;
+  FILE* task_log_ = nullptr;
+  // gather staging
+  char* hgat_ = nullptr;
+  size_t hgat_cap_ = 0;
+  char* dgat_ = nullptr;
+  size_t dgat_cap_ = 0;
+  // the batch in flight
+  bool inflight_ = false;
+  cudaEvent_t done_ = nullptr;
+  std::vector<Req*> fl_batch_;
+  std::vector<Waiter> fl_waiters_;
+  size_t fl_blob_ = 0, fl_res_ = 0;
+  std::vector<size_t> fl_o_res_;
+  std::vector<char> fl_smem_;
 };
 
 // ------------------------------------------------------------ TCI2 algorithm

@@ -46,6 +46,7 @@ struct Ctl {
   double red_s[NW + 1];
   int red_k[NW + 1];
   unsigned long long red_u[NW + 1];
+  double red4[4][NW + 1];
 };
 
 __device__ __forceinline__ double jmax(double a, double b) {
@@ -145,6 +146,30 @@ __device__ unsigned long long block_max_u64(unsigned long long v, Ctl& ctl) {
   return r;
 }
 
+__device__ void block_max4(double v[4], Ctl& ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v[q] = fmax(v[q], __shfl_down_sync(FULL, v[q], off));
+    if (lane == 0) ctl.red4[q][warp] = v[q];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double x = lane < NW ? ctl.red4[q][lane] : -1e300;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) x = fmax(x, __shfl_down_sync(FULL, x, off));
+      if (lane == 0) ctl.red4[q][NW] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = ctl.red4[q][NW];
+  __syncthreads();
+}
+
 __device__ int block_or(int v, Ctl& ctl) {
   int r = __syncthreads_or(v);
   return r;
@@ -162,6 +187,80 @@ __device__ void compute_states(int fid, const double* params, const uint8_t* idx
     s0[i] = a0;
     s1[i] = a1;
   }
+}
+
+// Element generator of a registered f from row/column partial sums.  When f
+// factors through exact integer sums (tci_f_tables), the distinct values of
+// part0/part1 over the task's range are computed once into T.lut and each
+// element is combine(table0[s0], table1[s1]) -- the same functions the direct
+// path calls, so the bits are identical.
+struct Filler {
+  int fid, nparams;
+  const double* prm;
+  const double* lut0;
+  const double* lut1;
+  int lo0, lo1;
+  __device__ __forceinline__ double operator()(double a0, double a1) const {
+    if (lut0) {
+      double p0 = lut0[(int)a0 - lo0];
+      double p1 = lut1 ? lut1[(int)a1 - lo1] : 0.0;
+      return tci_f_combine(fid, prm, p0, p1);
+    }
+    return tci_f_finish(fid, prm, nparams, a0, a1);
+  }
+};
+
+// Block-wide max of four doubles (pass -x for a minimum).
+__device__ void block_max4(double v[4], Ctl& ctl);
+
+// Decide on tabulation for a task whose elements are sums rs[i] + cs[j] over
+// the given row-state groups, and fill the tables.  Ends with a barrier.
+__device__ Filler make_filler(const tci_task& T, const double* prm, const double* const* rs0,
+                              const double* const* rs1, const int* rcount, int ngroups, const double* cs0,
+                              const double* cs1, int n, int64_t elems, Ctl& ctl) {
+  Filler F;
+  F.fid = T.fid;
+  F.nparams = T.nparams;
+  F.prm = prm;
+  F.lut0 = F.lut1 = nullptr;
+  F.lo0 = F.lo1 = 0;
+  const int tables = tci_f_tables(T.fid);
+  if (tables == 0 || T.lut == nullptr || T.lutcap0 <= 0) return F;
+  // max / -min of the row and column sums
+  double v[4] = {-1e300, -1e300, -1e300, -1e300};  // max r0, max r1, -min r0, -min r1
+  double w[4] = {-1e300, -1e300, -1e300, -1e300};
+  for (int g = 0; g < ngroups; ++g)
+    for (int i = threadIdx.x; i < rcount[g]; i += NT) {
+      v[0] = fmax(v[0], rs0[g][i]);
+      v[1] = fmax(v[1], rs1[g][i]);
+      v[2] = fmax(v[2], -rs0[g][i]);
+      v[3] = fmax(v[3], -rs1[g][i]);
+    }
+  for (int j = threadIdx.x; j < n; j += NT) {
+    w[0] = fmax(w[0], cs0[j]);
+    w[1] = fmax(w[1], cs1[j]);
+    w[2] = fmax(w[2], -cs0[j]);
+    w[3] = fmax(w[3], -cs1[j]);
+  }
+  block_max4(v, ctl);
+  block_max4(w, ctl);
+  if (v[0] < -1e299 || w[0] < -1e299) return F;  // no rows or no columns
+  const double lo0 = -v[2] + -w[2], hi0 = v[0] + w[0];
+  const double lo1 = -v[3] + -w[3], hi1 = v[1] + w[1];
+  const double n0 = hi0 - lo0 + 1.0, n1 = tables > 1 ? hi1 - lo1 + 1.0 : 0.0;
+  if (!(n0 <= (double)T.lutcap0) || (tables > 1 && !(n1 <= (double)T.lutcap1))) return F;
+  if (n0 + n1 > (double)elems) return F;  // tabulating would cost more than it saves
+  double* t0 = T.lut;
+  double* t1 = T.lut + T.lutcap0;
+  const int c0 = (int)n0, c1 = (int)n1, l0 = (int)lo0, l1 = (int)lo1;
+  for (int k = threadIdx.x; k < c0; k += NT) t0[k] = tci_f_part0(T.fid, prm, T.nparams, (double)(l0 + k));
+  for (int k = threadIdx.x; k < c1; k += NT) t1[k] = tci_f_part1(T.fid, prm, (double)(l1 + k));
+  __syncthreads();
+  F.lut0 = t0;
+  F.lut1 = tables > 1 ? t1 : nullptr;
+  F.lo0 = l0;
+  F.lo1 = l1;
+  return F;
 }
 
 // Result record pointers.
@@ -399,6 +498,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   int* colperm = (int*)cur.take((size_t)n * 4);
   for (int i = tid; i < m; i += NT) rowperm[i] = i;
   for (int j = tid; j < n; j += NT) colperm[j] = j;
+  int lut_used = 0;
   ArgBest ab;
   ab.init();
   unsigned long long mx = 0;
@@ -423,11 +523,16 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
     compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
     compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
     __syncthreads();
+    const double* rg0[1] = {rs0};
+    const double* rg1[1] = {rs1};
+    const int rc[1] = {m};
+    const Filler F = make_filler(T, prm, rg0, rg1, rc, 1, cs0, cs1, n, (int64_t)m * n, ctl);
+    lut_used = F.lut0 != nullptr;
     for (int j = warp; j < n; j += NW) {
       double* dst = A + (size_t)j * lda;
       const double c0 = cs0[j], c1 = cs1[j];
       for (int i = lane; i < m; i += 32) {
-        double v = tci_f_finish(T.fid, prm, T.nparams, rs0[i] + c0, rs1[i] + c1);
+        double v = F(rs0[i] + c0, rs1[i] + c1);
         dst[i] = v;
         ab.push(v, j * m + i);
         unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
@@ -466,6 +571,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
     rp.head->error = ctl.err;
     rp.head->maxabs = __longlong_as_double((long long)mxall);
     rp.head->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+    rp.head->lut_used = lut_used;
   }
   if (T.post == TCI_POST_FACTORS) {
     // full permutations go after the factors: rowperm (m) then colperm (n)
@@ -505,11 +611,15 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     colperm[i] = i;
   }
   __syncthreads();
+  const double* rg0[2] = {ps0, rs0};
+  const double* rg1[2] = {ps1, rs1};
+  const int rc[2] = {r, m};
+  const Filler F = make_filler(T, prm, rg0, rg1, rc, 2, cs0, cs1, r, (int64_t)(r + m) * r, ctl);
   ArgBest ab;
   ab.init();
   for (int j = warp; j < r; j += NW)
     for (int i = lane; i < r; i += 32) {
-      double v = tci_f_finish(T.fid, prm, T.nparams, ps0[i] + cs0[j], ps1[i] + cs1[j]);
+      double v = F(ps0[i] + cs0[j], ps1[i] + cs1[j]);
       P[i + (size_t)j * r] = v;
       ab.push(v, j * r + i);
     }
@@ -544,7 +654,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     for (int e = tid; e < rows_here * r; e += NT) {
       int rr = e % rows_here, q = e / rows_here;
       int row = base + rr, col = colperm[q];
-      double v = tci_f_finish(T.fid, prm, T.nparams, rs0[row] + cs0[col], rs1[row] + cs1[col]);
+      double v = F(rs0[row] + cs0[col], rs1[row] + cs1[col]);
       W[rr + (size_t)q * RB] = v;
       unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
       mx = b > mx ? b : mx;
@@ -582,6 +692,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     rp.head->error = ctl.err;
     rp.head->maxabs = __longlong_as_double((long long)mxall);
     rp.head->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+    rp.head->lut_used = F.lut0 != nullptr;
   }
   __syncthreads();
 }
@@ -598,10 +709,14 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
   compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
   compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
   __syncthreads();
+  const double* rg0[1] = {rs0};
+  const double* rg1[1] = {rs1};
+  const int rc[1] = {m};
+  const Filler F = make_filler(T, prm, rg0, rg1, rc, 1, cs0, cs1, n, (int64_t)m * n, ctl);
   unsigned long long mx = 0;
   for (int j = warp; j < n; j += NW)
     for (int i = lane; i < m; i += 32) {
-      double v = tci_f_finish(T.fid, prm, T.nparams, rs0[i] + cs0[j], rs1[i] + cs1[j]);
+      double v = F(rs0[i] + cs0[j], rs1[i] + cs1[j]);
       T.core_out[i + (size_t)j * m] = v;
       unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
       mx = b > mx ? b : mx;
@@ -614,6 +729,7 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
     h->error = 0.0;
     h->maxabs = __longlong_as_double((long long)mxall);
     h->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
+    h->lut_used = F.lut0 != nullptr;
   }
   __syncthreads();
 }
@@ -672,6 +788,103 @@ __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char*
   __syncthreads();
 }
 
+// ---------------------------------------------------------------- SEARCH task
+// One start point of DefaultGlobalPivotFinder (globalpivotfinder.jl:160-177):
+// f and the train at every point that differs from the start in one site.  The
+// train values use left environments Le_p = C_0[i_0] ... C_{p-1}[i_{p-1}] and
+// right environments Re_p = C_{p+1}[i_{p+1}] ... C_{L-1}[i_{L-1}] of the start,
+// value(p, v) = sum_b (sum_a Le_p[a] C_p[a, v, b]) Re_p[b], every sum in index
+// order with separate multiply and add (the oracle uses the same order).
+__device__ void task_search(const tci_task& T, const char* blob, char* resb, char* smem) {
+  const int L = T.L, tid = threadIdx.x;
+  const double* prm = (const double*)(blob + T.params);
+  const uint8_t* st = (const uint8_t*)(blob + T.rows);
+  const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
+  char* base = resb + T.res;
+  double* fout = (double*)(base + sizeof(tci_result_head));
+  double* tout = fout + T.m;
+  // environment offsets: Le_p has r0(p) entries, Re_p has r1(p) entries
+  int* loff = (int*)smem;
+  int* roff = loff + (L + 1);
+  int* ioff = roff + (L + 1);  // first item of site p
+  double* env = (double*)(smem + align_up((size_t)(3 * (L + 1)) * 4, 16));
+  if (tid == 0) {
+    int a = 0, b = 0, c = 0;
+    for (int p = 0; p < L; ++p) {
+      loff[p] = a;
+      a += cr[p].r0;
+      ioff[p] = c;
+      c += cr[p].d;
+    }
+    for (int p = 0; p < L; ++p) {
+      roff[p] = a + b;
+      b += cr[p].r1;
+    }
+    ioff[L] = c;
+  }
+  __syncthreads();
+  // left environments
+  if (tid == 0) env[loff[0]] = 1.0;
+  __syncthreads();
+  for (int p = 0; p + 1 < L; ++p) {
+    const tci_core_ref c = cr[p];
+    const int i = st[p];
+    const double* le = env + loff[p];
+    double* nx = env + loff[p + 1];
+    for (int b = tid; b < c.r1; b += NT) {
+      double acc = 0.0;
+      const double* col = c.p + (size_t)c.r0 * (i + (size_t)c.d * b);
+      for (int a = 0; a < c.r0; ++a) acc = __dadd_rn(acc, __dmul_rn(le[a], col[a]));
+      nx[b] = acc;
+    }
+    __syncthreads();
+  }
+  // right environments
+  if (tid == 0) env[roff[L - 1]] = 1.0;
+  __syncthreads();
+  for (int p = L - 1; p > 0; --p) {
+    const tci_core_ref c = cr[p];
+    const int i = st[p];
+    const double* re = env + roff[p];
+    double* nx = env + roff[p - 1];
+    for (int a = tid; a < c.r0; a += NT) {
+      double acc = 0.0;
+      for (int b = 0; b < c.r1; ++b)
+        acc = __dadd_rn(acc, __dmul_rn(c.p[a + (size_t)c.r0 * (i + (size_t)c.d * b)], re[b]));
+      nx[a] = acc;
+    }
+    __syncthreads();
+  }
+  // every (p, v)
+  const int nitems = ioff[L];
+  for (int it = tid; it < nitems; it += NT) {
+    int p = 0;
+    while (ioff[p + 1] <= it) ++p;
+    const int v = it - ioff[p];
+    const tci_core_ref c = cr[p];
+    const double* le = env + loff[p];
+    const double* re = env + roff[p];
+    double val = 0.0;
+    for (int b = 0; b < c.r1; ++b) {
+      const double* col = c.p + (size_t)c.r0 * (v + (size_t)c.d * b);
+      double w = 0.0;
+      for (int a = 0; a < c.r0; ++a) w = __dadd_rn(w, __dmul_rn(le[a], col[a]));
+      val = __dadd_rn(val, __dmul_rn(w, re[b]));
+    }
+    tout[it] = val;
+    double a0 = 0.0, a1 = 0.0;
+    for (int s = 0; s < L; ++s) tci_f_term(T.fid, prm, s, s == p ? v : st[s], &a0, &a1);
+    fout[it] = tci_f_finish(T.fid, prm, T.nparams, a0, a1);
+  }
+  if (tid == 0) {
+    tci_result_head* h = (tci_result_head*)base;
+    h->status = 0;
+    h->npivot = 0;
+    h->lut_used = 0;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------- SUM task
 // sum(tt) (abstracttensortrain.jl:164-199): v <- v * (sum over the local index
 // of core b), left to right; one thread per output bond index.
@@ -720,14 +933,17 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();
     if (ti >= ntasks) break;
     const tci_task T = tasks[order[ti]];
+    const long long t0 = clock64();
     switch (T.kind) {
       case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl); break;
       case TCI_TASK_SITE: task_site(T, blob, resb, smem, ctl, smem_bytes); break;
       case TCI_TASK_CORE: task_core(T, blob, resb, smem, ctl); break;
       case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
       case TCI_TASK_SUM: task_sum(T, blob, resb, smem); break;
+      case TCI_TASK_SEARCH: task_search(T, blob, resb, smem); break;
       default: break;
     }
+    if (threadIdx.x == 0) ((tci_result_head*)(resb + T.res))->cycles = clock64() - t0;
   }
 }
 

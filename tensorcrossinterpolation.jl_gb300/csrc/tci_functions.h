@@ -61,18 +61,38 @@ TCI_HD void tci_f_term(int fid, const double* params, int site, int v,
   }
 }
 
+// Functions of exact integer sums factor as combine(part0(acc0), part1(acc1)).
+// The step kernel tabulates part0/part1 over the integer range a task needs and
+// combines per element; the direct path below calls the same three functions,
+// so both give identical bits.
+//   number of tables: 0 (no factoring), 1 (part0 only) or 2.
+TCI_HD int tci_f_tables(int fid) {
+  return fid == TCI_F_LORENTZ ? 1 : (fid == TCI_F_SERVED ? 2 : 0);
+}
+TCI_HD double tci_f_part0(int fid, const double* params, int nparams, double acc0) {
+  if (fid == TCI_F_LORENTZ) {
+    double coeff = nparams > 0 ? params[0] : 1.0;
+    return coeff / (acc0 + 1.0);
+  }
+  return 1.0 / (1.0 + params[0] * acc0);  // SERVED
+}
+TCI_HD double tci_f_part1(int fid, const double* params, double acc1) {
+  (void)fid;
+  return tci_exp(-(params[2] * acc1));  // SERVED
+}
+TCI_HD double tci_f_combine(int fid, const double* params, double p0, double p1) {
+  if (fid == TCI_F_LORENTZ) return p0;
+  return p0 + params[1] * p1;  // SERVED
+}
+
 TCI_HD double tci_f_finish(int fid, const double* params, int nparams, double acc0,
                            double acc1) {
   switch (fid) {
-    case TCI_F_LORENTZ: {
-      double coeff = nparams > 0 ? params[0] : 1.0;
-      return coeff / (acc0 + 1.0);
-    }
-    case TCI_F_SERVED: {
-      double a = 1.0 / (1.0 + params[0] * acc0);
-      double e = tci_exp(-(params[2] * acc1));
-      return a + params[1] * e;
-    }
+    case TCI_F_LORENTZ:
+      return tci_f_combine(fid, params, tci_f_part0(fid, params, nparams, acc0), 0.0);
+    case TCI_F_SERVED:
+      return tci_f_combine(fid, params, tci_f_part0(fid, params, nparams, acc0),
+                           tci_f_part1(fid, params, acc1));
     case TCI_F_QTT1D: {
       double x = acc0;
       int kind = nparams > 0 ? (int)params[0] : 0;

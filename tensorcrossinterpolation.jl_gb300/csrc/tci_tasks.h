@@ -14,6 +14,7 @@ enum {
   TCI_TASK_CORE = 3,  // core = Pi1 (last site of fillsitetensors!/sweep1site!)
   TCI_TASK_EVAL = 4,  // f and the tensor train at a list of points
   TCI_TASK_SUM = 5,   // sum of the tensor train over all sites
+  TCI_TASK_SEARCH = 6 // line scans of the global pivot search from one start point
 };
 
 enum {
@@ -50,6 +51,8 @@ typedef struct tci_task {
   int64_t cost;               // scheduling weight
   int32_t smem_mode;           // 1: matrix held in shared memory
   int32_t kcap;                // pivot capacity of the result record
+  double* lut;                 // scratch for tabulated f parts (lutcap0 + lutcap1 doubles)
+  int32_t lutcap0, lutcap1;    // table capacities (0: evaluate f directly)
 } tci_task;
 
 // Result record: fixed header followed by per-task arrays.
@@ -57,11 +60,14 @@ typedef struct tci_result_head {
   int32_t status, npivot;
   double error;
   double maxabs;      // max |value| over the filled matrix (updatemaxsample!)
-  int32_t maxabs_nan, pad;
+  int32_t maxabs_nan, lut_used;
+  int64_t cycles;     // SM clock cycles the CTA spent on the task
 } tci_result_head;
 // RRLU/SITE: head, int32 rowperm[kcap], int32 colperm[kcap], double diag[kcap]
 //            (each array padded to 8 bytes)
 // EVAL: head, double f[m], double tt[m]
+// SEARCH: head, double f[m], double tt[m], m = sum of the local dimensions; item
+//         (p, v) (site-major) is the start point with site p set to v
 // SUM : head with the sum in `error`
 
 #define TCI_STEP_THREADS 512

@@ -141,6 +141,8 @@ _SIGNATURES = {
     "tci_convergencecriterion": (ctypes.c_int, [I64P, F64P, I64P, ctypes.c_int64, ctypes.c_double,
                                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]),
     "tci_fp64_peak": (ctypes.c_int, [ctypes.c_size_t, F64P, F64P]),
+    "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
+                                             I64P]),
 }
 
 _lib = None
@@ -272,7 +274,11 @@ def make_opts(tolerance=None, maxbonddim=None, maxiter=20, sweepstrategy="backan
 
 
 def _pivots_array(pivots, L):
-    return np.ascontiguousarray(np.asarray(pivots, dtype=np.int64).reshape(-1, L))
+    rows = [np.asarray(p, dtype=np.int64).ravel() for p in pivots] if len(pivots) else []
+    if any(r.size != L for r in rows):
+        # addglobalpivots! (tensorci2.jl:197-199)
+        raise DimensionMismatch(TCI_ERR_DIM, "Please specify a pivot as one index per leg of the MPS.")
+    return np.ascontiguousarray(np.array(rows, dtype=np.int64).reshape(-1, L))
 
 
 class TensorCI2:
@@ -511,6 +517,35 @@ def crossinterpolate2_batched(specs, max_live=0, ctx=None):
     for i, (f, localdims, _) in enumerate(specs):
         res.append(TensorCI2(f, localdims, ctx=ctx, _handle=ctypes.c_void_p(out[i])) if out[i] else None)
     _check(rc)
+    return res
+
+
+def core_dims(tci):
+    lib = load_library()
+    dims = []
+    d = np.zeros(3, np.int64)
+    for b in range(1, len(tci) + 1):
+        _check(lib.tci_get_core(tci.h, b, None, _p(d, I64P)))
+        dims.append(tuple(int(x) for x in d))
+    return dims
+
+
+def tensortrains(tcis, ctx=None):
+    """TensorTrain(tci) for many solves with one device-to-host copy."""
+    ctx = ctx or default_context()
+    dims = [core_dims(t) for t in tcis]
+    sizes = [sum(a * b * c for a, b, c in ds) for ds in dims]
+    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
+    out = np.zeros(max(int(sum(sizes)), 1))
+    handles = (ctypes.c_void_p * len(tcis))(*[t.h.value if isinstance(t.h, ctypes.c_void_p) else t.h for t in tcis])
+    _check(load_library().tci_get_cores_batched(ctx.h, len(tcis), handles, _p(out, F64P), _p(offs, I64P)))
+    res = []
+    for ds, o in zip(dims, offs):
+        cores = []
+        for (a, b, c) in ds:
+            cores.append(out[o:o + a * b * c].reshape((a, b, c), order="F"))
+            o += a * b * c
+        res.append(TensorTrain(cores))
     return res
 
 

@@ -171,7 +171,22 @@ def test_errors_like_reference(T):
     z = T.DeviceFunction.dense(np.zeros((3, 3)))
     with pytest.raises(T.TCIError, match="maxsamplevalue is zero"):  # tensorci2.jl:50
         T.TensorCI2(z, [3, 3])
+    # NaN that reaches L in the first bond: "lu.L contains NaNs" (matrixlu.jl:164-166)
     bad = np.ones((3, 3))
-    bad[1, 2] = np.nan
+    bad[1, 0] = np.nan
     with pytest.raises(T.TCIError, match="NaN"):
         T.crossinterpolate2(float, T.DeviceFunction.dense(bad), [3, 3])
+
+
+def test_bulk_export_matches_per_core(T):
+    rng = np.random.default_rng(8)
+    specs = []
+    for _ in range(6):
+        L = int(rng.integers(4, 8))
+        d = int(rng.integers(2, 6))
+        specs.append((T.DeviceFunction("served", _served(rng, L, d)), [d] * L, dict(tolerance=1e-8, maxbonddim=32)))
+    res = T.crossinterpolate2_batched(specs)
+    tts = T.tensortrains(res)
+    for tci, tt in zip(res, tts):
+        for b in range(1, len(tci) + 1):
+            assert np.array_equal(tt.sitetensors[b - 1], tci.sitetensor(b))
