@@ -214,6 +214,28 @@ int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t*
                      double abstol, int32_t leftorthogonal, int64_t* piv, const int64_t* piv_offsets,
                      int64_t* npivots, double* errors);
 
+/* rrlu on caller-owned device buffers, with no allocation by the library.
+ * No counterpart in the reference: it serves callers that cannot let a
+ * library allocate device memory -- code running while a stream is captured
+ * into a CUDA graph, latency-critical loops where cudaMalloc/cudaFree would
+ * stall the device, hosts whose every device buffer comes from their own
+ * allocator.  Same arithmetic and outputs as tci_rrlu, but all pointers are
+ * device pointers: A_dev (m x n column-major, read only); rowperm_dev (m) and
+ * colperm_dev (n) receive the full 0-based permutations, npivot_dev and
+ * error_dev one value each, factors_dev (m x n, optional, may be NULL) the
+ * factored matrix (L below the diagonal, U on and above, unit diagonal
+ * implied on the side leftorthogonal selects).  Work goes to `stream`.
+ * Limits: 1 <= m, n <= 16384 and m*n <= 524288 (larger sizes return
+ * TCI_ERR_ARG).  The working storage is one fixed device array of the library
+ * (about 8.6 MB on every GPU that loads it, kept until the process exits),
+ * shared by all calls: calls that overlap on the GPU race on it, calls on one
+ * stream are ordered.  The first call on a device looks up that array's
+ * device address and sets the kernel's shared-memory limit with the device
+ * current; make it before any stream capture.  Returns after enqueueing. */
+int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank, double reltol,
+                     double abstol, int32_t leftorthogonal, int32_t* rowperm_dev, int32_t* colperm_dev,
+                     int32_t* npivot_dev, double* error_dev, double* factors_dev, uintptr_t stream);
+
 /* ---- context utilities --------------------------------------------------- */
 /* cudaStream_t of the context, as an integer. */
 uintptr_t tci_ctx_stream(tci_ctx* ctx);

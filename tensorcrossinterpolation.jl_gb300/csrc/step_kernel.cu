@@ -966,3 +966,151 @@ cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* orde
                                                               counter_dev, tci_step_smem_bytes());
   return cudaGetLastError();
 }
+
+// ===================================================================== rrLU
+// without allocation (tci_rrlu_noalloc; no counterpart in the reference).
+//
+// Some callers cannot let the library allocate device memory: code that runs
+// while a stream is being captured into a CUDA graph, latency-critical serving
+// loops where a cudaMalloc/cudaFree would stall the device, and hosts that
+// own every device buffer through their own allocator (a Julia GPU array pool,
+// a framework arena).  This entry point runs the same rank-revealing LU as the
+// step kernel's RRLU task on caller-owned device buffers and keeps its working
+// copy of the matrix, the factors and the result record in the fixed array
+// below.  The array lives in every GPU that loads the library until the
+// process exits.  Calls share it, so two calls that overlap on the GPU (on
+// different streams, or interleaved with no ordering) race on it; calls issued
+// on one stream are ordered and safe.  Nothing in it needs clearing between
+// calls: every element a call reads is written earlier in the same call.
+#include <mutex>
+#include <string>
+
+// error codes of include/tci_gb300.h (that header's function ids clash with
+// tci_functions.h, so it is not included here)
+#define TCI_ERR_ARG 1
+#define TCI_ERR_CUDA 6
+
+namespace tci {
+void set_error(int code, const std::string& msg);
+}
+
+namespace {
+
+constexpr int64_t NOALLOC_MAX_ELEMS = (int64_t)1 << 19;  // m * n
+constexpr int64_t NOALLOC_MAX_DIM = 16384;               // m and n
+// working matrix | factors + full permutations | result record
+constexpr int64_t NOALLOC_FACT_DOUBLES = NOALLOC_MAX_ELEMS + NOALLOC_MAX_DIM;
+constexpr int64_t NOALLOC_RES_DOUBLES = 16 + 2 * NOALLOC_MAX_DIM;
+constexpr int64_t NOALLOC_SCRATCH_DOUBLES = NOALLOC_MAX_ELEMS + NOALLOC_FACT_DOUBLES + NOALLOC_RES_DOUBLES;
+
+static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
+
+__global__ void __launch_bounds__(NT, 1) rrlu_noalloc_kernel(const tci_task T, char* resb) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ Ctl ctl;
+  task_rrlu(T, nullptr, resb, smem, ctl);
+}
+
+// Copies the result record and the factors from the scratch array to the
+// caller's buffers.
+__global__ void rrlu_noalloc_epilogue(const double* fact, const char* resb, int m, int n, int32_t* rowperm,
+                                      int32_t* colperm, int32_t* npivot, double* error, double* factors_out) {
+  const tci_result_head* h = (const tci_result_head*)resb;
+  const int32_t* perms = (const int32_t*)(fact + (size_t)m * n);
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  for (int i = tid; i < m; i += nth) rowperm[i] = perms[i];
+  for (int j = tid; j < n; j += nth) colperm[j] = perms[m + j];
+  if (factors_out)
+    for (int64_t e = tid; e < (int64_t)m * n; e += nth) factors_out[e] = fact[e];
+  if (tid == 0) {
+    *npivot = h->npivot;
+    *error = h->error;
+  }
+}
+
+struct NoallocDevice {
+  bool ready = false;
+  double* scratch = nullptr;  // device address of g_noalloc_scratch
+};
+
+}  // namespace
+
+// See include/tci_gb300.h.  The first call on a device resolves the device
+// address of the scratch array (cudaGetSymbolAddress) and raises the kernel's
+// shared-memory limit, with that device current; make that first call before
+// any stream capture.  Later calls only launch two kernels on `stream_u`.
+extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank, double reltol,
+                                double abstol, int32_t leftorthogonal, int32_t* rowperm_dev, int32_t* colperm_dev,
+                                int32_t* npivot_dev, double* error_dev, double* factors_dev, uintptr_t stream_u) {
+  static std::mutex mu;
+  static NoallocDevice devs[64];
+  if (m < 1 || n < 1 || m > NOALLOC_MAX_DIM || n > NOALLOC_MAX_DIM || m * n > NOALLOC_MAX_ELEMS) {
+    tci::set_error(TCI_ERR_ARG, "tci_rrlu_noalloc: matrix must satisfy 1 <= m, n <= " +
+                                            std::to_string(NOALLOC_MAX_DIM) + " and m*n <= " +
+                                            std::to_string(NOALLOC_MAX_ELEMS) + " (got " + std::to_string(m) +
+                                            " x " + std::to_string(n) + ")");
+    return TCI_ERR_ARG;
+  }
+  if (!A_dev || !rowperm_dev || !colperm_dev || !npivot_dev || !error_dev) {
+    tci::set_error(TCI_ERR_ARG, "tci_rrlu_noalloc: null input or output pointer");
+    return TCI_ERR_ARG;
+  }
+  int dev = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce != cudaSuccess || dev < 0 || dev >= 64) {
+    tci::set_error(TCI_ERR_CUDA,std::string("tci_rrlu_noalloc: ") + cudaGetErrorString(ce));
+    return TCI_ERR_CUDA;
+  }
+  NoallocDevice& D = devs[dev];
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!D.ready) {
+      void* p = nullptr;
+      ce = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (ce == cudaSuccess)
+        ce = cudaFuncSetAttribute(rrlu_noalloc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)tci_step_smem_bytes());
+      if (ce != cudaSuccess) {
+        tci::set_error(TCI_ERR_CUDA,std::string("tci_rrlu_noalloc set-up: ") + cudaGetErrorString(ce));
+        return TCI_ERR_CUDA;
+      }
+      D.scratch = (double*)p;
+      D.ready = true;
+    }
+  }
+  double* work = D.scratch;
+  double* fact = D.scratch + NOALLOC_MAX_ELEMS;
+  char* resb = (char*)(D.scratch + NOALLOC_MAX_ELEMS + NOALLOC_FACT_DOUBLES);
+  tci_task T;
+  memset(&T, 0, sizeof(T));
+  T.kind = TCI_TASK_RRLU;
+  T.m = (int32_t)m;
+  T.n = (int32_t)n;
+  int64_t kmax = maxrank <= 0 ? (m < n ? m : n) : maxrank;
+  if (kmax > m) kmax = m;
+  if (kmax > n) kmax = n;
+  T.maxrank = (int32_t)kmax;
+  T.kcap = (int32_t)kmax;
+  T.reltol = reltol;
+  T.abstol = abstol;
+  T.leftorth = leftorthogonal ? 1 : 0;
+  T.post = TCI_POST_FACTORS;
+  T.ain = A_dev;
+  T.core_out = fact;
+  T.res = 0;
+  const size_t smem = tci_step_smem_bytes();
+  auto a16 = [](size_t x) { return (x + 15) / 16 * 16; };
+  const size_t perms = a16((size_t)m * 4) + a16((size_t)n * 4);
+  T.smem_mode = a16((size_t)m * n * 8) + perms <= smem ? 1 : 0;
+  T.work = T.smem_mode ? nullptr : work;
+  cudaStream_t stream = (cudaStream_t)stream_u;
+  rrlu_noalloc_kernel<<<1, NT, smem, stream>>>(T, resb);
+  rrlu_noalloc_epilogue<<<64, 256, 0, stream>>>(fact, resb, (int)m, (int)n, rowperm_dev, colperm_dev, npivot_dev,
+                                                error_dev, factors_dev);
+  ce = cudaGetLastError();
+  if (ce != cudaSuccess) {
+    tci::set_error(TCI_ERR_CUDA,std::string("tci_rrlu_noalloc: ") + cudaGetErrorString(ce));
+    return TCI_ERR_CUDA;
+  }
+  return 0;
+}
