@@ -111,7 +111,7 @@ int tci_f_lookup(const char* name, int* fid) {
 
 int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
   *out = nullptr;
-  int neng = 4;
+  int neng = 8;  // engines (streams + host threads) of the batched/served paths
   if (const char* s = std::getenv("TCI_ENGINES")) neng = std::max(1, std::min(16, std::atoi(s)));
   std::vector<std::unique_ptr<Engine>> pool;
   for (int i = 0; i < neng; ++i) {
@@ -416,12 +416,23 @@ struct Job {
   int rc = 0;
 };
 
-// Drive jobs with continuous batching over the context's engine pool.
-// arrival == nullptr: every request is available at t = 0.  Each admitted solve
-// is bound to the engine with the fewest live solves.  The loop completes
-// whichever engine's batch is ready (resuming its solves, which queue their
-// next tasks), relaunches it at once, and admits new requests between steps
-// while the live count and the HBM estimate allow.
+// Drive jobs with continuous batching, one host thread per engine of the
+// context's pool.  arrival == nullptr: every request is available at t = 0.
+// Each thread admits requests from the shared queue (by arrival time, the live
+// cap and the HBM estimate) onto its own engine, completes its engine's batch
+// when ready (resuming those solves, which queue their next tasks) and
+// relaunches it.  Solves never move between engines, so the only shared state
+// is the admission queue and the counters below.
+struct DriveShared {
+  std::mutex mu;
+  int64_t next = 0, live = 0, finished = 0;
+  double live_bytes = 0;
+  int first_rc = 0;
+  std::string first_msg;
+  int fatal = 0;
+  std::string fatal_msg;
+};
+
 int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
           std::vector<Job>& jobs, bool keep) {
   auto& pool = ctx->pool;
@@ -430,101 +441,144 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
   jobs.resize((size_t)n);
   if (max_live <= 0) max_live = n;
   const double t0 = now_s();
-  int64_t next = 0, live = 0, finished = 0;
-  double live_bytes = 0;
   const double budget = (double)pool[0]->hbm_budget;
   std::vector<double> est(n);
   for (int64_t i = 0; i < n; ++i) est[i] = solve_estimate_bytes(reqs[i]);
-  std::vector<std::vector<int64_t>> live_on(G);  // live job ids per engine
-  std::vector<int> job_engine(n, 0);
-  int first_rc = 0;
-  auto finish = [&](Job& j, int64_t i) {
-    j.done = true;
-    j.t_done = now_s() - t0;
-    j.rc = j.task->h.promise().rc;
-    if (j.rc && !first_rc) first_rc = j.rc;
-    j.task.reset();
-    --live;
-    ++finished;
-    live_bytes -= est[i];
-    if (!keep) pool[job_engine[i]]->release_cores(j.solve->s);
-  };
-  auto reap = [&](int g) {
-    auto& lst = live_on[g];
-    size_t w = 0;
-    for (size_t k = 0; k < lst.size(); ++k) {
-      Job& j = jobs[lst[k]];
-      if (j.task && j.task->h.done())
-        finish(j, lst[k]);
-      else
-        lst[w++] = lst[k];
-    }
-    lst.resize(w);
-  };
-  while (finished < n) {
-    double t = now_s() - t0;
-    while (next < n && live < max_live && (!arrival || arrival[next] <= t) &&
-           (live == 0 || live_bytes + est[next] <= budget)) {
-      Job& j = jobs[next];
-      j.arrival = arrival ? arrival[next] : 0.0;
-      j.t_start = t;
-      const tci_request& r = reqs[next];
-      int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
-      if (rc) {
-        j.started = j.done = true;
-        j.rc = rc;
-        if (!first_rc) first_rc = rc;
-        ++finished;
-        ++next;
-        continue;
+  DriveShared sh;
+
+  auto worker = [&](int g) {
+    Engine& e = *pool[g];
+    std::vector<int64_t> mine;  // live job ids on this engine
+    auto finish = [&](int64_t i) {
+      Job& j = jobs[i];
+      j.done = true;
+      j.t_done = now_s() - t0;
+      j.rc = j.task->h.promise().rc;
+      std::string msg = j.rc ? std::string(last_message()) : std::string();
+      j.task.reset();
+      if (!keep) e.release_cores(j.solve->s);
+      std::lock_guard<std::mutex> lk(sh.mu);
+      if (j.rc && !sh.first_rc) {
+        sh.first_rc = j.rc;
+        sh.first_msg = msg;
       }
-      int g = 0;
-      for (int k = 1; k < G; ++k)
-        if (live_on[k].size() < live_on[g].size()) g = k;
-      job_engine[next] = g;
-      std::vector<std::vector<uint8_t>> piv(1, std::vector<uint8_t>(r.L, 0));
-      j.task.emplace(co_crossinterpolate2(*pool[g], j.solve->s, piv, r.opts));
-      j.started = true;
-      ++live;
-      live_bytes += est[next];
-      live_on[g].push_back(next);
-      j.task->h.resume();
-      ++next;
-    }
-    bool progressed = false;
-    for (int g = 0; g < G; ++g) {
-      Engine& e = *pool[g];
+      --sh.live;
+      ++sh.finished;
+      sh.live_bytes -= est[i];
+    };
+    auto reap = [&]() {
+      size_t w = 0;
+      for (size_t k = 0; k < mine.size(); ++k) {
+        Job& j = jobs[mine[k]];
+        if (j.task && j.task->h.done())
+          finish(mine[k]);
+        else
+          mine[w++] = mine[k];
+      }
+      mine.resize(w);
+    };
+    // take at most a fair share of the live cap so every engine gets work
+    const int64_t share = std::max<int64_t>(1, (max_live + G - 1) / G);
+    for (;;) {
+      // admission
+      for (;;) {
+        int64_t idx = -1;
+        {
+          std::lock_guard<std::mutex> lk(sh.mu);
+          if (sh.fatal) return;
+          double t = now_s() - t0;
+          if (sh.next < n && sh.live < max_live && (int64_t)mine.size() < share &&
+              (!arrival || arrival[sh.next] <= t) && (sh.live == 0 || sh.live_bytes + est[sh.next] <= budget)) {
+            idx = sh.next++;
+            ++sh.live;
+            sh.live_bytes += est[idx];
+          }
+        }
+        if (idx < 0) break;
+        Job& j = jobs[idx];
+        j.arrival = arrival ? arrival[idx] : 0.0;
+        j.t_start = now_s() - t0;
+        const tci_request& r = reqs[idx];
+        int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
+        if (rc) {
+          j.started = j.done = true;
+          j.rc = rc;
+          std::lock_guard<std::mutex> lk(sh.mu);
+          if (!sh.first_rc) {
+            sh.first_rc = rc;
+            sh.first_msg = last_message();
+          }
+          --sh.live;
+          ++sh.finished;
+          sh.live_bytes -= est[idx];
+          continue;
+        }
+        std::vector<std::vector<uint8_t>> piv(1, std::vector<uint8_t>(r.L, 0));
+        j.task.emplace(co_crossinterpolate2(e, j.solve->s, piv, r.opts));
+        j.started = true;
+        mine.push_back(idx);
+        j.task->h.resume();
+      }
+      reap();
+      bool progressed = false;
       if (e.inflight() && e.ready()) {
         int rc = e.complete();
-        if (rc) return rc;
+        if (rc) {
+          std::lock_guard<std::mutex> lk(sh.mu);
+          sh.fatal = rc;
+          sh.fatal_msg = last_message();
+          return;
+        }
+        reap();
         progressed = true;
       }
-      reap(g);
       if (!e.inflight() && !e.idle()) {
         int rc = e.launch();
-        if (rc) return rc;
+        if (rc) {
+          std::lock_guard<std::mutex> lk(sh.mu);
+          sh.fatal = rc;
+          sh.fatal_msg = last_message();
+          return;
+        }
         progressed = true;
       }
+      if (progressed) continue;
+      if (e.inflight()) {  // nothing else to do here: wait for the GPU
+        int rc = e.complete();
+        if (rc) {
+          std::lock_guard<std::mutex> lk(sh.mu);
+          sh.fatal = rc;
+          sh.fatal_msg = last_message();
+          return;
+        }
+        reap();
+        continue;
+      }
+      if (!mine.empty()) {  // live solves but no pending task: cannot happen
+        std::lock_guard<std::mutex> lk(sh.mu);
+        sh.fatal = TCI_ERR_GENERIC;
+        sh.fatal_msg = "engine stalled with live solves";
+        return;
+      }
+      double wait = 0;
+      {
+        std::lock_guard<std::mutex> lk(sh.mu);
+        if (sh.next >= n || sh.fatal) return;  // nothing left for this engine
+        if (arrival) wait = arrival[sh.next] - (now_s() - t0);
+      }
+      if (wait > 0)
+        std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 1e-3)));
+      else
+        std::this_thread::yield();
     }
-    if (progressed || finished >= n) continue;
-    // nothing ready: block on the first batch in flight, or wait for arrivals
-    int busy = -1;
-    for (int g = 0; g < G && busy < 0; ++g)
-      if (pool[g]->inflight()) busy = g;
-    if (busy >= 0) {
-      int rc = pool[busy]->complete();
-      if (rc) return rc;
-      reap(busy);
-      continue;
-    }
-    if (live == 0 && next < n && arrival) {
-      double wait = arrival[next] - (now_s() - t0);
-      if (wait > 0) std::this_thread::sleep_for(std::chrono::duration<double>(wait));
-      continue;
-    }
-    if (live > 0) return fail(TCI_ERR_GENERIC, "engine stalled with live solves");
-  }
-  return first_rc;
+  };
+  std::vector<std::thread> threads;
+  for (int g = 1; g < G; ++g) threads.emplace_back(worker, g);
+  worker(0);
+  for (auto& t : threads) t.join();
+  if (sh.fatal) return fail(sh.fatal, sh.fatal_msg);
+  if (sh.first_rc) set_error(sh.first_rc, sh.first_msg);
+  return sh.first_rc;
 }
 }  // namespace
 

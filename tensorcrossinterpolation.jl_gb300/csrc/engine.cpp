@@ -837,9 +837,9 @@ CoTask co_sweep2site(Engine& e, Solve& s, int niter, int iter1, double abstol, i
   for (int iter = iter1; iter < iter1 + niter; ++iter) {
     std::vector<IndexSet> extraI, extraJ;
     bool use_extra = !strictlynested && s.has_hist;
-    if (use_extra) {
-      extraI = s.Ihist;
-      extraJ = s.Jhist;
+    if (use_extra) {  // the snapshot is replaced right below, so take it
+      extraI = std::move(s.Ihist);
+      extraJ = std::move(s.Jhist);
     }
     s.Ihist = s.Iset;
     s.Jhist = s.Jset;
