@@ -40,17 +40,9 @@ UNIT = "solves/s"
 
 def make_requests(n, seed):
     """Served-stream family requests (L, d, params, tol, maxbonddim)."""
-    rng = np.random.default_rng(seed)
-    out = []
-    for _ in range(n):
-        L = int(rng.integers(4, 17))
-        d = int(rng.integers(2, 17))
-        a, b, g = 10 ** rng.uniform(-2, 1, size=3)
-        c = rng.integers(1, d + 1, size=L)
-        tol = float(10 ** rng.uniform(-10, -6))
-        mbd = int(rng.choice([32, 64, 128, 256]))
-        out.append((L, d, [a, b, g] + [float(x) for x in c], tol, mbd))
-    return out
+    from tci_gb300 import workloads
+
+    return workloads.served_requests(n, seed)
 
 
 # FP64 operations per registered-function evaluation of the served family,
@@ -151,6 +143,47 @@ def cpu_baseline(reqs, seconds=20.0):
                       f"oracle on {cores} threads, {dt:.1f} s"}
 
 
+def rrlu_batch_bench(T, ctx, peak_sep, with_cpu=True, reps=3):
+    """The batched-rrLU configuration: 4096 matrices (2r)x(2r), r in [8, 128], seed 0,
+    reltol 1e-10, maxrank 256, one launch.  Device time from CUDA events around the
+    step kernel; e2e through tci_rrlu_batched with host buffers."""
+    from tci_gb300 import workloads
+
+    mats = workloads.rrlu_batch(4096, seed=0)
+    nbytes = sum(a.size for a in mats) * 8
+    T.rrlu_batched(mats[:64], maxrank=256, reltol=1e-10, ctx=ctx)  # warm-up
+    e2e = []
+    kern = []
+    ops = 0.0
+    for _ in range(reps):
+        ctx.stats(reset=True)
+        t0 = time.perf_counter()
+        res = T.rrlu_batched(mats, maxrank=256, reltol=1e-10, ctx=ctx)
+        e2e.append(time.perf_counter() - t0)
+        st = ctx.stats(reset=True)
+        kern.append(st["kernel_ms"] * 1e-3)
+        ops = 2.0 * st["lu_updates"]
+    kt = float(np.median(kern))
+    out = {"workload": "4096 matrices (2r)x(2r), r uniform in [8,128] (seed 0), U diag(10^(-k/4)) V^T + 1e-12 "
+                       "noise, reltol 1e-10, maxrank 256",
+           "matrices_per_s_device": len(mats) / kt, "kernel_ms": kt * 1e3,
+           "e2e_matrices_per_s": len(mats) / float(np.median(e2e)),
+           "mean_npivot": float(np.mean([r[2] for r in res])),
+           "fp64_tflops": ops / kt / 1e12, "fp64_frac_of_measured": ops / kt / peak_sep,
+           "input_gb": nbytes / 1e9, "input_read_gbs": nbytes / kt / 1e9}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        sub = mats[::16]
+        t0 = time.perf_counter()
+        O.rrlu_batched(sub, maxrank=256, reltol=1e-10)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": len(sub) / dt, "unit": "matrices/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"every 16th matrix ({len(sub)}), oracle rrlu on {os.cpu_count()} threads"}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -182,6 +215,8 @@ def main():
     ap.add_argument("--live", type=int, default=1024)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
+    ap.add_argument("--only", default="", help="'rrlu': run only the batched-rrLU configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -192,6 +227,9 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     ctx = T.Context(int(os.environ.get("LOCAL_RANK", "0")))
     peak_sep, peak_fma = T.fp64_peak(ctx)
+    if args.only == "rrlu":  # the batched-rrLU configuration alone (one warm-up launch, then --steps)
+        print(json.dumps(rrlu_batch_bench(T, ctx, peak_sep, with_cpu=False, reps=max(1, args.steps))))
+        return
 
     def specs_for(step):
         reqs = make_requests(args.batch, seed=1000 * step + rank)
@@ -275,6 +313,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(make_requests(4096, seed=31), seconds=20.0)
+    rrlu_line = None if args.no_rrlu else rrlu_batch_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
 
     line = {
         "metric": METRIC, "value": value * world, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -302,6 +341,8 @@ def main():
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if rrlu_line:
+        line["rrlu_batch"] = rrlu_line
     if rank == 0:
         print(json.dumps(line))
 

@@ -169,6 +169,30 @@ def rrlu(A, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True):
     return res
 
 
+def rrlu_batched(mats, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True, nthreads=None):
+    """Many rrLUs on host threads -> list of (rows, cols, npivot, error), 0-based."""
+    import os
+    ms = np.array([a.shape[0] for a in mats], np.int64)
+    ns = np.array([a.shape[1] for a in mats], np.int64)
+    offs = np.concatenate([[0], np.cumsum(ms * ns)[:-1]]).astype(np.int64)
+    flat = np.ascontiguousarray(np.concatenate([np.asarray(a, np.float64).reshape(-1, order="F") for a in mats]))
+    kcap = np.minimum(ms, ns)
+    poffs = np.concatenate([[0], np.cumsum(2 * kcap)[:-1]]).astype(np.int64)
+    piv = np.zeros(int(2 * kcap.sum()) + 1, np.int64)
+    npiv = np.zeros(len(mats), np.int64)
+    errs = np.zeros(len(mats))
+    _check(lib().orc_rrlu_batched(len(mats), _p(flat, F64P), _p(offs, I64P), _p(ms, I64P), _p(ns, I64P),
+                                  0 if maxrank is None else int(maxrank), reltol, abstol, int(leftorthogonal),
+                                  _p(piv, I64P), _p(poffs, I64P), _p(npiv, I64P), _p(errs, F64P),
+                                  int(nthreads or os.cpu_count() or 1)))
+    out = []
+    for i in range(len(mats)):
+        K = int(npiv[i])
+        o = poffs[i]
+        out.append((piv[o:o + 2 * K:2].copy(), piv[o + 1:o + 2 * K:2].copy(), K, float(errs[i])))
+    return out
+
+
 def luci(A, maxrank=None, reltol=1e-14, abstol=0.0, leftorthogonal=True):
     """MatrixLUCI left/right (matrixluci.jl:70-84)."""
     A = np.asfortranarray(A, dtype=np.float64)
