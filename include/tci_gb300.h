@@ -248,6 +248,13 @@ typedef struct tci_stats {
   double kernel_ms;
   int64_t feval, lu_updates;
   int64_t h2d_bytes, d2h_bytes;
+  /* host milliseconds spent packing/launching steps, waiting for them, and
+   * resuming the solves after them (summed over the engines' threads) */
+  double host_launch_ms, host_wait_ms, host_resume_ms;
+  /* SM clock cycles spent inside tasks, summed over all tasks (each task runs
+   * on one CTA, one CTA per SM): divided by SMs x clock x wall time it gives
+   * the fraction of the device kept busy */
+  int64_t task_cycles;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
 

@@ -157,6 +157,10 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.lu_updates += s.lu_updates;
     t.h2d_bytes += s.h2d_bytes;
     t.d2h_bytes += s.d2h_bytes;
+    t.host_launch_ms += s.host_launch_ms;
+    t.host_wait_ms += s.host_wait_ms;
+    t.host_resume_ms += s.host_resume_ms;
+    t.task_cycles += s.task_cycles;
     if (reset) e->stats = tci_stats{};
   }
   *out = t;

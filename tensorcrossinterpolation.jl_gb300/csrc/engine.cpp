@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <numeric>
@@ -335,8 +336,19 @@ int Engine::step() {
 
 bool Engine::ready() const { return !inflight_ || cudaEventQuery(done_) != cudaErrorNotReady; }
 
+namespace {
+// Adds the lifetime of the object, in milliseconds, to a counter.
+struct MsTimer {
+  double& acc;
+  std::chrono::steady_clock::time_point t0;
+  explicit MsTimer(double& a) : acc(a), t0(std::chrono::steady_clock::now()) {}
+  ~MsTimer() { acc += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count(); }
+};
+}  // namespace
+
 int Engine::launch() {
   if (pending_.empty() || inflight_) return 0;
+  MsTimer timer(stats.host_launch_ms);
   std::vector<Req*>& batch = fl_batch_;
   batch.clear();
   batch.swap(pending_);
@@ -469,7 +481,11 @@ int Engine::launch() {
 
 int Engine::complete() {
   if (!inflight_) return 0;
-  CUDA_TRY(cudaEventSynchronize(done_));
+  {
+    MsTimer timer(stats.host_wait_ms);
+    CUDA_TRY(cudaEventSynchronize(done_));
+  }
+  MsTimer timer(stats.host_resume_ms);
   inflight_ = false;
   std::vector<Req*>& batch = fl_batch_;
   const size_t nt = batch.size();
@@ -489,6 +505,7 @@ int Engine::complete() {
   for (size_t i = 0; i < nt; ++i) {
     Req& r = *batch[i];
     r.res = hres_ + o_res[i];
+    stats.task_cycles += r.head()->cycles;
     if (task_log_) {
       const tci_result_head* h = r.head();
       std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d\n", (long long)stats.steps, r.t.kind, r.t.m,

@@ -33,7 +33,6 @@ namespace {
 constexpr int NT = TCI_STEP_THREADS;
 constexpr int NW = NT / 32;
 constexpr unsigned FULL = 0xffffffffu;
-constexpr uint64_t ABS_MASK = 0x7fffffffffffffffULL;
 constexpr uint64_t NAN_FLOOR = 0x7ff0000000000000ULL;  // bits above this are NaN
 constexpr uint64_t SQ_SMALL = (uint64_t)(1023 - 500) << 52;  // below: squares may be subnormal
 constexpr uint64_t SQ_BIG = (uint64_t)(1023 + 500) << 52;    // above: squares may overflow
@@ -54,29 +53,51 @@ __device__ __forceinline__ double jmax(double a, double b) {
   return a > b ? a : b;
 }
 
+// Bit pattern of |v| computed on the integer pipe.  Written as a register move
+// plus integer AND so that it cannot be lowered to an FP64 absolute-value
+// instruction: on this GPU the FP64 pipe is 1/64 of the FP32 rate and is the
+// bottleneck of the rank-1 update.
+__device__ __forceinline__ uint64_t abs_bits(double v) {
+  unsigned lo, hi;
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(v));
+  return ((uint64_t)(hi & 0x7fffffffu) << 32) | (uint64_t)lo;
+}
+
 // Running argmax of abs2 with first-in-column-major tie breaking.
-struct ArgBest {
+// The argmax runs in two passes so that the FP64 pipe only sees the update:
+// while updating, each thread keeps the largest |v| bit pattern (integer ops,
+// NaN excluded); after a block-wide max M*, a read-only pass squares just the
+// elements whose |v| is within 16 ulps of M* (where v*v can tie with M*^2) and
+// picks the largest square, ties to the smallest column-major key.  Below
+// 2^-500 or above 2^500 squares can underflow or overflow, so there every
+// element is squared.
+struct AbsMax {
   uint64_t M;
+  __device__ __forceinline__ void init() { M = 0; }
+  __device__ __forceinline__ void push(double v) {
+    uint64_t b = abs_bits(v);
+    if (b <= NAN_FLOOR && b > M) M = b;
+  }
+};
+
+struct ArgBest {
   double bs;
   int key;
   __device__ __forceinline__ void init() {
-    M = 0;
     bs = -1.0;
     key = 0x7fffffff;
   }
-  __device__ __forceinline__ void push(double v, int k) {
-    uint64_t b = (uint64_t)__double_as_longlong(v) & ABS_MASK;
-    if (b > NAN_FLOOR) return;
-    if (b + 16 >= M || M < SQ_SMALL || M >= SQ_BIG) {
-      double s = __dmul_rn(v, v);
-      if (s > bs || (s == bs && k < key)) {
-        bs = s;
-        key = k;
-      }
-      if (b > M) M = b;
+  __device__ __forceinline__ void consider(double v, int k) {
+    double s = __dmul_rn(v, v);
+    if (s > bs || (s == bs && k < key)) {
+      bs = s;
+      key = k;
     }
   }
 };
+__device__ __forceinline__ bool near_max(uint64_t b, uint64_t Mstar) {
+  return b <= NAN_FLOOR && (b + 16 >= Mstar || Mstar < SQ_SMALL || Mstar >= SQ_BIG);
+}
 
 __device__ __forceinline__ void arg_combine(double& bs, int& key, double obs, int okey) {
   if (obs > bs || (obs == bs && okey < key)) {
@@ -168,6 +189,32 @@ __device__ void block_max4(double v[4], Ctl& ctl) {
 #pragma unroll
   for (int q = 0; q < 4; ++q) v[q] = ctl.red4[q][NW];
   __syncthreads();
+}
+
+// Second argmax pass over the block A[r0:r0+rows, c0:c0+cols] of a matrix with
+// m rows (keys j*m + i, the column-major position).  Every thread gets the
+// result; bs < 0 means no element qualified (all NaN).
+__device__ void exact_argmax(const double* A, int lda, int m, int r0, int rows, int c0, int cols,
+                             uint64_t Mstar, Ctl& ctl, double& bs, int& key) {
+  ArgBest ab;
+  ab.init();
+  if (rows > 0 && cols > 0) {
+    const long long total = (long long)rows * cols;
+    const int sq = NT / rows, sr = NT % rows;
+    int jj = threadIdx.x / rows, ii = threadIdx.x % rows;
+    for (long long e = threadIdx.x; e < total; e += NT) {
+      const int i = r0 + ii, j = c0 + jj;
+      const double v = A[i + (size_t)j * lda];
+      if (near_max(abs_bits(v), Mstar)) ab.consider(v, j * m + i);
+      ii += sr;
+      jj += sq;
+      if (ii >= rows) {
+        ii -= rows;
+        jj += 1;
+      }
+    }
+  }
+  block_argmax(ab, ctl, bs, key);
 }
 
 __device__ int block_or(int v, Ctl& ctl) {
@@ -288,7 +335,7 @@ __device__ ResPtrs res_ptrs(char* resb, const tci_task& T) {
 // first argmax already in ctl.r/ctl.c.  rowperm/colperm are full permutations.
 __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
                           bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   const int kmax = min(maxrank, min(m, n));
   if (tid == 0) {
     ctl.K = 0;
@@ -354,22 +401,35 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
     ++K;
     if (K == kmax) break;  // the trailing update after the last pivot is not observable
     // A[K:, K:] -= x * y^T fused with the argmax of abs2 for the next pivot
-    ArgBest ab;
-    ab.init();
-    const double* x = A + (size_t)(K - 1) * lda;
-    for (int j = K + warp; j < n; j += NW) {
-      double* col = A + (size_t)j * lda;
-      const double y = col[K - 1];
-      const int kb = j * m;
-      for (int i = K + lane; i < m; i += 32) {
-        double v = __dsub_rn(col[i], __dmul_rn(x[i], y));
+    // The trailing block is walked as one column-major sequence so that every
+    // lane of every warp has an element (no half-empty warps at column ends).
+    AbsMax am;
+    am.init();
+    {
+      const double* x = A + (size_t)(K - 1) * lda;
+      const int rows = m - K;
+      const long long total = (long long)rows * (n - K);
+      const int sq = NT / rows, sr = NT % rows;  // stride NT as (columns, rows)
+      int jj = tid / rows, ii = tid % rows;
+      for (long long e = tid; e < total; e += NT) {
+        const int i = K + ii, j = K + jj;
+        double* col = A + (size_t)j * lda;
+        double v = __dsub_rn(col[i], __dmul_rn(x[i], col[K - 1]));
         col[i] = v;
-        ab.push(v, kb + i);
+        am.push(v);
+        ii += sr;
+        jj += sq;
+        if (ii >= rows) {
+          ii -= rows;
+          jj += 1;
+        }
       }
     }
+    __syncthreads();
+    const uint64_t Mstar = block_max_u64(am.M, ctl);
     double bs;
     int key;
-    block_argmax(ab, ctl, bs, key);
+    exact_argmax(A, lda, m, K, m - K, K, n - K, Mstar, ctl, bs, key);
     if (tid == 0) {
       if (bs < 0.0) {  // every candidate NaN: Julia's loop keeps the first index
         ctl.r = K;
@@ -499,8 +559,8 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   for (int i = tid; i < m; i += NT) rowperm[i] = i;
   for (int j = tid; j < n; j += NT) colperm[j] = j;
   int lut_used = 0;
-  ArgBest ab;
-  ab.init();
+  AbsMax am;
+  am.init();
   unsigned long long mx = 0;
   if (T.ain) {
     for (int j = warp; j < n; j += NW) {
@@ -509,8 +569,8 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
       for (int i = lane; i < m; i += 32) {
         double v = src[i];
         dst[i] = v;
-        ab.push(v, j * m + i);
-        unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+        am.push(v);
+        unsigned long long b = abs_bits(v);
         mx = b > mx ? b : mx;
       }
     }
@@ -534,17 +594,18 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
       for (int i = lane; i < m; i += 32) {
         double v = F(rs0[i] + c0, rs1[i] + c1);
         dst[i] = v;
-        ab.push(v, j * m + i);
-        unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+        am.push(v);
+        unsigned long long b = abs_bits(v);
         mx = b > mx ? b : mx;
       }
     }
   }
   __syncthreads();
   unsigned long long mxall = block_max_u64(mx, ctl);
+  const uint64_t Mstar = block_max_u64(am.M, ctl);
   double bs;
   int key;
-  block_argmax(ab, ctl, bs, key);
+  exact_argmax(A, lda, m, 0, m, 0, n, Mstar, ctl, bs, key);
   if (tid == 0) {
     if (bs < 0.0 || m == 0 || n == 0) {
       ctl.r = 0;
@@ -615,18 +676,19 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   const double* rg1[2] = {ps1, rs1};
   const int rc[2] = {r, m};
   const Filler F = make_filler(T, prm, rg0, rg1, rc, 2, cs0, cs1, r, (int64_t)(r + m) * r, ctl);
-  ArgBest ab;
-  ab.init();
+  AbsMax am;
+  am.init();
   for (int j = warp; j < r; j += NW)
     for (int i = lane; i < r; i += 32) {
       double v = F(ps0[i] + cs0[j], ps1[i] + cs1[j]);
       P[i + (size_t)j * r] = v;
-      ab.push(v, j * r + i);
+      am.push(v);
     }
   __syncthreads();
+  const uint64_t Mstar = block_max_u64(am.M, ctl);
   double bs;
   int key;
-  block_argmax(ab, ctl, bs, key);
+  exact_argmax(P, r, r, 0, r, 0, r, Mstar, ctl, bs, key);
   if (tid == 0) {
     ctl.r = bs < 0.0 ? 0 : key % r;
     ctl.c = bs < 0.0 ? 0 : key / r;
@@ -656,7 +718,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
       int row = base + rr, col = colperm[q];
       double v = F(rs0[row] + cs0[col], rs1[row] + cs1[col]);
       W[rr + (size_t)q * RB] = v;
-      unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+      unsigned long long b = abs_bits(v);
       mx = b > mx ? b : mx;
     }
     __syncthreads();
@@ -718,7 +780,7 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
     for (int i = lane; i < m; i += 32) {
       double v = F(rs0[i] + cs0[j], rs1[i] + cs1[j]);
       T.core_out[i + (size_t)j * m] = v;
-      unsigned long long b = (unsigned long long)__double_as_longlong(v) & ABS_MASK;
+      unsigned long long b = abs_bits(v);
       mx = b > mx ? b : mx;
     }
   unsigned long long mxall = block_max_u64(mx, ctl);

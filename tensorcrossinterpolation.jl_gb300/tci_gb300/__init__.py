@@ -86,6 +86,10 @@ class Stats(ctypes.Structure):
         ("lu_updates", ctypes.c_int64),
         ("h2d_bytes", ctypes.c_int64),
         ("d2h_bytes", ctypes.c_int64),
+        ("host_launch_ms", ctypes.c_double),
+        ("host_wait_ms", ctypes.c_double),
+        ("host_resume_ms", ctypes.c_double),
+        ("task_cycles", ctypes.c_int64),
     ]
 
 
