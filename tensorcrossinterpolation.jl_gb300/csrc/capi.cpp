@@ -20,10 +20,15 @@ using namespace tci;
 // solves over all of them so that one engine's host work and kernel tail
 // overlap the others' kernels.
 struct tci_ctx {
+  // declaration order = reverse destruction order: the engines go first, then
+  // the ring, then the pools their blocks came from
+  std::unique_ptr<BlockPool> dpool;
+  std::vector<std::unique_ptr<BlockPool>> hpools, spools;  // per engine: task records, task scratch
+  std::unique_ptr<ResidentQueue> rq;  // null: batched launches only
   std::vector<std::unique_ptr<Engine>> pool;
-  Engine& eng;
+  Engine* engp = nullptr;
   std::mutex mu;
-  explicit tci_ctx(std::vector<std::unique_ptr<Engine>>&& p) : pool(std::move(p)), eng(*pool[0]) {}
+  Engine& eng_ref() { return *engp; }
 };
 
 struct tci_solve {
@@ -111,22 +116,40 @@ int tci_f_lookup(const char* name, int* fid) {
 
 int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
   *out = nullptr;
-  int neng = 8;  // engines (streams + host threads) of the batched/served paths
-  if (const char* s = std::getenv("TCI_ENGINES")) neng = std::max(1, std::min(16, std::atoi(s)));
-  std::vector<std::unique_ptr<Engine>> pool;
+  // Engines = host threads of the batched/served paths.  Resident mode (the
+  // default) feeds one persistent kernel through a ring in pinned memory;
+  // TCI_RESIDENT=0 selects one batched launch per engine step instead.
+  bool resident = true;
+  if (const char* s = std::getenv("TCI_RESIDENT")) resident = std::atoi(s) != 0;
+  int neng = resident ? 12 : 8;
+  if (const char* s = std::getenv("TCI_ENGINES")) neng = std::max(1, std::min(32, std::atoi(s)));
+  std::unique_ptr<tci_ctx> c(new tci_ctx());
+  c->dpool.reset(new BlockPool(BlockPool::DEVICE, device, true));
   for (int i = 0; i < neng; ++i) {
-    pool.emplace_back(new Engine(device));
-    int rc = pool.back()->init();
+    c->pool.emplace_back(new Engine(device));
+    int rc = c->pool.back()->init();  // fails first when there is no device
+    if (rc) return rc;
+    if (i == 0 && !c->dpool->reserve_slab()) return fail(TCI_ERR_OOM, "device memory for site tensors");
+    c->pool.back()->set_device_pool(c->dpool.get());
+    c->hpools.emplace_back(new BlockPool(BlockPool::HOST, device, false));
+    c->spools.emplace_back(new BlockPool(BlockPool::DEVICE, device, false));
+    if (resident && !c->hpools.back()->reserve_slab()) return fail(TCI_ERR_OOM, "pinned host memory");
+  }
+  c->engp = c->pool[0].get();
+  if (resident) {
+    c->rq.reset(new ResidentQueue());
+    int idle_us = 20000;
+    if (const char* s = std::getenv("TCI_RESIDENT_IDLE_US")) idle_us = std::max(100, std::atoi(s));
+    int rc = c->rq->init(device, c->pool[0]->num_sms, idle_us);
     if (rc) return rc;
   }
-  auto* c = new tci_ctx(std::move(pool));
   if (hbm_budget == 0) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     hbm_budget = (size_t)(0.8 * (double)fr);
   }
   for (auto& e : c->pool) e->hbm_budget = hbm_budget;
-  *out = c;
+  *out = c.release();
   return 0;
 }
 
@@ -135,7 +158,7 @@ int tci_ctx_destroy(tci_ctx* ctx) {
   return 0;
 }
 
-uintptr_t tci_ctx_stream(tci_ctx* ctx) { return (uintptr_t)ctx->eng.stream(); }
+uintptr_t tci_ctx_stream(tci_ctx* ctx) { return (uintptr_t)ctx->eng_ref().stream(); }
 
 int tci_ctx_synchronize(tci_ctx* ctx) {
   for (auto& eng : ctx->pool) {
@@ -163,6 +186,14 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.task_cycles += s.task_cycles;
     if (reset) e->stats = tci_stats{};
   }
+  if (ctx->rq) {
+    t.kernel_ms += ctx->rq->kernel_ms;
+    t.launches += ctx->rq->launches;
+    if (reset) {
+      ctx->rq->kernel_ms = 0;
+      ctx->rq->launches = 0;
+    }
+  }
   *out = t;
   return 0;
 }
@@ -189,11 +220,11 @@ int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t 
   if (rc) return rc;
   auto piv = to_pivots(pivots, np, L, (*out)->s.d, &rc);
   if (!rc) {
-    CoTask t = co_construct(ctx->eng, (*out)->s, piv);
-    rc = ctx->eng.run(t);
+    CoTask t = co_construct(ctx->eng_ref(), (*out)->s, piv);
+    rc = ctx->eng_ref().run(t);
   }
   if (rc) {
-    ctx->eng.release_cores((*out)->s);
+    ctx->eng_ref().release_cores((*out)->s);
     delete *out;
     *out = nullptr;
   }
@@ -203,7 +234,7 @@ int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t 
 int tci_solve_destroy(tci_solve* s) {
   if (!s) return 0;
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  s->ctx->eng.release_cores(s->s);
+  s->ctx->eng_ref().release_cores(s->s);
   delete s;
   return 0;
 }
@@ -227,11 +258,11 @@ int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int
       o = *opts;
     else
       tci_opts_default(&o);
-    CoTask t = co_crossinterpolate2(ctx->eng, (*out)->s, piv, o);
-    rc = ctx->eng.run(t);
+    CoTask t = co_crossinterpolate2(ctx->eng_ref(), (*out)->s, piv, o);
+    rc = ctx->eng_ref().run(t);
   }
   if (rc) {
-    ctx->eng.release_cores((*out)->s);
+    ctx->eng_ref().release_cores((*out)->s);
     delete *out;
     *out = nullptr;
   }
@@ -245,39 +276,39 @@ int tci_optimize(tci_solve* s, const tci_opts* opts) {
     o = *opts;
   else
     tci_opts_default(&o);
-  CoTask t = co_optimize(s->ctx->eng, s->s, o);
-  return s->ctx->eng.run(t);
+  CoTask t = co_optimize(s->ctx->eng_ref(), s->s, o);
+  return s->ctx->eng_ref().run(t);
 }
 
 int tci_updatepivots(tci_solve* s, int32_t b, int32_t leftorthogonal, double reltol, double abstol,
                      int64_t maxbonddim) {
   std::lock_guard<std::mutex> lk(s->ctx->mu);
   if (b < 1 || b > s->s.L - 1) return fail(TCI_ERR_ARG, "bond index out of range");
-  CoTask t = co_updatepivots(s->ctx->eng, s->s, b - 1, leftorthogonal != 0, reltol, abstol,
+  CoTask t = co_updatepivots(s->ctx->eng_ref(), s->s, b - 1, leftorthogonal != 0, reltol, abstol,
                              maxbonddim <= 0 ? TYPEMAX : maxbonddim, nullptr, nullptr);
-  return s->ctx->eng.run(t);
+  return s->ctx->eng_ref().run(t);
 }
 
 int tci_sweep2site(tci_solve* s, int32_t niter, int32_t iter1, double abstol, int64_t maxbonddim,
                    int32_t sweepstrategy, int32_t strictlynested, int32_t fillsitetensors) {
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  CoTask t = co_sweep2site(s->ctx->eng, s->s, niter, iter1, abstol, maxbonddim <= 0 ? TYPEMAX : maxbonddim,
+  CoTask t = co_sweep2site(s->ctx->eng_ref(), s->s, niter, iter1, abstol, maxbonddim <= 0 ? TYPEMAX : maxbonddim,
                            sweepstrategy, strictlynested != 0, fillsitetensors != 0);
-  return s->ctx->eng.run(t);
+  return s->ctx->eng_ref().run(t);
 }
 
 int tci_sweep1site(tci_solve* s, int32_t forward, double reltol, double abstol, int64_t maxbonddim,
                    int32_t updatetensors) {
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  CoTask t = co_sweep1site(s->ctx->eng, s->s, forward != 0, reltol, abstol,
+  CoTask t = co_sweep1site(s->ctx->eng_ref(), s->s, forward != 0, reltol, abstol,
                            maxbonddim <= 0 ? TYPEMAX : maxbonddim, updatetensors != 0);
-  return s->ctx->eng.run(t);
+  return s->ctx->eng_ref().run(t);
 }
 
 int tci_fillsitetensors(tci_solve* s) {
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  CoTask t = co_fillsitetensors(s->ctx->eng, s->s);
-  return s->ctx->eng.run(t);
+  CoTask t = co_fillsitetensors(s->ctx->eng_ref(), s->s);
+  return s->ctx->eng_ref().run(t);
 }
 
 int tci_addglobalpivots(tci_solve* s, const int64_t* pivots, int64_t np) {
@@ -286,7 +317,7 @@ int tci_addglobalpivots(tci_solve* s, const int64_t* pivots, int64_t np) {
   auto piv = to_pivots(pivots, np, s->s.L, s->s.d, &rc);
   if (rc) return rc;
   rc = addglobalpivots(s->s, piv);
-  if (!rc && !piv.empty()) s->ctx->eng.release_cores(s->s);
+  if (!rc && !piv.empty()) s->ctx->eng_ref().release_cores(s->s);
   return rc;
 }
 
@@ -339,10 +370,10 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
   dims[2] = c.d2;
   if (out && c.elems()) {
     cudaError_t e = cudaMemcpyAsync(out, c.p, c.elems() * sizeof(double), cudaMemcpyDeviceToHost,
-                                    s->ctx->eng.stream());
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->eng.stream());
+                                    s->ctx->eng_ref().stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->ctx->eng_ref().stream());
     if (e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(e));
-    s->ctx->eng.stats.d2h_bytes += (int64_t)(c.elems() * sizeof(double));
+    s->ctx->eng_ref().stats.d2h_bytes += (int64_t)(c.elems() * sizeof(double));
   }
   return 0;
 }
@@ -366,7 +397,7 @@ int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, dou
     expect = pos;
   }
   if (n == 0) return 0;
-  return ctx->eng.gather_to_host(src, len, out + out_offsets[0]);
+  return ctx->eng_ref().gather_to_host(src, len, out + out_offsets[0]);
 }
 
 int tci_get_errors(const tci_solve* s, double* pivoterrors, int64_t* npe, double* bonderrors) {
@@ -397,8 +428,8 @@ int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
   for (int64_t b = 0; b < np; b += chunk) {
     int64_t n = std::min(chunk, np - b);
     std::vector<uint8_t> sub(pts.begin() + b * s->s.L, pts.begin() + (b + n) * s->s.L);
-    CoTask t = co_evaluate(s->ctx->eng, s->s, sub, n, nullptr, out + b);
-    rc = s->ctx->eng.run(t);
+    CoTask t = co_evaluate(s->ctx->eng_ref(), s->s, sub, n, nullptr, out + b);
+    rc = s->ctx->eng_ref().run(t);
     if (rc) return rc;
   }
   return 0;
@@ -406,8 +437,8 @@ int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
 
 int tci_sum(tci_solve* s, double* out) {
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  CoTask t = co_sum(s->ctx->eng, s->s, out);
-  return s->ctx->eng.run(t);
+  CoTask t = co_sum(s->ctx->eng_ref(), s->s, out);
+  return s->ctx->eng_ref().run(t);
 }
 
 // ---------------------------------------------------------------- batches / serving
@@ -483,6 +514,7 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
     };
     // take at most a fair share of the live cap so every engine gets work
     const int64_t share = std::max<int64_t>(1, (max_live + G - 1) / G);
+    double last_progress = now_s(), last_done = last_progress;
     for (;;) {
       // admission
       for (;;) {
@@ -524,39 +556,58 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
         j.task->h.resume();
       }
       reap();
-      bool progressed = false;
-      if (e.inflight() && e.ready()) {
-        int rc = e.complete();
-        if (rc) {
-          std::lock_guard<std::mutex> lk(sh.mu);
-          sh.fatal = rc;
-          sh.fatal_msg = last_message();
-          return;
-        }
+      auto fatal = [&](int rc) {
+        std::lock_guard<std::mutex> lk(sh.mu);
+        sh.fatal = rc;
+        sh.fatal_msg = last_message();
+      };
+      if (e.resident()) {
+        // publish what the solves queued, resume those whose tasks are done
+        int rc = e.submit();
+        if (rc) return fatal(rc);
+        bool progressed = false;
+        rc = e.poll(progressed);
+        if (rc) return fatal(rc);
         reap();
-        progressed = true;
-      }
-      if (!e.inflight() && !e.idle()) {
-        int rc = e.launch();
-        if (rc) {
-          std::lock_guard<std::mutex> lk(sh.mu);
-          sh.fatal = rc;
-          sh.fatal_msg = last_message();
-          return;
+        const double tnow = now_s();
+        if (progressed) {
+          last_progress = last_done = tnow;
+          continue;
         }
-        progressed = true;
-      }
-      if (progressed) continue;
-      if (e.inflight()) {  // nothing else to do here: wait for the GPU
-        int rc = e.complete();
-        if (rc) {
-          std::lock_guard<std::mutex> lk(sh.mu);
-          sh.fatal = rc;
-          sh.fatal_msg = last_message();
-          return;
+        if (!e.idle()) continue;
+        if (e.has_flights()) {
+          if (tnow - last_progress > 2e-3) {  // the kernel may have left on its idle limit
+            rc = ctx->rq->ensure_alive();
+            if (rc) return fatal(rc);
+            last_progress = tnow;
+          }
+          if (tnow - last_done > 120.0) {
+            set_error(TCI_ERR_TIMEOUT, "resident mode: no task finished for 120 s");
+            return fatal(TCI_ERR_TIMEOUT);
+          }
+          std::this_thread::yield();
+          continue;
         }
-        reap();
-        continue;
+      } else {
+        bool progressed = false;
+        if (e.inflight() && e.ready()) {
+          int rc = e.complete();
+          if (rc) return fatal(rc);
+          reap();
+          progressed = true;
+        }
+        if (!e.inflight() && !e.idle()) {
+          int rc = e.launch();
+          if (rc) return fatal(rc);
+          progressed = true;
+        }
+        if (progressed) continue;
+        if (e.inflight()) {  // nothing else to do here: wait for the GPU
+          int rc = e.complete();
+          if (rc) return fatal(rc);
+          reap();
+          continue;
+        }
       }
       if (!mine.empty()) {  // live solves but no pending task: cannot happen
         std::lock_guard<std::mutex> lk(sh.mu);
@@ -576,10 +627,25 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
         std::this_thread::yield();
     }
   };
+  if (ctx->rq) {
+    int rc = ctx->rq->start();
+    if (rc) return rc;
+    for (int g = 0; g < G; ++g) pool[g]->set_resident(ctx->rq.get(), ctx->hpools[g].get(), ctx->spools[g].get());
+  }
   std::vector<std::thread> threads;
   for (int g = 1; g < G; ++g) threads.emplace_back(worker, g);
   worker(0);
   for (auto& t : threads) t.join();
+  if (ctx->rq) {
+    // every published task is done once the kernel has left (a CTA leaves only
+    // when it finds no published ticket, and the workers have stopped)
+    int rc = ctx->rq->stop();
+    for (int g = 0; g < G; ++g) {
+      pool[g]->abandon();  // nothing is left here unless a fatal error stopped the workers
+      pool[g]->set_resident(nullptr, nullptr, nullptr);
+    }
+    if (rc && !sh.fatal) return rc;
+  }
   if (sh.fatal) return fail(sh.fatal, sh.fatal_msg);
   if (sh.first_rc) set_error(sh.first_rc, sh.first_msg);
   return sh.first_rc;
@@ -625,8 +691,8 @@ int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams,
     std::vector<uint8_t> pts;
     pts.reserve((size_t)n * L);
     for (int64_t i = b; i < b + n; ++i) pts.insert(pts.end(), piv[i].begin(), piv[i].end());
-    CoTask t = co_evaluate(ctx->eng, s, pts, n, out + b, nullptr);
-    rc = ctx->eng.run(t);
+    CoTask t = co_evaluate(ctx->eng_ref(), s, pts, n, out + b, nullptr);
+    rc = ctx->eng_ref().run(t);
     if (rc) return rc;
   }
   return 0;
@@ -647,7 +713,7 @@ int tci_rrlu(tci_ctx* ctx, const double* A, int64_t m, int64_t n, int64_t maxran
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (m < 0 || n < 0 || m > INT32_MAX || n > INT32_MAX || m * n > INT32_MAX)
     return fail(TCI_ERR_ARG, "matrix size out of range");
-  Engine& e = ctx->eng;
+  Engine& e = ctx->eng_ref();
   Req r;
   r.t.kind = TCI_TASK_RRLU;
   r.t.m = (int32_t)m;
@@ -702,7 +768,7 @@ int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t*
                      const int64_t* ns, int64_t maxrank, double reltol, double abstol, int32_t leftorthogonal,
                      int64_t* piv, const int64_t* piv_offsets, int64_t* npivots, double* errors) {
   std::lock_guard<std::mutex> lk(ctx->mu);
-  Engine& e = ctx->eng;
+  Engine& e = ctx->eng_ref();
   std::vector<Req> rs((size_t)nmat);
   std::vector<Req*> ptrs;
   for (int64_t i = 0; i < nmat; ++i) {

@@ -13,12 +13,16 @@
 #include <cstdio>
 #include <cstdlib>
 #include <numeric>
+#include <thread>
 
 cudaError_t tci_step_configure();
 size_t tci_step_smem_bytes();
 cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
                             int* counter_dev, int grid, cudaStream_t stream);
 cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
+size_t tci_resident_smem_bytes();
+cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
+                                int grid, cudaStream_t stream);
 
 namespace tci {
 
@@ -190,12 +194,17 @@ int Engine::init() {
 
 double* Engine::alloc_core(size_t elems) {
   if (elems == 0) elems = 1;
+  if (dpool_) return (double*)dpool_->alloc(elems * sizeof(double));
   void* p = nullptr;
   if (cudaMallocAsync(&p, elems * sizeof(double), stream_) != cudaSuccess) return nullptr;
   return (double*)p;
 }
 void Engine::free_core(double* p) {
-  if (p) cudaFreeAsync(p, stream_);
+  if (!p) return;
+  if (dpool_)
+    dpool_->free(p);
+  else
+    cudaFreeAsync(p, stream_);
 }
 void Engine::release_cores(Solve& s) {
   for (auto& c : s.cores) {
@@ -479,6 +488,37 @@ int Engine::launch() {
   return 0;
 }
 
+// Per-task statistics and the optional task trace.
+void Engine::account(const Req& r, int smem_mode) {
+  const tci_result_head* h = r.head();
+  stats.task_cycles += h->cycles;
+  if (task_log_) {
+    std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d\n", (long long)stats.steps, r.t.kind, r.t.m, r.t.n,
+                 r.t.r, h->npivot, (long long)h->cycles, smem_mode, h->lut_used);
+  }
+  const tci_task& t = r.t;
+  switch (t.kind) {
+    case TCI_TASK_RRLU: {
+      if (!t.ain) stats.feval += (int64_t)t.m * t.n;
+      int64_t K = h->npivot;
+      for (int64_t k = 1; k < K; ++k) stats.lu_updates += (int64_t)(t.m - k) * (t.n - k);
+    } break;
+    case TCI_TASK_SITE:
+      stats.feval += (int64_t)t.r * t.r + (int64_t)t.m * t.r;
+      for (int64_t k = 1; k < t.r; ++k) stats.lu_updates += (int64_t)(t.r - k) * (t.r - k);
+      break;
+    case TCI_TASK_CORE:
+      stats.feval += (int64_t)t.m * t.n;
+      break;
+    case TCI_TASK_EVAL:
+    case TCI_TASK_SEARCH:
+      stats.feval += t.m;
+      break;
+    default:
+      break;
+  }
+}
+
 int Engine::complete() {
   if (!inflight_) return 0;
   {
@@ -505,33 +545,7 @@ int Engine::complete() {
   for (size_t i = 0; i < nt; ++i) {
     Req& r = *batch[i];
     r.res = hres_ + o_res[i];
-    stats.task_cycles += r.head()->cycles;
-    if (task_log_) {
-      const tci_result_head* h = r.head();
-      std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d\n", (long long)stats.steps, r.t.kind, r.t.m,
-                   r.t.n, r.t.r, h->npivot, (long long)h->cycles, (int)fl_smem_[i], h->lut_used);
-    }
-    const tci_task& t = r.t;
-    switch (t.kind) {
-      case TCI_TASK_RRLU: {
-        if (!t.ain) stats.feval += (int64_t)t.m * t.n;
-        int64_t K = r.head()->npivot;
-        for (int64_t k = 1; k < K; ++k) stats.lu_updates += (int64_t)(t.m - k) * (t.n - k);
-      } break;
-      case TCI_TASK_SITE:
-        stats.feval += (int64_t)t.r * t.r + (int64_t)t.m * t.r;
-        for (int64_t k = 1; k < t.r; ++k) stats.lu_updates += (int64_t)(t.r - k) * (t.r - k);
-        break;
-      case TCI_TASK_CORE:
-        stats.feval += (int64_t)t.m * t.n;
-        break;
-      case TCI_TASK_EVAL:
-      case TCI_TASK_SEARCH:
-        stats.feval += t.m;
-        break;
-      default:
-        break;
-    }
+    account(r, fl_smem_[i]);
   }
   // Resuming lets each solve continue to its next task (enqueued for the next
   // launch); the Req records of this batch may be gone afterwards.
@@ -541,6 +555,326 @@ int Engine::complete() {
   for (auto& w : ws) {
     w.op->status = 0;
     w.h.resume();
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- pools
+BlockPool::BlockPool(Kind kind, int device, bool locked) : kind_(kind), device_(device), locked_(locked) {
+  free_.resize(64);
+}
+
+BlockPool::~BlockPool() {
+  if (side_) cudaStreamSynchronize(side_);
+  for (void* p : owned_) {
+    if (kind_ == HOST)
+      cudaFreeHost(p);
+    else
+      cudaFree(p);
+  }
+  if (side_) cudaStreamDestroy(side_);
+}
+
+void* BlockPool::backing(size_t bytes) {
+  void* p = nullptr;
+  if (kind_ == HOST) {
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess) return nullptr;
+  } else {
+    if (!side_ && cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+    if (cudaMallocAsync(&p, bytes, side_) != cudaSuccess) return nullptr;
+    if (cudaStreamSynchronize(side_) != cudaSuccess) return nullptr;
+  }
+  owned_.push_back(p);
+  reserved_ += bytes;
+  return p;
+}
+
+bool BlockPool::reserve_slab() {
+  std::unique_lock<std::mutex> lk(mu_, std::defer_lock);
+  if (locked_) lk.lock();
+  char* p = (char*)backing((size_t)1 << SLAB_SHIFT);
+  if (!p) return false;
+  slab_ = p;
+  slab_left_ = (size_t)1 << SLAB_SHIFT;
+  return true;
+}
+
+void* BlockPool::alloc(size_t bytes) {
+  int k = MIN_SHIFT;
+  while (((size_t)1 << k) < bytes) ++k;
+  std::unique_lock<std::mutex> lk(mu_, std::defer_lock);
+  if (locked_) lk.lock();
+  auto& fl = free_[k];
+  if (!fl.empty()) {
+    void* p = fl.back();
+    fl.pop_back();
+    return p;
+  }
+  const size_t sz = (size_t)1 << k;
+  void* p = nullptr;
+  if (k <= CARVE_MAX) {
+    if (slab_left_ < sz) {
+      slab_ = (char*)backing((size_t)1 << SLAB_SHIFT);
+      slab_left_ = slab_ ? ((size_t)1 << SLAB_SHIFT) : 0;
+      if (!slab_) return nullptr;
+    }
+    p = slab_;
+    slab_ += sz;
+    slab_left_ -= sz;
+  } else {
+    p = backing(sz);
+    if (!p) return nullptr;
+  }
+  cls_[p] = k;
+  return p;
+}
+
+void BlockPool::free(void* p) {
+  if (!p) return;
+  std::unique_lock<std::mutex> lk(mu_, std::defer_lock);
+  if (locked_) lk.lock();
+  auto it = cls_.find(p);
+  if (it != cls_.end()) free_[it->second].push_back(p);
+}
+
+// ---------------------------------------------------------------- resident ring
+int ResidentQueue::init(int dev, int num_sms, int idle_us) {
+  device = dev;
+  grid = num_sms;
+  nslots = 1u << 15;
+  mask = nslots - 1;
+  CUDA_TRY(cudaSetDevice(dev));
+  CUDA_TRY(cudaHostAlloc((void**)&slots, sizeof(tci_queue_slot) * nslots,
+                         cudaHostAllocMapped | cudaHostAllocPortable));
+  std::memset((void*)slots, 0, sizeof(tci_queue_slot) * nslots);
+  CUDA_TRY(cudaHostAlloc((void**)&qc, sizeof(tci_queue_ctl), cudaHostAllocMapped | cudaHostAllocPortable));
+  std::memset((void*)qc, 0, sizeof(tci_queue_ctl));
+  qc->idle_us = idle_us;
+  CUDA_TRY(cudaMalloc((void**)&st_dev, sizeof(tci_resident_state)));
+  CUDA_TRY(cudaMemset(st_dev, 0, sizeof(tci_resident_state)));
+  CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&ev0));
+  CUDA_TRY(cudaEventCreate(&ev1));
+  CUDA_TRY(cudaDeviceSynchronize());
+  return 0;
+}
+
+ResidentQueue::~ResidentQueue() {
+  if (running) stop();
+  if (stream) cudaStreamSynchronize(stream);
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (stream) cudaStreamDestroy(stream);
+  if (st_dev) cudaFree(st_dev);
+  if (qc) cudaFreeHost(qc);
+  if (slots) cudaFreeHost(slots);
+}
+
+int ResidentQueue::start() {
+  std::lock_guard<std::mutex> lk(mu);
+  if (running) return 0;
+  std::atomic_ref<int32_t>(qc->stop).store(0, std::memory_order_release);
+  CUDA_TRY(cudaEventRecord(ev0, stream));
+  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, stream));
+  CUDA_TRY(cudaEventRecord(ev1, stream));
+  running = true;
+  ++launches;
+  return 0;
+}
+
+int ResidentQueue::ensure_alive() {
+  std::lock_guard<std::mutex> lk(mu);
+  if (!running) return 0;
+  cudaError_t q = cudaEventQuery(ev1);
+  if (q == cudaErrorNotReady) return 0;
+  if (q != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(q));
+  // every CTA has left on its idle limit: account the launch and start again
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  kernel_ms += ms;
+  CUDA_TRY(cudaEventRecord(ev0, stream));
+  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, stream));
+  CUDA_TRY(cudaEventRecord(ev1, stream));
+  ++launches;
+  return 0;
+}
+
+int ResidentQueue::stop() {
+  std::lock_guard<std::mutex> lk(mu);
+  if (!running) return 0;
+  std::atomic_ref<int32_t>(qc->stop).store(1, std::memory_order_release);
+  cudaError_t e = cudaEventSynchronize(ev1);
+  running = false;
+  std::atomic_ref<int32_t>(qc->stop).store(0, std::memory_order_release);
+  if (e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(e));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  kernel_ms += ms;
+  int32_t err = 0;
+  CUDA_TRY(cudaMemcpy(&err, &st_dev->error, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err) return fail(TCI_ERR_TIMEOUT, "resident kernel: a wait for a task hit its limit");
+  return 0;
+}
+
+int ResidentQueue::publish(const tci_task& t, uint64_t& ticket) {
+  ticket = tail.fetch_add(1, std::memory_order_relaxed);
+  tci_queue_slot& sl = slots[ticket & mask];
+  if (ticket >= nslots) {  // wait for the CTA that took this slot's previous ticket
+    const uint64_t want = ticket - nslots + 1;
+    auto t0 = std::chrono::steady_clock::now();
+    for (long it = 0; std::atomic_ref<uint64_t>(sl.taken).load(std::memory_order_acquire) != want; ++it) {
+      if ((it & 1023) == 1023) {
+        int rc = ensure_alive();
+        if (rc) return rc;
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::seconds(30))
+          return fail(TCI_ERR_TIMEOUT, "resident queue: ring slot not released");
+      }
+      std::this_thread::yield();
+    }
+  }
+  sl.t = t;
+  sl.t.ticket = ticket;
+  std::atomic_ref<uint64_t>(sl.seq).store(ticket + 1, std::memory_order_release);
+  return 0;
+}
+
+// ---------------------------------------------------------------- resident engine
+void Engine::set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scratch_pool) {
+  rq_ = q;
+  hpool_ = host_pool;
+  spool_ = scratch_pool;
+  res_smem_ = tci_resident_smem_bytes();
+}
+
+int Engine::submit() {
+  if (pending_.empty()) return 0;
+  MsTimer timer(stats.host_launch_ms);
+  std::vector<Req*> batch;
+  batch.swap(pending_);
+  std::vector<Waiter> ws;
+  ws.swap(waiters_);
+  for (auto& w : ws) {
+    Flight f;
+    f.w = w;
+    int rc = 0;
+    for (size_t k = w.first; k < w.first + w.count && !rc; ++k) {
+      Req& r = *batch[k];
+      tci_task& t = r.t;
+      size_t we = 0;
+      if (!plan_task(t, res_smem_, we)) {
+        rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
+        break;
+      }
+      // one host record: inputs, then the result record
+      size_t off = 0;
+      const size_t o_params = off;
+      off = a16(off + (size_t)t.nparams * 8);
+      const size_t o_rows = off;
+      off = a16(off + r.rows_bytes);
+      const size_t o_cols = off;
+      off = a16(off + r.cols_bytes);
+      const size_t o_prows = off;
+      off = a16(off + r.prows_bytes);
+      const size_t o_cores = off;
+      off = a16(off + (size_t)r.ncores * sizeof(tci_core_ref));
+      const size_t o_ain = off;
+      if (r.ain_host) off = a16(off + (size_t)t.m * t.n * 8);
+      const size_t o_res = off;
+      r.res_bytes = result_bytes(t);
+      off += r.res_bytes;
+      char* rec = (char*)hpool_->alloc(off);
+      if (!rec) {
+        rc = fail(TCI_ERR_OOM, "pinned host memory for task records");
+        break;
+      }
+      f.hblocks.push_back(rec);
+      if (t.nparams) std::memcpy(rec + o_params, r.params, (size_t)t.nparams * 8);
+      if (r.rows_bytes) std::memcpy(rec + o_rows, r.rows, r.rows_bytes);
+      if (r.cols_bytes) std::memcpy(rec + o_cols, r.cols, r.cols_bytes);
+      if (r.prows_bytes) std::memcpy(rec + o_prows, r.prows, r.prows_bytes);
+      if (r.ncores) std::memcpy(rec + o_cores, r.cores, (size_t)r.ncores * sizeof(tci_core_ref));
+      if (r.ain_host) std::memcpy(rec + o_ain, r.ain_host, (size_t)t.m * t.n * 8);
+      t.params = (int64_t)(uintptr_t)(rec + o_params);
+      t.rows = (int64_t)(uintptr_t)(rec + o_rows);
+      t.cols = (int64_t)(uintptr_t)(rec + o_cols);
+      t.prows = (int64_t)(uintptr_t)(rec + o_prows);
+      t.cores = r.ncores ? (int64_t)(uintptr_t)(rec + o_cores) : 0;
+      t.res = (int64_t)(uintptr_t)(rec + o_res);
+      if (r.ain_host) t.ain = (const double*)(rec + o_ain);
+      r.res = rec + o_res;
+      const size_t lut = t.lutcap0 > 0 ? (size_t)t.lutcap0 + (size_t)std::max(t.lutcap1, 0) : 0;
+      t.work = nullptr;
+      t.lut = nullptr;
+      if (we + lut > 0) {
+        double* d = (double*)spool_->alloc((we + lut) * sizeof(double));
+        if (!d) {
+          rc = fail(TCI_ERR_OOM, "device scratch for a task");
+          break;
+        }
+        f.dblocks.push_back(d);
+        if (!t.smem_mode) t.work = d;
+        if (lut) t.lut = d + we;
+      }
+      t.cost = task_cost(t);
+      stats.h2d_bytes += (int64_t)o_res;
+      stats.d2h_bytes += (int64_t)r.res_bytes;
+      rc = rq_->publish(t, r.ticket);
+      if (!rc) f.reqs.push_back(&r);
+    }
+    if (rc) {
+      if (!f.reqs.empty()) {  // some tasks are out: keep the blocks until they finish, then fail
+        f.w.op->status = rc;
+        flights_.push_back(std::move(f));
+        continue;
+      }
+      for (void* p : f.hblocks) hpool_->free(p);
+      for (void* p : f.dblocks) spool_->free(p);
+      w.op->status = rc;
+      w.h.resume();  // whatever it enqueues is submitted on the next call
+      continue;
+    }
+    flights_.push_back(std::move(f));
+  }
+  return 0;
+}
+
+void Engine::abandon() {
+  for (auto& f : flights_) {
+    for (void* p : f.hblocks) hpool_->free(p);
+    for (void* p : f.dblocks) spool_->free(p);
+  }
+  flights_.clear();
+  pending_.clear();
+  waiters_.clear();
+}
+
+int Engine::poll(bool& progressed) {
+  MsTimer timer(stats.host_resume_ms);
+  for (size_t i = 0; i < flights_.size();) {
+    Flight& f = flights_[i];
+    bool done = true;
+    for (Req* r : f.reqs) {
+      uint64_t* d = const_cast<uint64_t*>(&r->head()->done);
+      if (std::atomic_ref<uint64_t>(*d).load(std::memory_order_acquire) != r->ticket + 1) {
+        done = false;
+        break;
+      }
+    }
+    if (!done) {
+      ++i;
+      continue;
+    }
+    Flight g = std::move(f);
+    if (i + 1 != flights_.size()) flights_[i] = std::move(flights_.back());
+    flights_.pop_back();
+    stats.tasks += (int64_t)g.reqs.size();
+    for (Req* r : g.reqs) account(*r, r->t.smem_mode);
+    const int status = g.w.op->status;  // nonzero: a task of this op could not be submitted
+    g.w.op->status = status;
+    g.w.h.resume();  // the Req records of this op may be gone afterwards
+    for (void* p : g.hblocks) hpool_->free(p);
+    for (void* p : g.dblocks) spool_->free(p);
+    progressed = true;
   }
   return 0;
 }

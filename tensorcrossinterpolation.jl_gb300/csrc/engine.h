@@ -4,10 +4,13 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <coroutine>
 #include <cstdio>
 #include <cstdint>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/tci_gb300.h"
@@ -105,6 +108,7 @@ struct Req {
   const double* ain_host = nullptr;  // packed into the upload blob
   const char* res = nullptr;         // host copy of the result record after the step
   size_t res_bytes = 0;
+  uint64_t ticket = 0;               // resident mode: ring ticket of the task
   const tci_result_head* head() const { return (const tci_result_head*)res; }
   const int32_t* rowperm() const { return (const int32_t*)(res + sizeof(tci_result_head)); }
   const int32_t* colperm() const {
@@ -118,6 +122,65 @@ struct Req {
 };
 
 class Engine;
+
+// Power-of-two size-class pool.  Small blocks are carved from large slabs;
+// every block is kept for reuse until the pool is destroyed, so allocation in
+// steady state makes no CUDA call (a CUDA allocation while the resident kernel
+// runs would serialise the device).  Device pools back the allocations with
+// stream-ordered cudaMallocAsync on a private stream; host pools with mapped
+// pinned memory that the device reads and writes directly.
+class BlockPool {
+ public:
+  enum Kind { DEVICE, HOST };
+  BlockPool(Kind kind, int device, bool locked);
+  ~BlockPool();
+  void* alloc(size_t bytes);  // nullptr when the backing allocation fails
+  void free(void* p);
+  // Back the next small-block allocations now (a pinned allocation while the
+  // resident kernel runs would serialise the device).
+  bool reserve_slab();
+  size_t reserved() const { return reserved_; }
+
+ private:
+  static constexpr int MIN_SHIFT = 8;      // 256 B
+  static constexpr int SLAB_SHIFT = 26;    // 64 MiB slabs
+  static constexpr int CARVE_MAX = 22;     // blocks up to 4 MiB come from slabs
+  void* backing(size_t bytes);
+  Kind kind_;
+  int device_;
+  bool locked_;
+  std::mutex mu_;
+  cudaStream_t side_ = nullptr;
+  std::vector<void*> owned_;
+  std::vector<std::vector<void*>> free_;
+  std::unordered_map<void*, int> cls_;
+  char* slab_ = nullptr;
+  size_t slab_left_ = 0;
+  size_t reserved_ = 0;
+};
+
+// The ring of the resident kernel, shared by the engines of a context.
+struct ResidentQueue {
+  int device = 0;
+  int grid = 0;
+  uint32_t nslots = 0, mask = 0;
+  tci_queue_slot* slots = nullptr;       // mapped pinned host memory
+  tci_queue_ctl* qc = nullptr;           // mapped pinned host memory
+  tci_resident_state* st_dev = nullptr;   // device memory
+  std::atomic<uint64_t> tail{0};
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::mutex mu;
+  bool running = false;
+  double kernel_ms = 0;
+  int64_t launches = 0;
+  int init(int device, int num_sms, int idle_us);
+  ~ResidentQueue();
+  int start();        // launch the kernel unless it is running
+  int ensure_alive(); // relaunch it if every CTA has left (idle limit)
+  int stop();         // ask the CTAs to leave once the ring is drained; wait
+  int publish(const tci_task& t, uint64_t& ticket);
+};
 
 struct GpuOp {
   Engine* eng;
@@ -183,7 +246,20 @@ class Engine {
   // Drive a single coroutine (and any others already queued) to completion.
   int run(CoTask& t);
 
-  // Device memory for site tensors (stream-ordered pool).
+  // Resident mode: tasks go to the context's ring as soon as they are queued
+  // (submit) and each solve resumes as soon as its own tasks are done (poll),
+  // with no batch boundary.  The pools must outlive the engine.
+  void set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scratch_pool);
+  bool resident() const { return rq_ != nullptr; }
+  int submit();
+  int poll(bool& progressed);
+  bool has_flights() const { return !flights_.empty(); }
+  // Drop every queued and finished-but-unresumed task (after a fatal error,
+  // with the device idle); their solves are not resumed.
+  void abandon();
+  void set_device_pool(BlockPool* p) { dpool_ = p; }
+
+  // Device memory for site tensors (the context's device pool).
   double* alloc_core(size_t elems);
   void free_core(double* p);
   void release_cores(Solve& s);
@@ -207,7 +283,20 @@ class Engine {
     size_t first, count;
   };
   int ensure(size_t blob, size_t res, size_t work);
+  void account(const Req& r, int smem_mode);
   int device_ = 0;
+  // resident mode
+  struct Flight {
+    Waiter w;
+    std::vector<Req*> reqs;
+    std::vector<void*> hblocks, dblocks;
+  };
+  ResidentQueue* rq_ = nullptr;
+  BlockPool* hpool_ = nullptr;
+  BlockPool* spool_ = nullptr;  // device scratch of this engine's tasks (this thread only)
+  BlockPool* dpool_ = nullptr;
+  size_t res_smem_ = 0;
+  std::vector<Flight> flights_;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   std::vector<Req*> pending_;

@@ -23,6 +23,7 @@
 // (matrixlu.jl:16-31).  The comparison of v*v is skipped for elements whose |v|
 // is more than 16 ulps below the running maximum, where v*v is provably smaller.
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "tci_functions.h"
@@ -224,6 +225,13 @@ __device__ int block_or(int v, Ctl& ctl) {
 
 __device__ __forceinline__ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// base + offset as integer arithmetic: in resident mode the base is zero and
+// the offsets are absolute addresses.
+__device__ __forceinline__ const char* at(const char* base, int64_t off) {
+  return (const char*)((uintptr_t)base + (uintptr_t)off);
+}
+__device__ __forceinline__ char* atw(char* base, int64_t off) { return (char*)((uintptr_t)base + (uintptr_t)off); }
+
 // Row / column partial sums of the registered f (tci_functions.h).
 __device__ void compute_states(int fid, const double* params, const uint8_t* idx, int count, int len,
                                int site0, double* s0, double* s1) {
@@ -319,7 +327,7 @@ struct ResPtrs {
 };
 __device__ ResPtrs res_ptrs(char* resb, const tci_task& T) {
   ResPtrs p;
-  char* base = resb + T.res;
+  char* base = atw(resb, T.res);
   p.head = (tci_result_head*)base;
   const int kcap = T.kcap;
   size_t off = sizeof(tci_result_head);
@@ -575,13 +583,13 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
       }
     }
   } else {
-    const double* prm = (const double*)(blob + T.params);
+    const double* prm = (const double*)at(blob, T.params);
     double* rs0 = (double*)cur.take((size_t)m * 8);
     double* rs1 = (double*)cur.take((size_t)m * 8);
     double* cs0 = (double*)cur.take((size_t)n * 8);
     double* cs1 = (double*)cur.take((size_t)n * 8);
-    compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
-    compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
+    compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
+    compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
     __syncthreads();
     const double* rg0[1] = {rs0};
     const double* rg1[1] = {rs1};
@@ -653,7 +661,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
                           size_t smem_bytes) {
   const int r = T.r, m = T.m, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   ResPtrs rp = res_ptrs(resb, T);
-  const double* prm = (const double*)(blob + T.params);
+  const double* prm = (const double*)at(blob, T.params);
   SmemCursor cur{smem};
   double* P = T.smem_mode ? (double*)cur.take((size_t)r * r * 8) : T.work;
   int* rowperm = (int*)cur.take((size_t)r * 4);
@@ -664,9 +672,9 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   double* cs1 = (double*)cur.take((size_t)r * 8);
   double* rs0 = (double*)cur.take((size_t)m * 8);
   double* rs1 = (double*)cur.take((size_t)m * 8);
-  compute_states(T.fid, prm, (const uint8_t*)(blob + T.prows), r, T.nl, 0, ps0, ps1);
-  compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), r, T.nr, T.nl, cs0, cs1);
-  compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
+  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.prows), r, T.nl, 0, ps0, ps1);
+  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), r, T.nr, T.nl, cs0, cs1);
+  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
   for (int i = tid; i < r; i += NT) {
     rowperm[i] = i;
     colperm[i] = i;
@@ -762,14 +770,14 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
 // ---------------------------------------------------------------- CORE task
 __device__ void task_core(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
   const int m = T.m, n = T.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double* prm = (const double*)(blob + T.params);
+  const double* prm = (const double*)at(blob, T.params);
   SmemCursor cur{smem};
   double* rs0 = (double*)cur.take((size_t)m * 8);
   double* rs1 = (double*)cur.take((size_t)m * 8);
   double* cs0 = (double*)cur.take((size_t)n * 8);
   double* cs1 = (double*)cur.take((size_t)n * 8);
-  compute_states(T.fid, prm, (const uint8_t*)(blob + T.rows), m, T.nl, 0, rs0, rs1);
-  compute_states(T.fid, prm, (const uint8_t*)(blob + T.cols), n, T.nr, T.nl, cs0, cs1);
+  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
+  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
   __syncthreads();
   const double* rg0[1] = {rs0};
   const double* rg1[1] = {rs1};
@@ -785,7 +793,7 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
     }
   unsigned long long mxall = block_max_u64(mx, ctl);
   if (tid == 0) {
-    tci_result_head* h = (tci_result_head*)(resb + T.res);
+    tci_result_head* h = (tci_result_head*)(atw(resb, T.res));
     h->status = 0;
     h->npivot = 0;
     h->error = 0.0;
@@ -802,9 +810,9 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
 // separate multiply and add, as the oracle's loop.
 __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
   const int np = T.m, L = T.L, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double* prm = (const double*)(blob + T.params);
-  const uint8_t* pts = (const uint8_t*)(blob + T.rows);
-  char* base = resb + T.res;
+  const double* prm = (const double*)at(blob, T.params);
+  const uint8_t* pts = (const uint8_t*)at(blob, T.rows);
+  char* base = atw(resb, T.res);
   double* fout = (double*)(base + sizeof(tci_result_head));
   double* tout = fout + np;
   for (int p = tid; p < np; p += NT) {
@@ -813,7 +821,7 @@ __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char*
     fout[p] = tci_f_finish(T.fid, prm, T.nparams, a0, a1);
   }
   if (T.cores) {
-    const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
+    const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
     const int rmax = T.r;
     double* va = (double*)smem + (size_t)warp * 2 * rmax;
     double* vb = va + rmax;
@@ -859,10 +867,10 @@ __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char*
 // order with separate multiply and add (the oracle uses the same order).
 __device__ void task_search(const tci_task& T, const char* blob, char* resb, char* smem) {
   const int L = T.L, tid = threadIdx.x;
-  const double* prm = (const double*)(blob + T.params);
-  const uint8_t* st = (const uint8_t*)(blob + T.rows);
-  const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
-  char* base = resb + T.res;
+  const double* prm = (const double*)at(blob, T.params);
+  const uint8_t* st = (const uint8_t*)at(blob, T.rows);
+  const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
+  char* base = atw(resb, T.res);
   double* fout = (double*)(base + sizeof(tci_result_head));
   double* tout = fout + T.m;
   // environment offsets: Le_p has r0(p) entries, Re_p has r1(p) entries
@@ -952,7 +960,7 @@ __device__ void task_search(const tci_task& T, const char* blob, char* resb, cha
 // of core b), left to right; one thread per output bond index.
 __device__ void task_sum(const tci_task& T, const char* blob, char* resb, char* smem) {
   const int L = T.L, tid = threadIdx.x;
-  const tci_core_ref* cr = (const tci_core_ref*)(blob + T.cores);
+  const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
   double* v = (double*)smem;
   double* w = v + T.r;
   if (tid == 0) v[0] = 1.0;
@@ -974,12 +982,25 @@ __device__ void task_sum(const tci_task& T, const char* blob, char* resb, char* 
     w = t;
   }
   if (tid == 0) {
-    tci_result_head* h = (tci_result_head*)(resb + T.res);
+    tci_result_head* h = (tci_result_head*)(atw(resb, T.res));
     h->status = 0;
     h->npivot = 0;
     h->error = v[0];
   }
   __syncthreads();
+}
+
+__device__ void run_task(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl,
+                         size_t smem_bytes) {
+  switch (T.kind) {
+    case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl); break;
+    case TCI_TASK_SITE: task_site(T, blob, resb, smem, ctl, smem_bytes); break;
+    case TCI_TASK_CORE: task_core(T, blob, resb, smem, ctl); break;
+    case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
+    case TCI_TASK_SUM: task_sum(T, blob, resb, smem); break;
+    case TCI_TASK_SEARCH: task_search(T, blob, resb, smem); break;
+    default: break;
+  }
 }
 
 __global__ void __launch_bounds__(NT, 1)
@@ -996,16 +1017,172 @@ __global__ void __launch_bounds__(NT, 1)
     if (ti >= ntasks) break;
     const tci_task T = tasks[order[ti]];
     const long long t0 = clock64();
-    switch (T.kind) {
-      case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl); break;
-      case TCI_TASK_SITE: task_site(T, blob, resb, smem, ctl, smem_bytes); break;
-      case TCI_TASK_CORE: task_core(T, blob, resb, smem, ctl); break;
-      case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
-      case TCI_TASK_SUM: task_sum(T, blob, resb, smem); break;
-      case TCI_TASK_SEARCH: task_search(T, blob, resb, smem); break;
-      default: break;
+    run_task(T, blob, resb, smem, ctl, smem_bytes);
+    if (threadIdx.x == 0) ((tci_result_head*)(atw(resb, T.res)))->cycles = clock64() - t0;
+  }
+}
+
+// ------------------------------------------------------------ resident kernel
+// System-scope acquire / release on mapped host memory.
+__device__ __forceinline__ uint64_t ld_acquire_sys(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_sys(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.sys.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint64_t ld_acquire_gpu(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ int ld_acquire_gpu_s32(const int32_t* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_gpu(uint64_t* p, uint64_t v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void st_release_gpu_s32(int32_t* p, int v) {
+  asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr int RES_MAX_PARAMS = 64;                          // params copied to shared memory
+constexpr uint64_t RES_WAIT_LIMIT_NS = 60ull * 1000000000ull;  // a worker's longest wait for a ticket
+constexpr long long RES_MAX_POLLS = 1LL << 31;              // and its poll count
+constexpr int TASK_WORDS = (int)(sizeof(tci_task) / 8);
+static_assert(sizeof(tci_task) % 8 == 0, "task record is a whole number of words");
+
+// Warp 0 of CTA 0: move published host-ring descriptors, 32 at a time, into
+// the device ring (in ticket order, while the device ring has room), mark the
+// host slots free, publish the device tickets.  Leaves -- and tells the
+// workers -- when the host asks to stop and nothing published is left, or
+// after qc->idle_us with nothing published.
+__device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmask, tci_resident_state* st,
+                                  tci_queue_ctl* qc) {
+  const int lane = threadIdx.x;
+  unsigned long long pos = *(volatile unsigned long long*)&st->host_pos;
+  unsigned long long k = 0;
+  const uint64_t idle_ns = (uint64_t)(*(volatile int32_t*)&qc->idle_us) * 1000ull;
+  uint64_t t_idle = global_ns();
+  unsigned sleep_ns = 32;
+  for (;;) {
+    const unsigned long long hp = pos + lane, dk = k + lane;
+    tci_queue_slot* h = &hs[hp & hmask];
+    tci_queue_slot* d = &st->ring[dk & (TCI_DRING - 1)];
+    const bool pub = ld_acquire_sys(&h->seq) == hp + 1;
+    const bool room = dk < TCI_DRING || ld_acquire_gpu(&d->taken) == dk - TCI_DRING + 1;
+    const unsigned okm = __ballot_sync(FULL, pub && room);
+    const int p = okm == FULL ? 32 : __ffs(~okm) - 1;
+    if (p > 0) {
+      if (lane < p) {
+        const volatile uint64_t* src = (const volatile uint64_t*)&h->t;
+        uint64_t* dst = (uint64_t*)&d->t;
+        for (int w = 0; w < TASK_WORDS; ++w) dst[w] = src[w];
+        st_release_sys(&h->taken, hp + 1);
+        st_release_gpu(&d->seq, dk + 1);
+      }
+      pos += p;
+      k += p;
+      if (lane == 0) *(volatile unsigned long long*)&st->host_pos = pos;
+      t_idle = global_ns();
+      sleep_ns = 32;
+      continue;
     }
-    if (threadIdx.x == 0) ((tci_result_head*)(resb + T.res))->cycles = clock64() - t0;
+    int leave = 0;
+    if (lane == 0) {
+      const uint64_t waited = global_ns() - t_idle;
+      if (!pub)  // nothing published: the host is done, or quiet for too long
+        leave = (*(volatile int32_t*)&qc->stop != 0) || waited > idle_ns;
+      else       // published but no room: the workers must free slots; they may have failed
+        leave = (*(volatile int32_t*)&st->error != 0) || waited > RES_WAIT_LIMIT_NS;
+    }
+    if (__shfl_sync(FULL, leave, 0)) break;
+    __nanosleep(sleep_ns);
+    sleep_ns = sleep_ns < 512 ? sleep_ns * 2 : 512;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    *(volatile unsigned long long*)&st->count = k;
+    st_release_gpu_s32(&st->stop, 1);
+  }
+}
+
+// Persistent kernel of the resident mode (cooperative launch, one CTA per SM).
+// CTA 0 hosts the dispatcher; every other CTA claims the next device ticket
+// with one atomic, waits until it is dispatched (or the dispatcher has left:
+// tickets past the last dispatched one are never used), runs the task and
+// publishes the result record to the host.
+__global__ void __launch_bounds__(NT, 1)
+    tci_resident_kernel(tci_queue_slot* __restrict__ hslots, uint32_t hmask, tci_resident_state* st,
+                        tci_queue_ctl* qc, size_t smem_bytes) {
+  if (blockIdx.x == 0) {
+    if (threadIdx.x < 32) resident_dispatch(hslots, hmask, st, qc);
+    return;
+  }
+  extern __shared__ __align__(16) char smem[];
+  __shared__ Ctl ctl;
+  __shared__ __align__(16) tci_task Ts;
+  __shared__ double s_params[RES_MAX_PARAMS];
+  __shared__ long long s_ticket;
+  const int tid = threadIdx.x;
+  for (;;) {
+    if (tid == 0) {
+      long long got = -1;
+      const unsigned long long t = atomicAdd(&st->head, 1ull);
+      tci_queue_slot* d = &st->ring[t & (TCI_DRING - 1)];
+      const uint64_t t_begin = global_ns();
+      unsigned sleep_ns = 32;
+      for (long long it = 0;; ++it) {
+        if (ld_acquire_gpu(&d->seq) == t + 1) {
+          got = (long long)t;
+          break;
+        }
+        if (ld_acquire_gpu_s32(&st->stop)) {  // every dispatch happened before the stop flag
+          if (ld_acquire_gpu(&d->seq) == t + 1) got = (long long)t;
+          break;
+        }
+        if (it >= RES_MAX_POLLS || global_ns() - t_begin > RES_WAIT_LIMIT_NS) {
+          atomicExch(&st->error, 1);
+          break;
+        }
+        if (*(volatile int32_t*)&st->error) break;  // another wait has failed: leave too
+        __nanosleep(sleep_ns);
+        sleep_ns = sleep_ns < 256 ? sleep_ns * 2 : 256;
+      }
+      s_ticket = got;
+    }
+    __syncthreads();
+    const long long ticket = s_ticket;
+    if (ticket < 0) break;
+    tci_queue_slot* d = &st->ring[(unsigned long long)ticket & (TCI_DRING - 1)];
+    if (tid < TASK_WORDS) ((uint64_t*)&Ts)[tid] = ((const volatile uint64_t*)&d->t)[tid];
+    __syncthreads();
+    if (tid == 0) st_release_gpu(&d->taken, (uint64_t)ticket + 1);
+    if (Ts.nparams <= RES_MAX_PARAMS) {  // f parameters are read per element: keep them on chip
+      const double* src = (const double*)(uintptr_t)Ts.params;
+      for (int k = tid; k < Ts.nparams; k += NT) s_params[k] = src[k];
+    }
+    __syncthreads();
+    if (tid == 0 && Ts.nparams <= RES_MAX_PARAMS) Ts.params = (int64_t)(uintptr_t)s_params;
+    __syncthreads();
+    const long long t0 = clock64();
+    run_task(Ts, nullptr, nullptr, smem, ctl, smem_bytes);
+    __syncthreads();
+    if (tid == 0) {
+      tci_result_head* h = (tci_result_head*)(uintptr_t)Ts.res;
+      h->cycles = clock64() - t0;
+      __threadfence_system();
+      st_release_sys(&h->done, Ts.ticket + 1);
+    }
   }
 }
 
@@ -1014,9 +1191,29 @@ __global__ void __launch_bounds__(NT, 1)
 // Shared-memory budget of one CTA of the step kernel.
 size_t tci_step_smem_bytes() { return 227 * 1024 - 1024; }
 
+// Dynamic shared memory of the resident kernel (its static shared memory holds
+// the task record and the f parameters as well).
+size_t tci_resident_smem_bytes() { return tci_step_smem_bytes() - 2048; }
+
 cudaError_t tci_step_configure() {
-  return cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tci_step_smem_bytes());
+  cudaError_t e = cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tci_step_smem_bytes());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(tci_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tci_resident_smem_bytes());
+}
+
+// Launch the resident kernel: one CTA per SM, all resident at once
+// (cooperative launch), after clearing the per-launch part of its state.
+// slots/qc are mapped pinned host memory, st device memory.
+cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
+                                int grid, cudaStream_t stream) {
+  const size_t off = offsetof(tci_resident_state, count);
+  cudaError_t e = cudaMemsetAsync((char*)st + off, 0, sizeof(tci_resident_state) - off, stream);
+  if (e != cudaSuccess) return e;
+  size_t smem = tci_resident_smem_bytes();
+  void* args[] = {(void*)&slots, (void*)&mask, (void*)&st, (void*)&qc, (void*)&smem};
+  return cudaLaunchCooperativeKernel((const void*)tci_resident_kernel, dim3(grid), dim3(NT), args, smem, stream);
 }
 
 // Launch one step.  counter must be zero (the launcher clears it on the stream).

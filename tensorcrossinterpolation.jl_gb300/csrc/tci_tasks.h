@@ -1,10 +1,18 @@
 // Task records shared by the host engine and the step kernel.
 //
-// One engine step uploads a blob [tci_task array | params | uint8 index lists |
-// core tables | input matrices] and one result area.  The step kernel pulls
-// tasks from an atomic queue, one CTA per task, and writes one result record
-// per task.  All offsets are byte offsets from the start of the blob (inputs)
-// or of the result area (outputs).
+// Batch mode: one engine step uploads a blob [tci_task array | params | uint8
+// index lists | core tables | input matrices] and one result area.  The step
+// kernel pulls tasks from an atomic queue, one CTA per task, and writes one
+// result record per task.  All offsets are byte offsets from the start of the
+// blob (inputs) or of the result area (outputs).
+//
+// Resident mode: host threads publish tasks into a ring of tci_queue_slot in
+// mapped pinned host memory while the resident kernel runs.  One warp of the
+// kernel (the dispatcher) moves published descriptors into a ring in device
+// memory; the other CTAs claim device tickets with one atomic each, read the
+// task inputs from host memory and write the result record there, then set the
+// record's `done` word.  The offsets are then absolute addresses (the base
+// pointers passed to the kernel are zero).
 #pragma once
 #include <stdint.h>
 
@@ -53,6 +61,7 @@ typedef struct tci_task {
   int32_t kcap;                // pivot capacity of the result record
   double* lut;                 // scratch for tabulated f parts (lutcap0 + lutcap1 doubles)
   int32_t lutcap0, lutcap1;    // table capacities (0: evaluate f directly)
+  uint64_t ticket;             // resident mode: host-ring ticket (the record's done word = ticket + 1)
 } tci_task;
 
 // Result record: fixed header followed by per-task arrays.
@@ -62,6 +71,7 @@ typedef struct tci_result_head {
   double maxabs;      // max |value| over the filled matrix (updatemaxsample!)
   int32_t maxabs_nan, lut_used;
   int64_t cycles;     // SM clock cycles the CTA spent on the task
+  uint64_t done;      // resident mode: ticket + 1 once the record is complete
 } tci_result_head;
 // RRLU/SITE: head, int32 rowperm[kcap], int32 colperm[kcap], double diag[kcap]
 //            (each array padded to 8 bytes)
@@ -69,5 +79,37 @@ typedef struct tci_result_head {
 // SEARCH: head, double f[m], double tt[m], m = sum of the local dimensions; item
 //         (p, v) (site-major) is the start point with site p set to v
 // SUM : head with the sum in `error`
+
+// One ring slot of the resident queue.  seq = ticket + 1 once the host has
+// written `t` for that ticket; taken = ticket + 1 once a CTA has copied `t` out
+// (the slot may then be reused for ticket + ring size).
+typedef struct tci_queue_slot {
+  tci_task t;
+  uint64_t seq;
+  uint64_t taken;
+} tci_queue_slot;
+
+// Control words of the resident kernel (mapped pinned host memory).
+typedef struct tci_queue_ctl {
+  int32_t stop;        // host sets 1: the kernel leaves once every published task is dispatched
+  int32_t idle_us;     // the kernel leaves after this long with nothing published
+  int32_t pad[2];
+} tci_queue_ctl;
+
+// Device-memory state of the resident kernel.  host_pos persists across
+// launches; everything from `count` on is cleared before every launch.
+#define TCI_DRING 4096
+typedef struct tci_resident_state {
+  unsigned long long host_pos;  // next host-ring ticket to dispatch
+  unsigned long long pad0[15];
+  unsigned long long count;     // device tickets dispatched in this launch
+  unsigned long long pad1[15];
+  unsigned long long head;      // device tickets claimed in this launch
+  unsigned long long pad2[15];
+  int32_t stop;                 // dispatcher has left: no ticket beyond `count` will come
+  int32_t error;                // a worker's wait hit its limit
+  int32_t pad3[30];
+  tci_queue_slot ring[TCI_DRING];
+} tci_resident_state;
 
 #define TCI_STEP_THREADS 512

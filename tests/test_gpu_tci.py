@@ -190,3 +190,50 @@ def test_bulk_export_matches_per_core(T):
     for tci, tt in zip(res, tts):
         for b in range(1, len(tci) + 1):
             assert np.array_equal(tt.sitetensors[b - 1], tci.sitetensor(b))
+
+
+def _served_specs(T, seed, n, maxbonddim):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for _ in range(n):
+        L = int(rng.integers(4, 10))
+        d = int(rng.integers(2, 10))
+        specs.append((T.DeviceFunction("served", _served(rng, L, d)), [d] * L,
+                      dict(tolerance=10 ** rng.uniform(-10, -6), maxbonddim=maxbonddim)))
+    return specs
+
+
+def test_resident_equals_batched_launches(T, monkeypatch):
+    """The resident kernel (ring in pinned memory) and one launch per engine step
+    give identical solves."""
+    specs = _served_specs(T, 21, 24, 64)
+    monkeypatch.setenv("TCI_RESIDENT", "0")
+    ctx_b = T.Context(0)
+    monkeypatch.setenv("TCI_RESIDENT", "1")
+    ctx_r = T.Context(0)
+    a = T.crossinterpolate2_batched(specs, max_live=8, ctx=ctx_b)
+    b = T.crossinterpolate2_batched(specs, max_live=8, ctx=ctx_r)
+    assert ctx_r.stats()["tasks"] > 0
+    for ta, tb, (_, dims, _) in zip(a, b, specs):
+        assert list(ta.linkdims()) == list(tb.linkdims())
+        for s in range(1, len(dims) + 1):
+            assert np.array_equal(ta.sets(s)[0], tb.sets(s)[0])
+            assert np.array_equal(ta.sets(s)[1], tb.sets(s)[1])
+            assert np.array_equal(ta.sitetensor(s), tb.sitetensor(s))
+
+
+def test_resident_relaunch_after_idle(T, monkeypatch):
+    """With a short idle limit the resident kernel leaves between sparse
+    arrivals and is launched again; every request is still served."""
+    monkeypatch.setenv("TCI_RESIDENT", "1")
+    monkeypatch.setenv("TCI_RESIDENT_IDLE_US", "300")
+    ctx = T.Context(0)
+    specs = _served_specs(T, 22, 8, 32)
+    arrival = np.arange(len(specs)) * 0.02  # 20 ms apart: longer than the idle limit
+    lat, rank, wall = T.serve(specs, arrival, max_live=4, ctx=ctx)
+    assert np.all(lat > 0) and np.all(rank >= 1)
+    assert ctx.stats()["launches"] >= 2
+    for i in [0, 5]:
+        f, dims, kw = specs[i]
+        ta, _, _ = T.crossinterpolate2(float, f, dims, ctx=ctx, **kw)
+        assert ta.rank() == rank[i]
