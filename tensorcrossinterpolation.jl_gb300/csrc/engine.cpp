@@ -264,6 +264,9 @@ int Engine::ensure(size_t blob, size_t res, size_t work) {
 static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
   const size_t m = (size_t)t.m, n = (size_t)t.n;
   work_elems = 0;
+  // argmax keys pack (column << 16) | row
+  if ((t.kind == TCI_TASK_RRLU && (m > 65535 || n > 65535)) || (t.kind == TCI_TASK_SITE && t.r > 65535))
+    return false;
   switch (t.kind) {
     case TCI_TASK_RRLU: {
       size_t rest = a16(m * 4) + a16(n * 4);

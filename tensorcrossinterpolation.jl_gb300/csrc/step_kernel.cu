@@ -29,6 +29,11 @@
 #include "tci_functions.h"
 #include "tci_tasks.h"
 
+// Optional per-phase timing hook (defined by an instrumented build; no-op here).
+#ifndef TCI_PHASE
+#define TCI_PHASE(id) ((void)0)
+#endif
+
 namespace {
 
 constexpr int NT = TCI_STEP_THREADS;
@@ -40,12 +45,13 @@ constexpr uint64_t SQ_BIG = (uint64_t)(1023 + 500) << 52;    // above: squares m
 
 struct Ctl {
   int task;
-  int r, c, K, stop, kmax;
+  int r, c, K, stop, kmax, need_exact;
   int status;
   double piv, maxerror, err;
   double red_s[NW + 1];
   int red_k[NW + 1];
   unsigned long long red_u[NW + 1];
+  unsigned long long red_b[NW + 1];
   double red4[4][NW + 1];
 };
 
@@ -64,34 +70,69 @@ __device__ __forceinline__ uint64_t abs_bits(double v) {
   return ((uint64_t)(hi & 0x7fffffffu) << 32) | (uint64_t)lo;
 }
 
-// Running argmax of abs2 with first-in-column-major tie breaking.
-// The argmax runs in two passes so that the FP64 pipe only sees the update:
-// while updating, each thread keeps the largest |v| bit pattern (integer ops,
-// NaN excluded); after a block-wide max M*, a read-only pass squares just the
-// elements whose |v| is within 16 ulps of M* (where v*v can tie with M*^2) and
-// picks the largest square, ties to the smallest column-major key.  Below
-// 2^-500 or above 2^500 squares can underflow or overflow, so there every
-// element is squared.
-struct AbsMax {
-  uint64_t M;
-  __device__ __forceinline__ void init() { M = 0; }
-  __device__ __forceinline__ void push(double v) {
+// Argmax of abs2 with first-in-column-major tie breaking, without squaring on
+// the FP64 pipe in the common case: while updating, each thread tracks the
+// largest |v| bit pattern, its first key and the next smaller pattern (integer
+// ops, NaN excluded); one block reduction gives the winner unless another
+// element lies within 16 ulps of the largest |v| (where v*v can tie with the
+// largest square) or the magnitude is below 2^-500 or above 2^500 (squares can
+// underflow or overflow).  Then a read-only pass squares the elements near the
+// maximum and picks the largest square, ties to the smallest key.
+// Element keys are (column << 16) | row: ordered like the column-major position
+// (matrices have at most 65535 rows and columns).
+__device__ __forceinline__ uint32_t pack_key(int i, int j) { return ((uint32_t)j << 16) | (uint32_t)i; }
+
+// One thread's running argmax of |v| in key order, integer pipe only: A = the
+// largest |v| bit pattern + 1, k = its first key, B = the largest bit pattern
+// + 1 below A (0 = none).  NaN never wins (the reference's scan starts from
+// typemin and compares with '>').
+struct ArgTrack {
+  uint64_t A, B;
+  uint32_t k;
+  __device__ __forceinline__ void init() {
+    A = B = 0;
+    k = 0xffffffffu;
+  }
+  __device__ __forceinline__ void push(double v, uint32_t key) {
     uint64_t b = abs_bits(v);
-    if (b <= NAN_FLOOR && b > M) M = b;
+    if (b > NAN_FLOOR) return;
+    b += 1;
+    if (b > A) {
+      B = A;
+      A = b;
+      k = key;
+    } else if (b < A && b > B) {
+      B = b;
+    }
   }
 };
-
-struct ArgBest {
-  double bs;
-  int key;
-  __device__ __forceinline__ void init() {
-    bs = -1.0;
-    key = 0x7fffffff;
+__device__ __forceinline__ void track_combine(uint64_t& A, uint32_t& k, uint64_t& B, uint64_t A2, uint32_t k2,
+                                              uint64_t B2) {
+  if (A2 > A) {
+    B = B2 > A ? B2 : A;
+    A = A2;
+    k = k2;
+  } else if (A2 == A) {
+    B = B2 > B ? B2 : B;
+    k = k2 < k ? k2 : k;
+  } else if (A2 > B) {
+    B = A2;
   }
-  __device__ __forceinline__ void consider(double v, int k) {
-    double s = __dmul_rn(v, v);
-    if (s > bs || (s == bs && k < key)) {
-      bs = s;
+}
+
+// Exact candidate of the second pass: abs2 = v*v (never NaN here, >= +0), so
+// its bit pattern orders like its value; ties go to the smaller key.
+struct ArgBest {
+  uint64_t s;  // abs2 bits + 1, 0 = none
+  uint32_t key;
+  __device__ __forceinline__ void init() {
+    s = 0;
+    key = 0xffffffffu;
+  }
+  __device__ __forceinline__ void consider(double v, uint32_t k) {
+    const uint64_t q = (uint64_t)__double_as_longlong(__dmul_rn(v, v)) + 1;
+    if (q > s || (q == s && k < key)) {
+      s = q;
       key = k;
     }
   }
@@ -100,46 +141,45 @@ __device__ __forceinline__ bool near_max(uint64_t b, uint64_t Mstar) {
   return b <= NAN_FLOOR && (b + 16 >= Mstar || Mstar < SQ_SMALL || Mstar >= SQ_BIG);
 }
 
-__device__ __forceinline__ void arg_combine(double& bs, int& key, double obs, int okey) {
-  if (obs > bs || (obs == bs && okey < key)) {
-    bs = obs;
-    key = okey;
-  }
-}
-
-// Block-wide argmax; every thread gets the result.  Ends with a barrier.
-__device__ void block_argmax(const ArgBest& a, Ctl& ctl, double& out_s, int& out_key) {
+// Block-wide exact argmax; every thread gets (abs2 bits + 1, key).  Ends with a barrier.
+__device__ void block_argmax(const ArgBest& a, Ctl& ctl, uint64_t& out_s, uint32_t& out_key) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  double bs = a.bs;
-  int key = a.key;
+  uint64_t s = a.s;
+  uint32_t key = a.key;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    double obs = __shfl_down_sync(FULL, bs, off);
-    int okey = __shfl_down_sync(FULL, key, off);
-    arg_combine(bs, key, obs, okey);
+    const uint64_t os = __shfl_down_sync(FULL, s, off);
+    const uint32_t ok = __shfl_down_sync(FULL, key, off);
+    if (os > s || (os == s && ok < key)) {
+      s = os;
+      key = ok;
+    }
   }
   if (lane == 0) {
-    ctl.red_s[warp] = bs;
-    ctl.red_k[warp] = key;
+    ctl.red_u[warp] = s;
+    ctl.red_k[warp] = (int)key;
   }
   __syncthreads();
   if (warp == 0) {
-    bs = lane < NW ? ctl.red_s[lane] : -1.0;
-    key = lane < NW ? ctl.red_k[lane] : 0x7fffffff;
+    s = lane < NW ? ctl.red_u[lane] : 0ULL;
+    key = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-      double obs = __shfl_down_sync(FULL, bs, off);
-      int okey = __shfl_down_sync(FULL, key, off);
-      arg_combine(bs, key, obs, okey);
+      const uint64_t os = __shfl_down_sync(FULL, s, off);
+      const uint32_t ok = __shfl_down_sync(FULL, key, off);
+      if (os > s || (os == s && ok < key)) {
+        s = os;
+        key = ok;
+      }
     }
     if (lane == 0) {
-      ctl.red_s[NW] = bs;
-      ctl.red_k[NW] = key;
+      ctl.red_u[NW] = s;
+      ctl.red_k[NW] = (int)key;
     }
   }
   __syncthreads();
-  out_s = ctl.red_s[NW];
-  out_key = ctl.red_k[NW];
+  out_s = ctl.red_u[NW];
+  out_key = (uint32_t)ctl.red_k[NW];
   __syncthreads();
 }
 
@@ -192,11 +232,11 @@ __device__ void block_max4(double v[4], Ctl& ctl) {
   __syncthreads();
 }
 
-// Second argmax pass over the block A[r0:r0+rows, c0:c0+cols] of a matrix with
-// m rows (keys j*m + i, the column-major position).  Every thread gets the
-// result; bs < 0 means no element qualified (all NaN).
-__device__ void exact_argmax(const double* A, int lda, int m, int r0, int rows, int c0, int cols,
-                             uint64_t Mstar, Ctl& ctl, double& bs, int& key) {
+// Second argmax pass over the block A[r0:r0+rows, c0:c0+cols]: squares only
+// the elements near the largest |v| (Mstar).  Every thread gets the result;
+// s == 0 means no element qualified (all NaN).
+__device__ void exact_argmax(const double* A, int lda, int r0, int rows, int c0, int cols, uint64_t Mstar,
+                             Ctl& ctl, uint64_t& s, uint32_t& key) {
   ArgBest ab;
   ab.init();
   if (rows > 0 && cols > 0) {
@@ -206,7 +246,7 @@ __device__ void exact_argmax(const double* A, int lda, int m, int r0, int rows, 
     for (long long e = threadIdx.x; e < total; e += NT) {
       const int i = r0 + ii, j = c0 + jj;
       const double v = A[i + (size_t)j * lda];
-      if (near_max(abs_bits(v), Mstar)) ab.consider(v, j * m + i);
+      if (near_max(abs_bits(v), Mstar)) ab.consider(v, pack_key(i, j));
       ii += sr;
       jj += sq;
       if (ii >= rows) {
@@ -215,7 +255,74 @@ __device__ void exact_argmax(const double* A, int lda, int m, int r0, int rows, 
       }
     }
   }
-  block_argmax(ab, ctl, bs, key);
+  block_argmax(ab, ctl, s, key);
+}
+
+// The pivot of the next step (submatrixargmax of abs2, matrixlu.jl:1-32) from
+// every thread's ArgTrack over the block A[r0:, c0:]; sets ctl.r / ctl.c and
+// ends with a barrier.  One integer reduction decides it unless some element
+// other than the largest |v| lies within 16 ulps of it (its square could tie)
+// or the magnitude is where squares underflow or overflow; then the exact
+// second pass runs.
+__device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int r0, int rows, int c0, int cols,
+                               Ctl& ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t a = t.A, b = t.B;
+  uint32_t k = t.k;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+    const uint32_t k2 = __shfl_down_sync(FULL, k, off);
+    track_combine(a, k, b, a2, k2, b2);
+  }
+  if (lane == 0) {
+    ctl.red_u[warp] = a;
+    ctl.red_b[warp] = b;
+    ctl.red_k[warp] = (int)k;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < NW ? ctl.red_u[lane] : 0ULL;
+    b = lane < NW ? ctl.red_b[lane] : 0ULL;
+    k = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+      const uint32_t k2 = __shfl_down_sync(FULL, k, off);
+      track_combine(a, k, b, a2, k2, b2);
+    }
+    if (lane == 0) {
+      const uint64_t Mstar = a ? a - 1 : 0;
+      const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
+      const bool close = b != 0 && (b - 1) + 16 >= Mstar;
+      if (a == 0) {  // every element NaN: the scan keeps its start
+        ctl.r = r0;
+        ctl.c = c0;
+        ctl.need_exact = 0;
+      } else if (safe && !close) {
+        ctl.r = (int)(k & 0xffffu);
+        ctl.c = (int)(k >> 16);
+        ctl.need_exact = 0;
+      } else {
+        ctl.need_exact = 1;
+      }
+      ctl.red_u[NW] = Mstar;
+    }
+  }
+  __syncthreads();
+  if (ctl.need_exact) {
+    const uint64_t Mstar = ctl.red_u[NW];
+    uint64_t s;
+    uint32_t key;
+    exact_argmax(A, lda, r0, rows, c0, cols, Mstar, ctl, s, key);
+    if (threadIdx.x == 0) {
+      ctl.r = s ? (int)(key & 0xffffu) : r0;
+      ctl.c = s ? (int)(key >> 16) : c0;
+    }
+    __syncthreads();
+  }
 }
 
 __device__ int block_or(int v, Ctl& ctl) {
@@ -354,6 +461,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
   __syncthreads();
   int K = 0;
   while (K < kmax) {
+    TCI_PHASE(0);
     if (tid == 0) {
       const int r = ctl.r, c = ctl.c;
       double piv = A[r + (size_t)c * lda];
@@ -374,6 +482,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
       }
     }
     __syncthreads();
+    TCI_PHASE(1);
     if (ctl.stop) break;
     const int r = ctl.r, c = ctl.c;
     const double piv = ctl.piv;
@@ -386,6 +495,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
         col[r] = a;
       }
     __syncthreads();
+    TCI_PHASE(2);
     // swapcol! (matrixlu.jl:106-112) and, for leftorthogonal, A[K+1:end, K] ./= A[K, K]
     {
       double* ck = A + (size_t)K * lda;
@@ -406,13 +516,14 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
       for (int j = K + 1 + tid; j < n; j += NT) A[K + (size_t)j * lda] = __ddiv_rn(A[K + (size_t)j * lda], piv);
       __syncthreads();
     }
+    TCI_PHASE(3);
     ++K;
     if (K == kmax) break;  // the trailing update after the last pivot is not observable
     // A[K:, K:] -= x * y^T fused with the argmax of abs2 for the next pivot
     // The trailing block is walked as one column-major sequence so that every
     // lane of every warp has an element (no half-empty warps at column ends).
-    AbsMax am;
-    am.init();
+    ArgTrack at;
+    at.init();
     {
       const double* x = A + (size_t)(K - 1) * lda;
       const int rows = m - K;
@@ -424,7 +535,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
         double* col = A + (size_t)j * lda;
         double v = __dsub_rn(col[i], __dmul_rn(x[i], col[K - 1]));
         col[i] = v;
-        am.push(v);
+        at.push(v, pack_key(i, j));
         ii += sr;
         jj += sq;
         if (ii >= rows) {
@@ -433,21 +544,9 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
         }
       }
     }
-    __syncthreads();
-    const uint64_t Mstar = block_max_u64(am.M, ctl);
-    double bs;
-    int key;
-    exact_argmax(A, lda, m, K, m - K, K, n - K, Mstar, ctl, bs, key);
-    if (tid == 0) {
-      if (bs < 0.0) {  // every candidate NaN: Julia's loop keeps the first index
-        ctl.r = K;
-        ctl.c = K;
-      } else {
-        ctl.r = key % m;
-        ctl.c = key / m;
-      }
-    }
-    __syncthreads();
+    TCI_PHASE(4);
+    argmax_resolve(at, A, lda, K, m - K, K, n - K, ctl);
+    TCI_PHASE(6);
   }
   if (tid == 0) {
     ctl.K = K;
@@ -567,7 +666,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   for (int i = tid; i < m; i += NT) rowperm[i] = i;
   for (int j = tid; j < n; j += NT) colperm[j] = j;
   int lut_used = 0;
-  AbsMax am;
+  ArgTrack am;
   am.init();
   unsigned long long mx = 0;
   if (T.ain) {
@@ -577,7 +676,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
       for (int i = lane; i < m; i += 32) {
         double v = src[i];
         dst[i] = v;
-        am.push(v);
+        am.push(v, pack_key(i, j));
         unsigned long long b = abs_bits(v);
         mx = b > mx ? b : mx;
       }
@@ -602,7 +701,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
       for (int i = lane; i < m; i += 32) {
         double v = F(rs0[i] + c0, rs1[i] + c1);
         dst[i] = v;
-        am.push(v);
+        am.push(v, pack_key(i, j));
         unsigned long long b = abs_bits(v);
         mx = b > mx ? b : mx;
       }
@@ -610,21 +709,8 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   }
   __syncthreads();
   unsigned long long mxall = block_max_u64(mx, ctl);
-  const uint64_t Mstar = block_max_u64(am.M, ctl);
-  double bs;
-  int key;
-  exact_argmax(A, lda, m, 0, m, 0, n, Mstar, ctl, bs, key);
-  if (tid == 0) {
-    if (bs < 0.0 || m == 0 || n == 0) {
-      ctl.r = 0;
-      ctl.c = 0;
-    } else {
-      ctl.r = key % m;
-      ctl.c = key / m;
-    }
-    ctl.status = 0;
-  }
-  __syncthreads();
+  if (tid == 0) ctl.status = 0;
+  argmax_resolve(am, A, lda, 0, m, 0, n, ctl);
   const bool leftorth = T.leftorth != 0;
   rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl);
   const int K = ctl.K;
@@ -684,24 +770,15 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   const double* rg1[2] = {ps1, rs1};
   const int rc[2] = {r, m};
   const Filler F = make_filler(T, prm, rg0, rg1, rc, 2, cs0, cs1, r, (int64_t)(r + m) * r, ctl);
-  AbsMax am;
+  ArgTrack am;
   am.init();
   for (int j = warp; j < r; j += NW)
     for (int i = lane; i < r; i += 32) {
       double v = F(ps0[i] + cs0[j], ps1[i] + cs1[j]);
       P[i + (size_t)j * r] = v;
-      am.push(v);
+      am.push(v, pack_key(i, j));
     }
-  __syncthreads();
-  const uint64_t Mstar = block_max_u64(am.M, ctl);
-  double bs;
-  int key;
-  exact_argmax(P, r, r, 0, r, 0, r, Mstar, ctl, bs, key);
-  if (tid == 0) {
-    ctl.r = bs < 0.0 ? 0 : key % r;
-    ctl.c = bs < 0.0 ? 0 : key / r;
-  }
-  __syncthreads();
+  argmax_resolve(am, P, r, 0, r, 0, r, ctl);
   rrlu_loop(P, r, r, r, r, 0.0, 0.0, true, rowperm, colperm, rp.diag, ctl);
   int singular = 0;
   if (tid == 0) {
@@ -1189,11 +1266,11 @@ __global__ void __launch_bounds__(NT, 1)
 }  // namespace
 
 // Shared-memory budget of one CTA of the step kernel.
-size_t tci_step_smem_bytes() { return 227 * 1024 - 1024; }
+size_t tci_step_smem_bytes() { return 227 * 1024 - 2048; }
 
 // Dynamic shared memory of the resident kernel (its static shared memory holds
 // the task record and the f parameters as well).
-size_t tci_resident_smem_bytes() { return tci_step_smem_bytes() - 2048; }
+size_t tci_resident_smem_bytes() { return tci_step_smem_bytes(); }
 
 cudaError_t tci_step_configure() {
   cudaError_t e = cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
