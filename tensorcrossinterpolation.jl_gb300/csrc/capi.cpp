@@ -10,6 +10,7 @@
 #include <thread>
 #include <cstdlib>
 #include <algorithm>
+#include <numeric>
 
 #include "engine.h"
 
@@ -479,6 +480,13 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
   const double budget = (double)pool[0]->hbm_budget;
   std::vector<double> est(n);
   for (int64_t i = 0; i < n; ++i) est[i] = solve_estimate_bytes(reqs[i]);
+  // Admission order: by arrival when there are arrival times; otherwise the
+  // largest solves first, so that the longest serial chains do not start last
+  // and leave the device with a tail of a few live solves.
+  std::vector<int64_t> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  if (!arrival)
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return est[a] > est[b]; });
   DriveShared sh;
 
   auto worker = [&](int g) {
@@ -524,8 +532,9 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
           if (sh.fatal) return;
           double t = now_s() - t0;
           if (sh.next < n && sh.live < max_live && (int64_t)mine.size() < share &&
-              (!arrival || arrival[sh.next] <= t) && (sh.live == 0 || sh.live_bytes + est[sh.next] <= budget)) {
-            idx = sh.next++;
+              (!arrival || arrival[sh.next] <= t) &&
+              (sh.live == 0 || sh.live_bytes + est[order[sh.next]] <= budget)) {
+            idx = order[sh.next++];
             ++sh.live;
             sh.live_bytes += est[idx];
           }

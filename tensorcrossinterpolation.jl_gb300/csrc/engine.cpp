@@ -281,7 +281,7 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
     }
     case TCI_TASK_SITE: {
       const size_t r = (size_t)t.r;
-      size_t rest = 2 * a16(r * 4) + 4 * a16(r * 8) + 2 * a16(m * 8);
+      size_t rest = 2 * a16(r * 4) + 5 * a16(r * 8) + 2 * a16(m * 8);
       size_t want_rows = std::min<size_t>(std::max<size_t>(m, 1), 64);
       if (a16(r * r * 8) + rest + want_rows * (r * 8 + 8) <= smem) {
         t.smem_mode = 1;
@@ -496,8 +496,9 @@ void Engine::account(const Req& r, int smem_mode) {
   const tci_result_head* h = r.head();
   stats.task_cycles += h->cycles;
   if (task_log_) {
-    std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d\n", (long long)stats.steps, r.t.kind, r.t.m, r.t.n,
-                 r.t.r, h->npivot, (long long)h->cycles, smem_mode, h->lut_used);
+    std::fprintf(task_log_, "%lld %d %d %d %d %d %lld %d %d %d %d %d %d\n", (long long)stats.steps, r.t.kind,
+                 r.t.m, r.t.n, r.t.r, h->npivot, (long long)h->cycles, smem_mode, h->lut_used, h->status,
+                 r.t.nl, r.t.nr, r.t.lutcap0);
   }
   const tci_task& t = r.t;
   switch (t.kind) {
@@ -805,6 +806,9 @@ int Engine::submit() {
       t.res = (int64_t)(uintptr_t)(rec + o_res);
       if (r.ain_host) t.ain = (const double*)(rec + o_ain);
       r.res = rec + o_res;
+      // the block may hold anything from an earlier use: clear the done word so
+      // that a stale value can never read as this task's completion
+      ((tci_result_head*)r.res)->done = 0;
       const size_t lut = t.lutcap0 > 0 ? (size_t)t.lutcap0 + (size_t)std::max(t.lutcap1, 0) : 0;
       t.work = nullptr;
       t.lut = nullptr;
@@ -1114,7 +1118,17 @@ CoTask co_updatepivots(Engine& e, Solve& s, int b, bool leftorth, double reltol,
   const tci_result_head* h = r.head();
   s.nfeval += (i64)Ic.n * (i64)Jc.n;
   updatemaxsample(s, h->maxabs);
-  if (h->status & TCI_ST_NAN) co_return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  if (h->status & TCI_ST_NAN) {
+    if (std::getenv("TCI_DEBUG_NAN")) {
+      std::fprintf(stderr, "NaN task: b %d m %d n %d nl %d nr %d lutcap %d %d lut_used %d smem %d K %d maxabs %g "
+                   "maxabs_nan %d cycles %lld fid %d nparams %d L %d resident %d\n", b, r.t.m, r.t.n, r.t.nl,
+                   r.t.nr, r.t.lutcap0, r.t.lutcap1, h->lut_used, r.t.smem_mode, h->npivot, h->maxabs,
+                   h->maxabs_nan, (long long)h->cycles, r.t.fid, r.t.nparams, s.L, (int)e.resident());
+      for (int q = 0; q < (int)s.params.size(); ++q) std::fprintf(stderr, " %g", s.params[q]);
+      std::fprintf(stderr, "\n");
+    }
+    co_return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  }
   const int K = h->npivot;
   s.Iset[b + 1] = select(Ic, r.rowperm(), K);
   s.Jset[b] = select(Jc, r.colperm(), K);

@@ -23,6 +23,7 @@
 // (matrixlu.jl:16-31).  The comparison of v*v is skipped for elements whose |v|
 // is more than 16 ulps below the running maximum, where v*v is provably smaller.
 #include <cuda_runtime.h>
+#include <limits.h>
 #include <stddef.h>
 #include <stdint.h>
 
@@ -52,7 +53,7 @@ struct Ctl {
   int red_k[NW + 1];
   unsigned long long red_u[NW + 1];
   unsigned long long red_b[NW + 1];
-  double red4[4][NW + 1];
+  long long red4[4][NW + 1];
 };
 
 __device__ __forceinline__ double jmax(double a, double b) {
@@ -208,29 +209,6 @@ __device__ unsigned long long block_max_u64(unsigned long long v, Ctl& ctl) {
   return r;
 }
 
-__device__ void block_max4(double v[4], Ctl& ctl) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) v[q] = fmax(v[q], __shfl_down_sync(FULL, v[q], off));
-    if (lane == 0) ctl.red4[q][warp] = v[q];
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      double x = lane < NW ? ctl.red4[q][lane] : -1e300;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) x = fmax(x, __shfl_down_sync(FULL, x, off));
-      if (lane == 0) ctl.red4[q][NW] = x;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int q = 0; q < 4; ++q) v[q] = ctl.red4[q][NW];
-  __syncthreads();
-}
 
 // Second argmax pass over the block A[r0:r0+rows, c0:c0+cols]: squares only
 // the elements near the largest |v| (Mstar).  Every thread gets the result;
@@ -339,13 +317,31 @@ __device__ __forceinline__ const char* at(const char* base, int64_t off) {
 }
 __device__ __forceinline__ char* atw(char* base, int64_t off) { return (char*)((uintptr_t)base + (uintptr_t)off); }
 
-// Row / column partial sums of the registered f (tci_functions.h).
-__device__ void compute_states(int fid, const double* params, const uint8_t* idx, int count, int len,
+// Row / column partial sums of the registered f (tci_functions.h).  For a
+// task that may tabulate f (int_states), the sums are exact integers and are
+// stored as long long in the same 8-byte slots; make_filler turns them back
+// into doubles if it decides against tables.
+__device__ __forceinline__ bool int_states(const tci_task& T) {
+  return tci_f_tables(T.fid) > 0 && T.lut != nullptr && T.lutcap0 > 0;
+}
+__device__ void compute_states(const tci_task& T, const double* params, const uint8_t* idx, int count, int len,
                                int site0, double* s0, double* s1) {
+  if (int_states(T)) {
+    long long* q0 = (long long*)s0;
+    long long* q1 = (long long*)s1;
+    for (int i = threadIdx.x; i < count; i += NT) {
+      long long a0 = 0, a1 = 0;
+      const uint8_t* v = idx + (size_t)i * len;
+      for (int p = 0; p < len; ++p) tci_f_term_int(T.fid, params, site0 + p, v[p], &a0, &a1);
+      q0[i] = a0;
+      q1[i] = a1;
+    }
+    return;
+  }
   for (int i = threadIdx.x; i < count; i += NT) {
     double a0 = 0.0, a1 = 0.0;
     const uint8_t* v = idx + (size_t)i * len;
-    for (int p = 0; p < len; ++p) tci_f_term(fid, params, site0 + p, v[p], &a0, &a1);
+    for (int p = 0; p < len; ++p) tci_f_term(T.fid, params, site0 + p, v[p], &a0, &a1);
     s0[i] = a0;
     s1[i] = a1;
   }
@@ -353,75 +349,131 @@ __device__ void compute_states(int fid, const double* params, const uint8_t* idx
 
 // Element generator of a registered f from row/column partial sums.  When f
 // factors through exact integer sums (tci_f_tables), the distinct values of
-// part0/part1 over the task's range are computed once into T.lut and each
-// element is combine(table0[s0], table1[s1]) -- the same functions the direct
-// path calls, so the bits are identical.
+// part0 and of scale1(part1) over the task's range are computed once into
+// T.lut and each element is combine_scaled(table0[s0], table1[s1]) -- one FP64
+// operation; the direct path computes the same functions, so the bits are
+// identical.
 struct Filler {
   int fid, nparams;
   const double* prm;
   const double* lut0;
   const double* lut1;
   int lo0, lo1;
-  __device__ __forceinline__ double operator()(double a0, double a1) const {
+  // element (i, j) from row states r0/r1 and column states c0/c1
+  __device__ __forceinline__ double val(const double* r0, const double* r1, int i, const double* c0,
+                                        const double* c1, int j) const {
     if (lut0) {
-      double p0 = lut0[(int)a0 - lo0];
-      double p1 = lut1 ? lut1[(int)a1 - lo1] : 0.0;
-      return tci_f_combine(fid, prm, p0, p1);
+      const double p0 = lut0[(int)(((const long long*)r0)[i] + ((const long long*)c0)[j]) - lo0];
+      if (!lut1) return p0;
+      const double q1 = lut1[(int)(((const long long*)r1)[i] + ((const long long*)c1)[j]) - lo1];
+      return tci_f_combine_scaled(fid, p0, q1);
     }
-    return tci_f_finish(fid, prm, nparams, a0, a1);
+    return tci_f_finish(fid, prm, nparams, r0[i] + c0[j], r1[i] + c1[j]);
   }
 };
 
-// Block-wide max of four doubles (pass -x for a minimum).
-__device__ void block_max4(double v[4], Ctl& ctl);
+// Block-wide max of four signed 64-bit integers (pass -x for a minimum).
+__device__ void block_max4_i64(long long v[4], Ctl& ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const long long o = __shfl_down_sync(FULL, v[q], off);
+      v[q] = o > v[q] ? o : v[q];
+    }
+    if (lane == 0) ctl.red4[q][warp] = v[q];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      long long x = lane < NW ? ctl.red4[q][lane] : LLONG_MIN;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const long long o = __shfl_down_sync(FULL, x, off);
+        x = o > x ? o : x;
+      }
+      if (lane == 0) ctl.red4[q][NW] = x;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q) v[q] = ctl.red4[q][NW];
+  __syncthreads();
+}
 
 // Decide on tabulation for a task whose elements are sums rs[i] + cs[j] over
 // the given row-state groups, and fill the tables.  Ends with a barrier.
-__device__ Filler make_filler(const tci_task& T, const double* prm, const double* const* rs0,
-                              const double* const* rs1, const int* rcount, int ngroups, const double* cs0,
-                              const double* cs1, int n, int64_t elems, Ctl& ctl) {
+__device__ Filler make_filler(const tci_task& T, const double* prm, double* const* rs0, double* const* rs1,
+                              const int* rcount, int ngroups, double* cs0, double* cs1, int n, int64_t elems,
+                              Ctl& ctl) {
   Filler F;
   F.fid = T.fid;
   F.nparams = T.nparams;
   F.prm = prm;
   F.lut0 = F.lut1 = nullptr;
   F.lo0 = F.lo1 = 0;
+  if (!int_states(T)) return F;
   const int tables = tci_f_tables(T.fid);
-  if (tables == 0 || T.lut == nullptr || T.lutcap0 <= 0) return F;
   // max / -min of the row and column sums
-  double v[4] = {-1e300, -1e300, -1e300, -1e300};  // max r0, max r1, -min r0, -min r1
-  double w[4] = {-1e300, -1e300, -1e300, -1e300};
-  for (int g = 0; g < ngroups; ++g)
+  long long v[4] = {LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN};  // max r0, max r1, -min r0, -min r1
+  long long w[4] = {LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN};
+  for (int g = 0; g < ngroups; ++g) {
+    const long long* a0 = (const long long*)rs0[g];
+    const long long* a1 = (const long long*)rs1[g];
     for (int i = threadIdx.x; i < rcount[g]; i += NT) {
-      v[0] = fmax(v[0], rs0[g][i]);
-      v[1] = fmax(v[1], rs1[g][i]);
-      v[2] = fmax(v[2], -rs0[g][i]);
-      v[3] = fmax(v[3], -rs1[g][i]);
+      v[0] = max(v[0], a0[i]);
+      v[1] = max(v[1], a1[i]);
+      v[2] = max(v[2], -a0[i]);
+      v[3] = max(v[3], -a1[i]);
     }
-  for (int j = threadIdx.x; j < n; j += NT) {
-    w[0] = fmax(w[0], cs0[j]);
-    w[1] = fmax(w[1], cs1[j]);
-    w[2] = fmax(w[2], -cs0[j]);
-    w[3] = fmax(w[3], -cs1[j]);
   }
-  block_max4(v, ctl);
-  block_max4(w, ctl);
-  if (v[0] < -1e299 || w[0] < -1e299) return F;  // no rows or no columns
-  const double lo0 = -v[2] + -w[2], hi0 = v[0] + w[0];
-  const double lo1 = -v[3] + -w[3], hi1 = v[1] + w[1];
-  const double n0 = hi0 - lo0 + 1.0, n1 = tables > 1 ? hi1 - lo1 + 1.0 : 0.0;
-  if (!(n0 <= (double)T.lutcap0) || (tables > 1 && !(n1 <= (double)T.lutcap1))) return F;
-  if (n0 + n1 > (double)elems) return F;  // tabulating would cost more than it saves
+  {
+    const long long* b0 = (const long long*)cs0;
+    const long long* b1 = (const long long*)cs1;
+    for (int j = threadIdx.x; j < n; j += NT) {
+      w[0] = max(w[0], b0[j]);
+      w[1] = max(w[1], b1[j]);
+      w[2] = max(w[2], -b0[j]);
+      w[3] = max(w[3], -b1[j]);
+    }
+  }
+  block_max4_i64(v, ctl);
+  block_max4_i64(w, ctl);
+  bool use = v[0] != LLONG_MIN && w[0] != LLONG_MIN;  // rows and columns exist
+  long long lo0 = 0, lo1 = 0, n0 = 0, n1 = 0;
+  if (use) {
+    lo0 = -v[2] - w[2];
+    lo1 = -v[3] - w[3];
+    n0 = v[0] + w[0] - lo0 + 1;
+    n1 = tables > 1 ? v[1] + w[1] - lo1 + 1 : 0;
+    use = n0 <= T.lutcap0 && (tables == 1 || n1 <= T.lutcap1) &&
+          n0 + n1 <= elems;  // tabulating must cost less than it saves
+  }
+  if (!use) {  // direct evaluation: the sums become doubles (exact)
+    for (int g = 0; g < ngroups; ++g)
+      for (int i = threadIdx.x; i < rcount[g]; i += NT) {
+        rs0[g][i] = (double)((const long long*)rs0[g])[i];
+        rs1[g][i] = (double)((const long long*)rs1[g])[i];
+      }
+    for (int j = threadIdx.x; j < n; j += NT) {
+      cs0[j] = (double)((const long long*)cs0)[j];
+      cs1[j] = (double)((const long long*)cs1)[j];
+    }
+    __syncthreads();
+    return F;
+  }
   double* t0 = T.lut;
   double* t1 = T.lut + T.lutcap0;
-  const int c0 = (int)n0, c1 = (int)n1, l0 = (int)lo0, l1 = (int)lo1;
-  for (int k = threadIdx.x; k < c0; k += NT) t0[k] = tci_f_part0(T.fid, prm, T.nparams, (double)(l0 + k));
-  for (int k = threadIdx.x; k < c1; k += NT) t1[k] = tci_f_part1(T.fid, prm, (double)(l1 + k));
+  for (int k = threadIdx.x; k < (int)n0; k += NT) t0[k] = tci_f_part0(T.fid, prm, T.nparams, (double)(lo0 + k));
+  for (int k = threadIdx.x; k < (int)n1; k += NT)
+    t1[k] = tci_f_scale1(T.fid, prm, tci_f_part1(T.fid, prm, (double)(lo1 + k)));
   __syncthreads();
   F.lut0 = t0;
   F.lut1 = tables > 1 ? t1 : nullptr;
-  F.lo0 = l0;
-  F.lo1 = l1;
+  F.lo0 = (int)lo0;
+  F.lo1 = (int)lo1;
   return F;
 }
 
@@ -687,19 +739,18 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
     double* rs1 = (double*)cur.take((size_t)m * 8);
     double* cs0 = (double*)cur.take((size_t)n * 8);
     double* cs1 = (double*)cur.take((size_t)n * 8);
-    compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
-    compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
+    compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
+    compute_states(T, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
     __syncthreads();
-    const double* rg0[1] = {rs0};
-    const double* rg1[1] = {rs1};
+    double* const rg0[1] = {rs0};
+    double* const rg1[1] = {rs1};
     const int rc[1] = {m};
     const Filler F = make_filler(T, prm, rg0, rg1, rc, 1, cs0, cs1, n, (int64_t)m * n, ctl);
     lut_used = F.lut0 != nullptr;
     for (int j = warp; j < n; j += NW) {
       double* dst = A + (size_t)j * lda;
-      const double c0 = cs0[j], c1 = cs1[j];
       for (int i = lane; i < m; i += 32) {
-        double v = F(rs0[i] + c0, rs1[i] + c1);
+        double v = F.val(rs0, rs1, i, cs0, cs1, j);
         dst[i] = v;
         am.push(v, pack_key(i, j));
         unsigned long long b = abs_bits(v);
@@ -758,23 +809,23 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   double* cs1 = (double*)cur.take((size_t)r * 8);
   double* rs0 = (double*)cur.take((size_t)m * 8);
   double* rs1 = (double*)cur.take((size_t)m * 8);
-  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.prows), r, T.nl, 0, ps0, ps1);
-  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), r, T.nr, T.nl, cs0, cs1);
-  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
+  compute_states(T, prm, (const uint8_t*)at(blob, T.prows), r, T.nl, 0, ps0, ps1);
+  compute_states(T, prm, (const uint8_t*)at(blob, T.cols), r, T.nr, T.nl, cs0, cs1);
+  compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
   for (int i = tid; i < r; i += NT) {
     rowperm[i] = i;
     colperm[i] = i;
   }
   __syncthreads();
-  const double* rg0[2] = {ps0, rs0};
-  const double* rg1[2] = {ps1, rs1};
+  double* const rg0[2] = {ps0, rs0};
+  double* const rg1[2] = {ps1, rs1};
   const int rc[2] = {r, m};
   const Filler F = make_filler(T, prm, rg0, rg1, rc, 2, cs0, cs1, r, (int64_t)(r + m) * r, ctl);
   ArgTrack am;
   am.init();
   for (int j = warp; j < r; j += NW)
     for (int i = lane; i < r; i += 32) {
-      double v = F(ps0[i] + cs0[j], ps1[i] + cs1[j]);
+      double v = F.val(ps0, ps1, i, cs0, cs1, j);
       P[i + (size_t)j * r] = v;
       am.push(v, pack_key(i, j));
     }
@@ -789,6 +840,9 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   }
   __syncthreads();
   // T = Pi1 * inv(P): per row, w = Pi1[row, colperm]; z U = w; s L = z; t[rowperm] = s.
+  // The diagonal of U is inverted once; rows multiply by the reciprocals.
+  double* dinv = (double*)cur.take((size_t)r * 8);
+  for (int q = tid; q < r; q += NT) dinv[q] = 1.0 / P[q + (size_t)q * r];
   size_t used = (size_t)(cur.p - smem);
   int RB = (int)((smem_bytes > used ? smem_bytes - used : 0) / ((size_t)r * 8 + 8));
   RB = RB > NT ? NT : RB;
@@ -801,7 +855,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     for (int e = tid; e < rows_here * r; e += NT) {
       int rr = e % rows_here, q = e / rows_here;
       int row = base + rr, col = colperm[q];
-      double v = F(rs0[row] + cs0[col], rs1[row] + cs1[col]);
+      double v = F.val(rs0, rs1, row, cs0, cs1, col);
       W[rr + (size_t)q * RB] = v;
       unsigned long long b = abs_bits(v);
       mx = b > mx ? b : mx;
@@ -811,7 +865,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
       for (int rr = tid; rr < rows_here; rr += NT) {
         // forward: z U = w (U upper, non-unit)
         for (int q = 0; q < r; ++q) {
-          double zq = W[rr + (size_t)q * RB] / P[q + (size_t)q * r];
+          double zq = W[rr + (size_t)q * RB] * dinv[q];
           W[rr + (size_t)q * RB] = zq;
           for (int p = q + 1; p < r; ++p) W[rr + (size_t)p * RB] = W[rr + (size_t)p * RB] - zq * P[q + (size_t)p * r];
         }
@@ -853,17 +907,17 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
   double* rs1 = (double*)cur.take((size_t)m * 8);
   double* cs0 = (double*)cur.take((size_t)n * 8);
   double* cs1 = (double*)cur.take((size_t)n * 8);
-  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
-  compute_states(T.fid, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
+  compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
+  compute_states(T, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
   __syncthreads();
-  const double* rg0[1] = {rs0};
-  const double* rg1[1] = {rs1};
+  double* const rg0[1] = {rs0};
+  double* const rg1[1] = {rs1};
   const int rc[1] = {m};
   const Filler F = make_filler(T, prm, rg0, rg1, rc, 1, cs0, cs1, n, (int64_t)m * n, ctl);
   unsigned long long mx = 0;
   for (int j = warp; j < n; j += NW)
     for (int i = lane; i < m; i += 32) {
-      double v = F(rs0[i] + cs0[j], rs1[i] + cs1[j]);
+      double v = F.val(rs0, rs1, i, cs0, cs1, j);
       T.core_out[i + (size_t)j * m] = v;
       unsigned long long b = abs_bits(v);
       mx = b > mx ? b : mx;

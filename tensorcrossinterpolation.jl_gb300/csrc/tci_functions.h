@@ -24,7 +24,7 @@ enum {
 
 // Parameter layouts (double array `params`):
 //   LORENTZ: [coeff]                      (empty => coeff = 1)
-//   SERVED : [alpha, beta, gamma, c_1 .. c_L]
+//   SERVED : [alpha, beta, gamma, c_1 .. c_L]  (c truncated to integers)
 //   QTT1D  : [kind]   kind 0: exp(-x) cos(2000 pi x) + 0.5 exp(-(x-0.3)^2/1e-4)
 //                     kind 1: exp(-x)
 //                     kind 2: exp(-x) + 1e-4 exp(-2x)
@@ -43,7 +43,7 @@ TCI_HD void tci_f_term(int fid, const double* params, int site, int v,
     } break;
     case TCI_F_SERVED: {
       double v1 = (double)(v + 1);
-      double dv = v1 - params[3 + site];
+      double dv = v1 - (double)(long long)params[3 + site];  // centres are lattice points
       *acc0 = *acc0 + v1 * v1;
       *acc1 = *acc1 + dv * dv;
     } break;
@@ -80,9 +80,31 @@ TCI_HD double tci_f_part1(int fid, const double* params, double acc1) {
   (void)fid;
   return tci_exp(-(params[2] * acc1));  // SERVED
 }
+// combine(p0, p1) = combine_scaled(p0, scale1(p1)): tables of part1 may hold the
+// scaled value, so that combining costs one operation per element.
+TCI_HD double tci_f_scale1(int fid, const double* params, double p1) {
+  (void)fid;
+  return params[1] * p1;  // SERVED
+}
+TCI_HD double tci_f_combine_scaled(int fid, double p0, double q1) {
+  if (fid == TCI_F_LORENTZ) return p0;
+  return p0 + q1;  // SERVED
+}
 TCI_HD double tci_f_combine(int fid, const double* params, double p0, double p1) {
   if (fid == TCI_F_LORENTZ) return p0;
-  return p0 + params[1] * p1;  // SERVED
+  return tci_f_combine_scaled(fid, p0, tci_f_scale1(fid, params, p1));
+}
+
+// Integer form of the per-site terms of the factored functions (exact: the
+// double sums of tci_f_term hold the same integers).  Only valid when the
+// SERVED centres c are integers.
+TCI_HD void tci_f_term_int(int fid, const double* params, int site, int v, long long* acc0, long long* acc1) {
+  const long long v1 = v + 1;
+  *acc0 += v1 * v1;
+  if (fid == TCI_F_SERVED) {
+    const long long dv = v1 - (long long)params[3 + site];
+    *acc1 += dv * dv;
+  }
 }
 
 TCI_HD double tci_f_finish(int fid, const double* params, int nparams, double acc0,
