@@ -255,6 +255,9 @@ typedef struct tci_stats {
    * on one CTA, one CTA per SM): divided by SMs x clock x wall time it gives
    * the fraction of the device kept busy */
   int64_t task_cycles;
+  /* elements of feval computed from tables of the factored f parts (one FP64
+   * operation each) rather than by evaluating f */
+  int64_t feval_tabulated;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
 

@@ -185,6 +185,7 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.host_wait_ms += s.host_wait_ms;
     t.host_resume_ms += s.host_resume_ms;
     t.task_cycles += s.task_cycles;
+    t.feval_tabulated += s.feval_tabulated;
     if (reset) e->stats = tci_stats{};
   }
   if (ctx->rq) {

@@ -501,6 +501,10 @@ void Engine::account(const Req& r, int smem_mode) {
                  r.t.nl, r.t.nr, r.t.lutcap0);
   }
   const tci_task& t = r.t;
+  if (h->lut_used) {
+    if (t.kind == TCI_TASK_RRLU || t.kind == TCI_TASK_CORE) stats.feval_tabulated += (int64_t)t.m * t.n;
+    if (t.kind == TCI_TASK_SITE) stats.feval_tabulated += (int64_t)t.r * t.r + (int64_t)t.m * t.r;
+  }
   switch (t.kind) {
     case TCI_TASK_RRLU: {
       if (!t.ain) stats.feval += (int64_t)t.m * t.n;

@@ -90,6 +90,7 @@ class Stats(ctypes.Structure):
         ("host_wait_ms", ctypes.c_double),
         ("host_resume_ms", ctypes.c_double),
         ("task_cycles", ctypes.c_int64),
+        ("feval_tabulated", ctypes.c_int64),
     ]
 
 
