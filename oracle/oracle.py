@@ -127,6 +127,16 @@ def lib():
                                                ctypes.c_int64, ctypes.c_int64, ctypes.c_int]
         L.orc_solve_batch.argtypes = [ctypes.c_int64, I32P, I64P, I64P, I32P, F64P, I64P, I64P, F64P,
                                       I64P, ctypes.POINTER(Opts), I64P, F64P, ctypes.c_int]
+        L.orc_tt4_contract.restype = ctypes.c_void_p
+        L.orc_tt4_contract.argtypes = [ctypes.c_int, I64P, F64P, I64P, F64P, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+        L.orc_tt4_compress.restype = ctypes.c_void_p
+        L.orc_tt4_compress.argtypes = [ctypes.c_int, I64P, F64P, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_int)]
+        L.orc_tt4_length.argtypes = [ctypes.c_void_p]
+        L.orc_tt4_dims.argtypes = [ctypes.c_void_p, I64P]
+        L.orc_tt4_core.argtypes = [ctypes.c_void_p, ctypes.c_int, F64P]
+        L.orc_tt4_free.argtypes = [ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -412,3 +422,61 @@ def dense_params(table):
     dims = table.shape
     strides = np.cumprod((1,) + dims[:-1])
     return np.concatenate([[len(dims)], strides.astype(np.float64), table.reshape(-1, order="F")])
+
+
+def _tt4_pack(cores):
+    cores = [np.asarray(c, dtype=np.float64) for c in cores]
+    dims = np.ascontiguousarray([list(c.shape) for c in cores], dtype=np.int64).reshape(-1)
+    vals = np.ascontiguousarray(np.concatenate([c.reshape(-1, order="F") for c in cores]))
+    return dims, vals
+
+
+def _tt4_unpack(h, rc):
+    L = lib()
+    try:
+        if rc.value:
+            raise OracleError(rc.value, L.orc_last_error().decode())
+        n = L.orc_tt4_length(h)
+        dims = np.zeros(4 * n, np.int64)
+        L.orc_tt4_dims(h, _p(dims, I64P))
+        out = []
+        for b in range(n):
+            shape = tuple(int(x) for x in dims[4 * b:4 * b + 4])
+            buf = np.zeros(int(np.prod(shape)), np.float64)
+            L.orc_tt4_core(h, b, _p(buf, F64P))
+            out.append(buf.reshape(shape, order="F"))
+        return out
+    finally:
+        L.orc_tt4_free(h)
+
+
+def tt4_contract(a, b, algorithm="zipup", tolerance=1e-12, maxbonddim=None):
+    """contract_naive / contract_zipup(:LU) (contraction.jl:351-372, 442-486) of two
+    trains of 4-leg cores; returns the list of cores."""
+    ad, av = _tt4_pack(a)
+    bd, bv = _tt4_pack(b)
+    rc = ctypes.c_int()
+    h = lib().orc_tt4_contract(len(a), _p(ad, I64P), _p(av, F64P), _p(bd, I64P), _p(bv, F64P),
+                               1 if algorithm == "naive" else 2, float(tolerance), int(maxbonddim or 0),
+                               ctypes.byref(rc))
+    return _tt4_unpack(h, rc)
+
+
+def tt4_compress(cores, tolerance=1e-12, maxbonddim=None, normalizeerror=True):
+    """compress!(tt, :LU) (tensortrain.jl:149-183); returns the list of cores."""
+    d, v = _tt4_pack(cores)
+    rc = ctypes.c_int()
+    h = lib().orc_tt4_compress(len(cores), _p(d, I64P), _p(v, F64P), float(tolerance), int(maxbonddim or 0),
+                               int(bool(normalizeerror)), ctypes.byref(rc))
+    return _tt4_unpack(h, rc)
+
+
+def tt4_full(cores):
+    """The operator of a train of 4-leg cores as a dense (prod s_in) x (prod s_out)
+    matrix, first site fastest (the reference tests' _tomat)."""
+    t = np.ones((1, 1, 1))  # (rows, cols, bond)
+    for c in cores:
+        r0, s1, s2, r1 = c.shape
+        x = np.einsum("abr,rstq->asbtq", t, c)  # (rows, s1, cols, s2, r1)
+        t = x.reshape(t.shape[0] * s1, t.shape[1] * s2, r1, order="F")
+    return t[:, :, 0]

@@ -851,6 +851,188 @@ std::vector<MultiIndex> read_pivots(const int64_t* piv, i64 np, int L) {
   return out;
 }
 
+// ---------------------------------------------------------------- tensor-train contraction
+// Cores with 4 legs (link, s_in, s_out, link'), column-major.  Every contracted
+// element is a sum in ascending order of the contracted (fused) index with a
+// separate multiply and add -- the reference leaves that order to BLAS
+// (contraction.jl:71-93); fixing it makes the device results reproducible.
+struct Core4 {
+  i64 d[4] = {1, 1, 1, 1};
+  std::vector<double> v;
+  i64 size() const { return d[0] * d[1] * d[2] * d[3]; }
+};
+using TT4 = std::vector<Core4>;
+
+// left(lu) / right(lu) (matrixlu.jl:374-392): rows / columns put back in place.
+void lu_left(const RRLU& lu, std::vector<double>& out) {
+  const i64 m = lu.m, K = lu.npivot;
+  out.assign((size_t)(m * K), 0.0);
+  for (i64 k = 0; k < K; ++k)
+    for (i64 i = 0; i < m; ++i) out[lu.rowperm[i] + m * k] = lu.L[i + m * k];
+}
+void lu_right(const RRLU& lu, std::vector<double>& out) {
+  const i64 n = lu.n, K = lu.npivot;
+  out.assign((size_t)(K * n), 0.0);
+  for (i64 j = 0; j < n; ++j)
+    for (i64 k = 0; k < K; ++k) out[k + K * lu.colperm[j]] = lu.U[k + K * j];
+}
+
+// _contractsitetensors (contraction.jl:333-349)
+Core4 naive_site(const Core4& a, const Core4& b) {
+  Core4 c;
+  c.d[0] = a.d[0] * b.d[0];
+  c.d[1] = a.d[1];
+  c.d[2] = b.d[2];
+  c.d[3] = a.d[3] * b.d[3];
+  c.v.assign((size_t)c.size(), 0.0);
+  const i64 ra = a.d[0], s1 = a.d[1], s2 = a.d[2], ra2 = a.d[3], rb = b.d[0], s3 = b.d[2], rb2 = b.d[3];
+  i64 e = 0;
+  for (i64 jb = 0; jb < rb2; ++jb)
+    for (i64 ja = 0; ja < ra2; ++ja)
+      for (i64 i3 = 0; i3 < s3; ++i3)
+        for (i64 i1 = 0; i1 < s1; ++i1)
+          for (i64 ib = 0; ib < rb; ++ib)
+            for (i64 ia = 0; ia < ra; ++ia, ++e) {
+              double acc = 0.0;
+              for (i64 k = 0; k < s2; ++k)
+                acc = acc + a.v[ia + ra * (i1 + s1 * (k + s2 * ja))] * b.v[ib + rb * (k + s2 * (i3 + s3 * jb))];
+              c.v[e] = acc;
+            }
+  return c;
+}
+
+// C = A (M x K) * B (K x N), column-major.
+void matmul(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 ldc, i64 M, i64 N, i64 K) {
+  for (i64 j = 0; j < N; ++j)
+    for (i64 i = 0; i < M; ++i) {
+      double acc = 0.0;
+      for (i64 k = 0; k < K; ++k) acc = acc + A[i + lda * k] * B[k + ldb * j];
+      C[i + ldc * j] = acc;
+    }
+}
+
+// _factorize(A, :LU; tolerance, maxbonddim, leftorthogonal, normalizeerror)
+// (tensortrain.jl:95-110)
+int factorize_lu(const std::vector<double>& A, i64 m, i64 n, double tolerance, i64 maxbonddim, bool leftorth,
+                 bool normalizeerror, std::vector<double>& left, std::vector<double>& right, i64& K) {
+  const double reltol = normalizeerror ? tolerance : 1e-14;
+  const double abstol = normalizeerror ? 0.0 : tolerance;
+  RRLU lu;
+  int rc = rrlu(A.data(), m, n, maxbonddim, reltol, abstol, leftorth, lu);
+  if (rc) return rc;
+  lu_left(lu, left);
+  lu_right(lu, right);
+  K = lu.npivot;
+  return ORC_OK;
+}
+
+// contract_zipup(A, B; tolerance, method=:LU, maxbonddim) (contraction.jl:442-486)
+int contract_zipup_lu(const TT4& A, const TT4& B, double tolerance, i64 maxbonddim, TT4& out) {
+  out.clear();
+  const size_t L = A.size();
+  std::vector<double> R(1, 1.0);  // (link_ab, link_an, link_bn)
+  i64 nab = 1, rna = 1, rnb = 1;
+  for (size_t n = 0; n < L; ++n) {
+    const Core4 &a = A[n], &b = B[n];
+    const i64 s = a.d[1], sp = a.d[2], an2 = a.d[3], spp = b.d[2], bn2 = b.d[3];
+    // RA[ab, bn, s, s', an'] = sum_an R[ab, an, bn] A[an, s, s', an']
+    std::vector<double> RA((size_t)(nab * rnb * s * sp * an2));
+    const i64 ncol = s * sp * an2;
+    for (i64 col = 0; col < ncol; ++col)
+      for (i64 bn = 0; bn < rnb; ++bn)
+        for (i64 ab = 0; ab < nab; ++ab) {
+          double acc = 0.0;
+          for (i64 k = 0; k < rna; ++k) acc = acc + R[ab + nab * (k + rna * bn)] * a.v[k + rna * col];
+          RA[ab + nab * (bn + rnb * col)] = acc;
+        }
+    // C[ab, s, s'', an', bn'] = sum_{s', bn} RA[ab, bn, s, s', an'] B[bn, s', s'', bn']
+    const i64 rows = nab * s * spp, cols = an2 * bn2;
+    std::vector<double> C((size_t)(rows * cols));
+    i64 e = 0;
+    for (i64 b2 = 0; b2 < bn2; ++b2)
+      for (i64 a2 = 0; a2 < an2; ++a2)
+        for (i64 ipp = 0; ipp < spp; ++ipp)
+          for (i64 i = 0; i < s; ++i)
+            for (i64 ab = 0; ab < nab; ++ab, ++e) {
+              double acc = 0.0;
+              for (i64 q = 0; q < sp; ++q)
+                for (i64 bn = 0; bn < rnb; ++bn)
+                  acc = acc + RA[ab + nab * (bn + rnb * (i + s * (q + sp * a2)))] *
+                                  b.v[bn + rnb * (q + sp * (ipp + spp * b2))];
+              C[e] = acc;
+            }
+    Core4 core;
+    core.d[0] = nab;
+    core.d[1] = s;
+    core.d[2] = spp;
+    if (n + 1 == L) {
+      core.d[3] = cols;
+      core.v.swap(C);
+      out.push_back(core);
+      break;
+    }
+    std::vector<double> left, right;
+    i64 K = 0;
+    int rc = factorize_lu(C, rows, cols, tolerance, maxbonddim, false, true, left, right, K);
+    if (rc) return rc;
+    core.d[3] = K;
+    core.v.swap(left);
+    out.push_back(core);
+    R.swap(right);
+    nab = K;
+    rna = an2;
+    rnb = bn2;
+  }
+  return ORC_OK;
+}
+
+// compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
+int compress_lu(TT4& tt, double tolerance, i64 maxbonddim, bool normalizeerror) {
+  const size_t L = tt.size();
+  for (size_t l = 0; l + 1 < L; ++l) {
+    Core4 &c = tt[l], &nx = tt[l + 1];
+    const i64 m = c.d[0] * c.d[1] * c.d[2], ncol = c.d[3];
+    std::vector<double> left, right;
+    i64 K = 0;
+    int rc = factorize_lu(c.v, m, ncol, 0.0, TYPEMAX, true, true, left, right, K);
+    if (rc) return rc;
+    const i64 nrest = nx.d[1] * nx.d[2] * nx.d[3];
+    std::vector<double> nt((size_t)(K * nrest));
+    matmul(right.data(), K, nx.v.data(), nx.d[0], nt.data(), K, K, nrest, nx.d[0]);
+    c.v.swap(left);
+    c.d[3] = K;
+    nx.v.swap(nt);
+    nx.d[0] = K;
+  }
+  for (size_t l = L - 1; L >= 2 && l >= 1; --l) {
+    Core4 &c = tt[l], &pv = tt[l - 1];
+    const i64 mrow = c.d[0], ncol = c.d[1] * c.d[2] * c.d[3];
+    std::vector<double> left, right;
+    i64 K = 0;
+    int rc = factorize_lu(c.v, mrow, ncol, tolerance, maxbonddim, false, normalizeerror, left, right, K);
+    if (rc) return rc;
+    const i64 prow = pv.d[0] * pv.d[1] * pv.d[2];
+    std::vector<double> nt((size_t)(prow * K));
+    matmul(pv.v.data(), prow, left.data(), mrow, nt.data(), prow, prow, K, mrow);
+    c.v.swap(right);
+    c.d[0] = K;
+    pv.v.swap(nt);
+    pv.d[3] = K;
+  }
+  return ORC_OK;
+}
+
+TT4 read_tt4(int L, const int64_t* dims, const double* values) {
+  TT4 t((size_t)L);
+  i64 off = 0;
+  for (int b = 0; b < L; ++b) {
+    for (int q = 0; q < 4; ++q) t[b].d[q] = dims[4 * b + q];
+    t[b].v.assign(values + off, values + off + t[b].size());
+    off += t[b].size();
+  }
+  return t;
+}
+
 }  // namespace
 
 // ======================================================================== C ABI
@@ -1146,5 +1328,43 @@ int orc_solve_batch(int64_t nreq, const int32_t* Ls, const int64_t* dims, const 
   for (auto& x : th) x.join();
   return bad.load();
 }
+
+// Tensor-train contraction.  Cores are concatenated in `values` (core b's
+// column-major values after core b-1's); dims[4*b + q] is the size of leg q of
+// core b.  algorithm: 1 naive (recompressed with compress!(:LU) when tolerance
+// > 0 or maxbonddim > 0), 2 zipup with rrLU.  Returns a handle to read with
+// orc_tt4_* and free with orc_tt4_free.
+void* orc_tt4_contract(int L, const int64_t* a_dims, const double* a_values, const int64_t* b_dims,
+                       const double* b_values, int algorithm, double tolerance, int64_t maxbonddim, int* rc) {
+  TT4 a = read_tt4(L, a_dims, a_values), b = read_tt4(L, b_dims, b_values);
+  auto* out = new TT4();
+  *rc = ORC_OK;
+  if (algorithm == 1) {
+    for (int n = 0; n < L; ++n) out->push_back(naive_site(a[n], b[n]));
+    if (tolerance > 0 || maxbonddim > 0) *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, true);
+  } else {
+    *rc = contract_zipup_lu(a, b, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, *out);
+  }
+  return out;
+}
+
+void* orc_tt4_compress(int L, const int64_t* dims, const double* values, double tolerance, int64_t maxbonddim,
+                       int normalizeerror, int* rc) {
+  auto* out = new TT4(read_tt4(L, dims, values));
+  *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, normalizeerror != 0);
+  return out;
+}
+
+int orc_tt4_length(void* h) { return (int)((TT4*)h)->size(); }
+void orc_tt4_dims(void* h, int64_t* dims) {
+  const TT4& t = *(TT4*)h;
+  for (size_t b = 0; b < t.size(); ++b)
+    for (int q = 0; q < 4; ++q) dims[4 * b + q] = t[b].d[q];
+}
+void orc_tt4_core(void* h, int b, double* out) {
+  const Core4& c = (*(TT4*)h)[(size_t)b];
+  std::memcpy(out, c.v.data(), c.v.size() * sizeof(double));
+}
+void orc_tt4_free(void* h) { delete (TT4*)h; }
 
 }  // extern "C"

@@ -25,11 +25,12 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # function values) are built with -fmad=false.
 CU_SOURCES = {
     "step_kernel.cu": ["-fmad=false"],
+    "contract.cu": ["-fmad=false"],
     "peak.cu": [],
     "gather.cu": [],
 }
-CXX_SOURCES = ["engine.cpp", "capi.cpp"]
-HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h"]
+CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp"]
+HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h"]
 
 
 def _newer(target, deps):

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <numeric>
 
+#include "contract.h"
 #include "engine.h"
 
 using namespace tci;
@@ -815,6 +816,134 @@ int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t*
     }
   }
   if (bad) return fail(TCI_ERR_NAN, "lu.L contains NaNs");
+  return 0;
+}
+
+// ---------------------------------------------------------------- tensor-train contraction
+}  // extern "C"
+
+struct tci_tt4 {
+  tci_ctx* ctx = nullptr;
+  TT4 tt;
+};
+
+namespace {
+int upload_tt4(Engine& e, int32_t L, const int64_t* dims, const double* const* cores, TT4& out) {
+  out.cores.clear();
+  for (int32_t b = 0; b < L; ++b) {
+    Tensor4 c;
+    for (int q = 0; q < 4; ++q) c.d[q] = dims[4 * b + q];
+    for (int q = 0; q < 4; ++q)
+      if (c.d[q] < 1 || c.d[q] > INT32_MAX) {
+        out.release(e);
+        return fail(TCI_ERR_DIM, "bad core dimensions");
+      }
+    if (!cores[b]) {
+      out.release(e);
+      return fail(TCI_ERR_ARG, "missing core");
+    }
+    c.p = e.alloc_core(c.elems());
+    if (!c.p) {
+      out.release(e);
+      return fail(TCI_ERR_OOM, "device memory for the cores");
+    }
+    out.cores.push_back(c);
+    cudaError_t ce = cudaMemcpyAsync(c.p, cores[b], c.elems() * sizeof(double), cudaMemcpyHostToDevice, e.stream());
+    if (ce != cudaSuccess) {
+      out.release(e);
+      return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+    }
+  }
+  cudaError_t ce = cudaStreamSynchronize(e.stream());
+  if (ce != cudaSuccess) {
+    out.release(e);
+    return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
+                     const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, double tolerance,
+                     int64_t maxbonddim, tci_tt4** out) {
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (algorithm != TCI_CONTRACT_NAIVE && algorithm != TCI_CONTRACT_ZIPUP)
+    return fail(TCI_ERR_ARG, "Unknown algorithm.");
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  TT4 a, b;
+  int rc = upload_tt4(e, L, a_dims, a_cores, a);
+  if (!rc) rc = upload_tt4(e, L, b_dims, b_cores, b);
+  if (!rc) rc = tt4_check_pair(a, b, true);
+  std::unique_ptr<tci_tt4> res(new tci_tt4());
+  res->ctx = ctx;
+  if (!rc) {
+    if (algorithm == TCI_CONTRACT_NAIVE) {
+      rc = tt4_contract_naive(e, a, b, res->tt);
+      if (!rc && (tolerance > 0 || maxbonddim > 0))
+        rc = tt4_compress_lu(e, res->tt, tolerance, maxbonddim, true);
+    } else {
+      rc = tt4_contract_zipup(e, a, b, tolerance, maxbonddim, res->tt);
+    }
+  }
+  a.release(e);
+  b.release(e);
+  if (rc) {
+    res->tt.release(e);
+    return rc;
+  }
+  *out = res.release();
+  return 0;
+}
+
+int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double tolerance,
+                     int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out) {
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  std::unique_ptr<tci_tt4> res(new tci_tt4());
+  res->ctx = ctx;
+  int rc = upload_tt4(e, L, dims, cores, res->tt);
+  if (!rc) rc = tt4_check(res->tt);
+  if (!rc) rc = tt4_compress_lu(e, res->tt, tolerance, maxbonddim, normalizeerror != 0);
+  if (rc) {
+    res->tt.release(e);
+    return rc;
+  }
+  *out = res.release();
+  return 0;
+}
+
+int32_t tci_tt4_length(const tci_tt4* t) { return (int32_t)t->tt.cores.size(); }
+
+int tci_tt4_dims(const tci_tt4* t, int64_t* dims) {
+  for (size_t b = 0; b < t->tt.cores.size(); ++b)
+    for (int q = 0; q < 4; ++q) dims[4 * b + q] = t->tt.cores[b].d[q];
+  return 0;
+}
+
+int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out) {
+  if (b < 1 || b > (int32_t)t->tt.cores.size()) return fail(TCI_ERR_ARG, "site index out of range");
+  std::lock_guard<std::mutex> lk(t->ctx->mu);
+  Engine& e = t->ctx->eng_ref();
+  const Tensor4& c = t->tt.cores[b - 1];
+  cudaError_t ce = cudaMemcpyAsync(out, c.p, c.elems() * sizeof(double), cudaMemcpyDeviceToHost, e.stream());
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e.stream());
+  if (ce != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  return 0;
+}
+
+int tci_tt4_destroy(tci_tt4* t) {
+  if (!t) return 0;
+  {
+    std::lock_guard<std::mutex> lk(t->ctx->mu);
+    t->tt.release(t->ctx->eng_ref());
+  }
+  delete t;
   return 0;
 }
 

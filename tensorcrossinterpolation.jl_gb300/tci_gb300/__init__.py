@@ -23,6 +23,7 @@ F64P = ctypes.POINTER(ctypes.c_double)
 
 TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
+TCI_CONTRACT_NAIVE, TCI_CONTRACT_ZIPUP = 1, 2
 SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
 FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5}
 
@@ -146,6 +147,15 @@ _SIGNATURES = {
     "tci_convergencecriterion": (ctypes.c_int, [I64P, F64P, I64P, ctypes.c_int64, ctypes.c_double,
                                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]),
     "tci_fp64_peak": (ctypes.c_int, [ctypes.c_size_t, F64P, F64P]),
+    "tci_tt4_contract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
+                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int64,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_tt4_compress": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, ctypes.c_double,
+                                        ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_tt4_length": (ctypes.c_int32, [ctypes.c_void_p]),
+    "tci_tt4_dims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
+    "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
+    "tci_tt4_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -478,6 +488,94 @@ class TensorTrain:
 
     def rank(self):
         return max(self.linkdims())
+
+
+def _tt4_args(cores):
+    cores = [np.asfortranarray(c, dtype=np.float64) for c in cores]
+    dims = np.ascontiguousarray([list(c.shape) for c in cores], dtype=np.int64).reshape(-1)
+    ptrs = (ctypes.c_void_p * len(cores))(*[c.ctypes.data for c in cores])
+    return cores, dims, ptrs
+
+
+def _tt4_fetch(h):
+    lib = load_library()
+    try:
+        L = lib.tci_tt4_length(h)
+        dims = np.zeros(4 * L, np.int64)
+        _check(lib.tci_tt4_dims(h, _p(dims, I64P)))
+        out = []
+        for b in range(L):
+            shape = tuple(int(x) for x in dims[4 * b:4 * b + 4])
+            buf = np.zeros(int(np.prod(shape)), np.float64)
+            _check(lib.tci_tt4_get_core(h, b + 1, _p(buf, F64P)))
+            out.append(buf.reshape(shape, order="F"))
+        return out
+    finally:
+        lib.tci_tt4_destroy(h)
+
+
+def _as_tt4(t, left_operand):
+    """Cores of a tensor train as 4-leg tensors; 3-leg cores get a unit leg
+    (TensorTrain{4}(A, [(1, s...)]) for the left operand, (s..., 1) for the
+    right one, contraction.jl:548-560)."""
+    cores = t.sitetensors if isinstance(t, TensorTrain) else (t.sitetensors() if isinstance(t, TensorCI2) else t)
+    cores = [np.asarray(c, dtype=np.float64) for c in cores]
+    three = all(c.ndim == 3 for c in cores)
+    if three:
+        cores = [c.reshape((c.shape[0], 1, c.shape[1], c.shape[2]) if left_operand else
+                           (c.shape[0], c.shape[1], 1, c.shape[2]), order="F") for c in cores]
+    elif not all(c.ndim == 4 for c in cores):
+        raise ArgumentError(TCI_ERR_ARG, "site tensors must all have 3 or all have 4 legs")
+    return cores, three
+
+
+def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU", ctx=None, f=None):
+    """contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) of
+    tensor trains with 4-leg cores (A's third leg against B's second), or of a
+    3-leg train with a 4-leg one.  algorithm "naive" or "zipup"; factorizations
+    use the rank-revealing LU (method "LU") -- the reference's SVD is not on the
+    device.  Returns a TensorTrain."""
+    if f is not None and algorithm != "TCI":
+        raise TCIError(TCI_ERR_GENERIC, f"{algorithm.capitalize()} contraction implementation cannot contract "
+                       "matrix product with a function. Use algorithm=:TCI instead.")
+    if algorithm == "TCI":
+        raise TCIError(TCI_ERR_GENERIC, "algorithm=:TCI is not available on the device; use 'naive' or 'zipup'")
+    alg = {"naive": TCI_CONTRACT_NAIVE, "zipup": TCI_CONTRACT_ZIPUP}.get(algorithm)
+    if alg is None:
+        raise ArgumentError(TCI_ERR_ARG, f"Unknown algorithm {algorithm}.")
+    if method != "LU":
+        raise ArgumentError(TCI_ERR_ARG, "only method=:LU is available on the device")
+    ctx = ctx or default_context()
+    a, a3 = _as_tt4(A, True)
+    b, b3 = _as_tt4(B, False)
+    if len(a) != len(b):
+        raise ArgumentError(TCI_ERR_ARG, "Cannot contract tensor trains with different length.")
+    a, ad, ap = _tt4_args(a)
+    b, bd, bp = _tt4_args(b)
+    h = ctypes.c_void_p()
+    _check(load_library().tci_tt4_contract(ctx.h, len(a), _p(ad, I64P), ap, _p(bd, I64P), bp, alg,
+                                           float(tolerance), int(maxbonddim or 0), ctypes.byref(h)))
+    cores = _tt4_fetch(h)
+    if a3 or b3:  # TensorTrain{3}(tt, prod.(sitedims(tt)))
+        cores = [c.reshape((c.shape[0], c.shape[1] * c.shape[2], c.shape[3]), order="F") for c in cores]
+    return TensorTrain(cores)
+
+
+def compress(tt, method="LU", tolerance=1e-12, maxbonddim=None, normalizeerror=True, ctx=None):
+    """compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
+    on a train with 4-leg (or 3-leg) cores; returns a new TensorTrain."""
+    if method != "LU":
+        raise ArgumentError(TCI_ERR_ARG, "only method=:LU is available on the device")
+    ctx = ctx or default_context()
+    cores, three = _as_tt4(tt, True)
+    cores, d, ptrs = _tt4_args(cores)
+    h = ctypes.c_void_p()
+    _check(load_library().tci_tt4_compress(ctx.h, len(cores), _p(d, I64P), ptrs, float(tolerance),
+                                           int(maxbonddim or 0), int(bool(normalizeerror)), ctypes.byref(h)))
+    out = _tt4_fetch(h)
+    if three:
+        out = [c.reshape((c.shape[0], c.shape[2], c.shape[3]), order="F") for c in out]
+    return TensorTrain(out)
 
 
 def crossinterpolate2(ValueType, f, localdims, initialpivots=None, ctx=None, **kwargs):
