@@ -279,7 +279,7 @@ def main():
         # end to end: pull every result back to host memory
         st0 = ctx.stats()
         tts = T.tensortrains(res, ctx=ctx)
-        ranks = [tci.rank() for tci in res]
+        ranks = [tt.rank() for tt in tts]
         e2e_s.append(time.perf_counter() - t0)
         nsolves += len(res)
         del res

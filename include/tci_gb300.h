@@ -145,6 +145,9 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims);
  * site by site (each column-major), start at out + out_offsets[i]; offsets must
  * be contiguous (offset[i+1] = offset[i] + sum of solve i's tensor sizes).
  * The TensorTrain(tci) conversion (tensortrain.jl:62-64) for a batch. */
+/* The (r0, d, r1) of every site tensor of n solves, concatenated (3 * sum of
+ * the lengths entries); one call instead of one tci_get_core per site. */
+int tci_get_core_dims_batched(int64_t n, tci_solve* const* solves, int64_t* dims);
 int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
                           const int64_t* out_offsets);
 /* pivoterrors (length *npe) and bonderrors (L-1) (tensorci2.jl:13-16). */

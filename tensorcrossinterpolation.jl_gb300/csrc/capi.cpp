@@ -381,6 +381,20 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
   return 0;
 }
 
+int tci_get_core_dims_batched(int64_t n, tci_solve* const* solves, int64_t* dims) {
+  int64_t q = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const Solve& s = solves[i]->s;
+    if (!s.cores_valid) return fail(TCI_ERR_GENERIC, "site tensors are not available");
+    for (const Core& c : s.cores) {
+      dims[q++] = c.d0;
+      dims[q++] = c.d1;
+      dims[q++] = c.d2;
+    }
+  }
+  return 0;
+}
+
 int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
                           const int64_t* out_offsets) {
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -426,8 +440,8 @@ int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
   std::vector<uint8_t> pts;
   pts.reserve((size_t)np * s->s.L);
   for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
-  // evaluate in chunks so the result record stays modest
-  const int64_t chunk = 1 << 16;
+  // up to 2^20 points per engine step (split into tasks inside co_evaluate)
+  const int64_t chunk = 1 << 20;
   for (int64_t b = 0; b < np; b += chunk) {
     int64_t n = std::min(chunk, np - b);
     std::vector<uint8_t> sub(pts.begin() + b * s->s.L, pts.begin() + (b + n) * s->s.L);
@@ -696,7 +710,7 @@ int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams,
   if (rc) return rc;
   auto piv = to_pivots(points, np, L, s.d, &rc);
   if (rc) return rc;
-  const int64_t chunk = 1 << 16;
+  const int64_t chunk = 1 << 20;
   for (int64_t b = 0; b < np; b += chunk) {
     int64_t n = std::min(chunk, np - b);
     std::vector<uint8_t> pts;

@@ -923,7 +923,25 @@ int Engine::gather_to_host(const std::vector<const double*>& src, const std::vec
   CUDA_TRY(cudaMemcpyAsync(hgat_ + table, dgat_ + table, total * sizeof(double), cudaMemcpyDeviceToHost,
                            stream_));
   CUDA_TRY(cudaStreamSynchronize(stream_));
-  std::memcpy(host_out, hgat_ + table, total * sizeof(double));
+  // staging -> caller's (pageable) buffer: large copies in parallel, which also
+  // spreads the first-touch page faults of a fresh buffer over the threads
+  const char* src0 = hgat_ + table;
+  char* dst0 = (char*)host_out;
+  const size_t bytes = total * sizeof(double);
+  const size_t nthr = bytes >= ((size_t)64 << 20) ? 8 : 1;
+  if (nthr == 1) {
+    std::memcpy(dst0, src0, bytes);
+  } else {
+    const size_t part = (bytes / nthr + 4095) & ~(size_t)4095;
+    std::vector<std::thread> th;
+    for (size_t q = 1; q < nthr; ++q) {
+      const size_t b = q * part;
+      if (b >= bytes) break;
+      th.emplace_back([=] { std::memcpy(dst0 + b, src0 + b, std::min(part, bytes - b)); });
+    }
+    std::memcpy(dst0, src0, std::min(part, bytes));
+    for (auto& t : th) t.join();
+  }
   stats.launches += 1;
   stats.h2d_bytes += (int64_t)table;
   stats.d2h_bytes += (int64_t)(total * sizeof(double));
@@ -1343,24 +1361,37 @@ CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np,
   if (ttout && !s.cores_valid) co_return fail(TCI_ERR_GENERIC, "site tensors are not available");
   std::vector<tci_core_ref> tab;
   int rmax = 1;
-  Req r;
-  r.t.kind = TCI_TASK_EVAL;
-  fill_f(r, s);
-  r.t.m = (int32_t)np;
-  r.t.nl = s.L;
-  r.rows = pts.data();
-  r.rows_bytes = pts.size();
-  if (ttout) {
-    core_table(s, tab, rmax);
-    r.cores = tab.data();
-    r.ncores = s.L;
-    r.t.r = rmax;
+  if (ttout) core_table(s, tab, rmax);
+  // one EVAL task per chunk of points, all in one step, so every SM takes a share
+  const i64 chunk = 4096;
+  const i64 ntask = (np + chunk - 1) / chunk;
+  std::vector<Req> reqs((size_t)ntask);
+  std::vector<Req*> ptrs;
+  for (i64 q = 0; q < ntask; ++q) {
+    Req& r = reqs[(size_t)q];
+    const i64 p0 = q * chunk, n = std::min(chunk, np - p0);
+    r.t.kind = TCI_TASK_EVAL;
+    fill_f(r, s);
+    r.t.m = (int32_t)n;
+    r.t.nl = s.L;
+    r.rows = pts.data() + (size_t)p0 * s.L;
+    r.rows_bytes = (size_t)n * s.L;
+    if (ttout) {
+      r.cores = tab.data();
+      r.ncores = s.L;
+      r.t.r = rmax;
+    }
+    ptrs.push_back(&r);
   }
-  GpuOp op{&e, {&r}};
+  GpuOp op{&e, ptrs};
   co_await op;
   if (op.status) co_return op.status;
-  if (fout) std::memcpy(fout, r.fvals(), (size_t)np * 8);
-  if (ttout) std::memcpy(ttout, r.ttvals(), (size_t)np * 8);
+  for (i64 q = 0; q < ntask; ++q) {
+    const Req& r = reqs[(size_t)q];
+    const i64 p0 = q * chunk;
+    if (fout) std::memcpy(fout + p0, r.fvals(), (size_t)r.t.m * 8);
+    if (ttout) std::memcpy(ttout + p0, r.ttvals(), (size_t)r.t.m * 8);
+  }
   co_return 0;
 }
 

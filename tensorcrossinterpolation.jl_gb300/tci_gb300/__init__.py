@@ -156,6 +156,7 @@ _SIGNATURES = {
     "tci_tt4_dims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
     "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
     "tci_tt4_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_get_core_dims_batched": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), I64P]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -640,18 +641,26 @@ def core_dims(tci):
 def tensortrains(tcis, ctx=None):
     """TensorTrain(tci) for many solves with one device-to-host copy."""
     ctx = ctx or default_context()
-    dims = [core_dims(t) for t in tcis]
-    sizes = [sum(a * b * c for a, b, c in ds) for ds in dims]
-    offs = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int64)
-    out = np.zeros(max(int(sum(sizes)), 1))
     handles = (ctypes.c_void_p * len(tcis))(*[t.h.value if isinstance(t.h, ctypes.c_void_p) else t.h for t in tcis])
-    _check(load_library().tci_get_cores_batched(ctx.h, len(tcis), handles, _p(out, F64P), _p(offs, I64P)))
+    lens = [len(t) for t in tcis]
+    dims = np.zeros(3 * max(sum(lens), 1), np.int64)
+    lib = load_library()
+    _check(lib.tci_get_core_dims_batched(len(tcis), handles, _p(dims, I64P)))
+    d3 = dims[:3 * sum(lens)].reshape(-1, 3)
+    elems = d3.prod(axis=1)
+    core_off = np.concatenate([[0], np.cumsum(elems)]).astype(np.int64)
+    solve_first = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    offs = np.ascontiguousarray(core_off[solve_first[:-1]])
+    out = np.empty(max(int(core_off[-1]), 1))
+    _check(lib.tci_get_cores_batched(ctx.h, len(tcis), handles, _p(out, F64P), _p(offs, I64P)))
     res = []
-    for ds, o in zip(dims, offs):
+    d3l = d3.tolist()
+    col = core_off.tolist()
+    for i in range(len(tcis)):
         cores = []
-        for (a, b, c) in ds:
-            cores.append(out[o:o + a * b * c].reshape((a, b, c), order="F"))
-            o += a * b * c
+        for q in range(int(solve_first[i]), int(solve_first[i + 1])):
+            a, b, c = d3l[q]
+            cores.append(out[col[q]:col[q + 1]].reshape((a, b, c), order="F"))
         res.append(TensorTrain(cores))
     return res
 
