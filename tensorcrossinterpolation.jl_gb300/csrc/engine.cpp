@@ -21,6 +21,12 @@ cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* orde
                             int* counter_dev, int grid, cudaStream_t stream);
 cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
 size_t tci_resident_smem_bytes();
+size_t tci_rrlu_big_smem(int64_t m, int64_t n);
+bool tci_rrlu_big_fits(int64_t m, int64_t n);
+size_t tci_rrlu_big_scratch_bytes(int grid);
+cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, char* res, void* scratch, int m,
+                                int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
+                                cudaStream_t stream);
 cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
                                 int grid, cudaStream_t stream);
 
@@ -954,7 +960,68 @@ static CoTask co_tasks(Engine& e, std::vector<Req*> reqs) {
   co_return op.status;
 }
 
+// A rank-revealing LU of a given matrix large enough to spread over every SM:
+// the multi-CTA kernel instead of one CTA working out of global memory.
+static bool big_eligible(const Req& r, bool resident) {
+  const tci_task& t = r.t;
+  return !resident && t.kind == TCI_TASK_RRLU && (t.ain || r.ain_host) &&
+         (t.post == TCI_POST_FACTORS || t.post == TCI_POST_NONE) && (int64_t)t.m * t.n >= ((int64_t)1 << 18) &&
+         tci_rrlu_big_fits(t.m, t.n);
+}
+
+int Engine::run_big(Req& r) {
+  tci_task& t = r.t;
+  const int64_t m = t.m, n = t.n;
+  const int grid = num_sms;
+  const size_t rb = result_bytes(t);
+  const size_t scratch = tci_rrlu_big_scratch_bytes(grid);
+  // one device block: result record, scratch, input copy (if host), working matrix
+  const size_t in_elems = r.ain_host ? (size_t)(m * n) : 0;
+  const size_t fact_elems = t.post == TCI_POST_FACTORS ? 0 : (size_t)(m * n) + ((size_t)(m + n) * 4 + 7) / 8;
+  const size_t head_bytes = a16(rb) + a16(scratch);
+  const size_t total = head_bytes / 8 + in_elems + (size_t)(m * n) + fact_elems;
+  double* blk = alloc_core(total);
+  if (!blk) return fail(TCI_ERR_OOM, "device memory for the rrLU");
+  char* res = (char*)blk;
+  void* scr = (char*)blk + a16(rb);
+  double* in = blk + head_bytes / 8;
+  double* work = in + in_elems;
+  double* fact = t.post == TCI_POST_FACTORS ? t.core_out : work + (size_t)(m * n);
+  const double* ain = t.ain;
+  int rc = 0;
+  cudaError_t ce = cudaSuccess;
+  if (r.ain_host) {
+    ce = cudaMemcpyAsync(in, r.ain_host, (size_t)(m * n) * 8, cudaMemcpyHostToDevice, stream_);
+    ain = in;
+  }
+  if (ce == cudaSuccess && timing) ce = cudaEventRecord(ev0_, stream_);
+  if (ce == cudaSuccess)
+    ce = tci_rrlu_big_launch(ain, work, fact, res, scr, (int)m, (int)n, t.maxrank, t.kcap, t.leftorth, t.reltol,
+                             t.abstol, grid, stream_);
+  if (ce == cudaSuccess && timing) ce = cudaEventRecord(ev1_, stream_);
+  big_res_.resize(rb);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(big_res_.data(), res, rb, cudaMemcpyDeviceToHost, stream_);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);
+  free_core(blk);
+  if (ce != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  if (timing) {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ev0_, ev1_);
+    stats.kernel_ms += ms;
+  }
+  r.res = big_res_.data();
+  r.res_bytes = rb;
+  stats.launches += 1;
+  stats.tasks += 1;
+  stats.h2d_bytes += (int64_t)(in_elems * 8);
+  stats.d2h_bytes += (int64_t)rb;
+  for (int64_t k = 1; k < r.head()->npivot; ++k) stats.lu_updates += (m - k) * (n - k);
+  if (r.head()->status & TCI_ST_TOO_LARGE) rc = fail(TCI_ERR_TIMEOUT, "multi-CTA rrLU: a grid barrier hit its bound");
+  return rc;
+}
+
 int Engine::run_tasks(std::vector<Req*>& reqs) {
+  if (reqs.size() == 1 && big_eligible(*reqs[0], resident())) return run_big(*reqs[0]);
   CoTask t = co_tasks(*this, reqs);
   return run(t);
 }

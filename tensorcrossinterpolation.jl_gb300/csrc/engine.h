@@ -263,8 +263,10 @@ class Engine {
   double* alloc_core(size_t elems);
   void free_core(double* p);
   void release_cores(Solve& s);
-  // Run a list of tasks outside any solve (rrLU entry points).
+  // Run a list of tasks outside any solve (rrLU entry points).  A single large
+  // rrLU of a given matrix runs on the multi-CTA kernel (run_big).
   int run_tasks(std::vector<Req*>& reqs);
+  int run_big(Req& r);
   // Copy many device arrays to one host buffer: gather on the device into a
   // contiguous staging buffer, then a single device-to-host copy.
   int gather_to_host(const std::vector<const double*>& src, const std::vector<int64_t>& len,
@@ -297,6 +299,7 @@ class Engine {
   BlockPool* dpool_ = nullptr;
   size_t res_smem_ = 0;
   std::vector<Flight> flights_;
+  std::vector<char> big_res_;  // host copy of the last multi-CTA rrLU's result record
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
   std::vector<Req*> pending_;

@@ -46,7 +46,7 @@ constexpr uint64_t SQ_BIG = (uint64_t)(1023 + 500) << 52;    // above: squares m
 
 struct Ctl {
   int task;
-  int r, c, K, stop, kmax, need_exact;
+  int r, c, K, stop, kmax, need_exact, bar_err;
   int status;
   double piv, maxerror, err;
   double red_s[NW + 1];
@@ -94,6 +94,21 @@ struct ArgTrack {
     A = B = 0;
     k = 0xffffffffu;
   }
+  // elements visited in any key order: equal maxima keep the smaller key
+  __device__ __forceinline__ void push_any(double v, uint32_t key) {
+    uint64_t b = abs_bits(v);
+    if (b > NAN_FLOOR) return;
+    b += 1;
+    if (b > A) {
+      B = A;
+      A = b;
+      k = key;
+    } else if (b == A) {
+      k = key < k ? key : k;
+    } else if (b > B) {
+      B = b;
+    }
+  }
   __device__ __forceinline__ void push(double v, uint32_t key) {
     uint64_t b = abs_bits(v);
     if (b > NAN_FLOOR) return;
@@ -126,15 +141,18 @@ __device__ __forceinline__ void track_combine(uint64_t& A, uint32_t& k, uint64_t
 struct ArgBest {
   uint64_t s;  // abs2 bits + 1, 0 = none
   uint32_t key;
+  double val;  // the element at key
   __device__ __forceinline__ void init() {
     s = 0;
     key = 0xffffffffu;
+    val = 0.0;
   }
   __device__ __forceinline__ void consider(double v, uint32_t k) {
     const uint64_t q = (uint64_t)__double_as_longlong(__dmul_rn(v, v)) + 1;
     if (q > s || (q == s && k < key)) {
       s = q;
       key = k;
+      val = v;
     }
   }
 };
@@ -1317,6 +1335,418 @@ __global__ void __launch_bounds__(NT, 1)
   }
 }
 
+// ------------------------------------------------------------ multi-CTA rrLU
+// One rank-revealing LU spread over every SM (cooperative launch, one CTA per
+// SM) for matrices far larger than shared memory: CTA b owns the columns
+// j = b, b + G, ...  Columns are never moved: the column swaps of swapcol!
+// (matrixlu.jl:106-112) are tracked as a permutation (pos: column -> physical
+// position, stor: position -> column), and the argmax key of an element is
+// (physical column << 16) | row, so ties break exactly as in the physically
+// permuted matrix.  Rows are swapped physically inside each CTA's own columns.
+// Per pivot: decision (every CTA, identically), row swap + scaling in own
+// columns, grid barrier, rank-1 update of own trailing columns with the pivot
+// column read from L2, partial argmax, grid barrier, reduction of the partials
+// (every CTA, in the same order).  The arithmetic per element is the same
+// __dmul_rn/__dsub_rn/__ddiv_rn sequence as rrlu_loop, so the factors are
+// bit-identical.
+
+struct BigBar {
+  unsigned int count, gen;
+  int error, pad;
+};
+struct BigPartial {
+  unsigned long long A, B;
+  unsigned int k, nan;
+  double v;  // the element at key k (the next pivot's value)
+};
+
+// ArgTrack that also carries the value at its key (push in any key order).
+struct BigTrack {
+  uint64_t A, B;
+  uint32_t k;
+  double v;
+  __device__ __forceinline__ void init() {
+    A = B = 0;
+    k = 0xffffffffu;
+    v = 0.0;
+  }
+  __device__ __forceinline__ void push(double x, uint32_t key) {
+    uint64_t b = abs_bits(x);
+    if (b > NAN_FLOOR) return;
+    b += 1;
+    if (b > A) {
+      B = A;
+      A = b;
+      k = key;
+      v = x;
+    } else if (b == A) {
+      if (key < k) {
+        k = key;
+        v = x;
+      }
+    } else if (b > B) {
+      B = b;
+    }
+  }
+};
+__device__ __forceinline__ void big_combine(uint64_t& A, uint32_t& k, uint64_t& B, double& v, uint64_t A2,
+                                            uint32_t k2, uint64_t B2, double v2) {
+  if (A2 > A) {
+    B = B2 > A ? B2 : A;
+    A = A2;
+    k = k2;
+    v = v2;
+  } else if (A2 == A) {
+    B = B2 > B ? B2 : B;
+    if (k2 < k) {
+      k = k2;
+      v = v2;
+    }
+  } else if (A2 > B) {
+    B = A2;
+  }
+}
+
+__device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+constexpr long long BIG_BAR_POLLS = 1LL << 24;  // bounded wait of one grid barrier (a few seconds)
+
+// Grid-wide barrier (sense by generation).  Returns false once any CTA has hit
+// the wait bound; every CTA then leaves the factorization.
+__device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, Ctl& ctl) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned g = gen;
+    if (atomicAdd(&bar->count, 1u) == nblocks - 1) {
+      atomicExch(&bar->count, 0u);
+      __threadfence();
+      atomicExch(&bar->gen, g + 1);
+    } else {
+      unsigned sleep_ns = 32;
+      for (long long it = 0; ld_acquire_gpu_u32(&bar->gen) == g; ++it) {
+        if (it > BIG_BAR_POLLS || *(volatile int*)&bar->error) {
+          atomicExch(&bar->error, 1);
+          break;
+        }
+        __nanosleep(sleep_ns);
+        sleep_ns = sleep_ns < 256 ? sleep_ns * 2 : 256;
+      }
+    }
+    gen = g + 1;
+    ctl.bar_err = *(volatile int*)&bar->error;
+  }
+  __syncthreads();
+  return ctl.bar_err == 0;
+}
+
+// The CTA's (A, k, B, v) of a BigTrack; lane 0 of warp 0 gets the result.
+__device__ void block_track(const BigTrack& t, Ctl& ctl, BigPartial* out) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t a = t.A, b = t.B;
+  uint32_t kk = t.k;
+  double v = t.v;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+    const double v2 = __shfl_down_sync(FULL, v, off);
+    big_combine(a, kk, b, v, a2, k2, b2, v2);
+  }
+  if (lane == 0) {
+    ctl.red_u[warp] = a;
+    ctl.red_b[warp] = b;
+    ctl.red_k[warp] = (int)kk;
+    ctl.red_s[warp] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < NW ? ctl.red_u[lane] : 0ULL;
+    b = lane < NW ? ctl.red_b[lane] : 0ULL;
+    kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+    v = lane < NW ? ctl.red_s[lane] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+      const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+      const double v2 = __shfl_down_sync(FULL, v, off);
+      big_combine(a, kk, b, v, a2, k2, b2, v2);
+    }
+    if (lane == 0) {
+      out->A = a;
+      out->B = b;
+      out->k = kk;
+      out->v = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Warp 0 reduces the G partials (same order in every CTA); lane 0 gets it.
+__device__ void big_reduce(const BigPartial* parts, int G, uint64_t& A, uint32_t& k, uint64_t& B, double& v,
+                           unsigned& nan) {
+  const int lane = threadIdx.x & 31;
+  uint64_t a = 0, b = 0;
+  uint32_t kk = 0xffffffffu;
+  double vv = 0.0;
+  unsigned nn = 0;
+  for (int g = lane; g < G; g += 32) {
+    const uint64_t a2 = __ldcg(&parts[g].A), b2 = __ldcg(&parts[g].B);
+    const uint32_t k2 = __ldcg(&parts[g].k);
+    const double v2 = __ldcg(&parts[g].v);
+    nn |= __ldcg(&parts[g].nan);
+    big_combine(a, kk, b, vv, a2, k2, b2, v2);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+    const double v2 = __shfl_down_sync(FULL, vv, off);
+    nn |= __shfl_down_sync(FULL, nn, off);
+    big_combine(a, kk, b, vv, a2, k2, b2, v2);
+  }
+  A = a;
+  k = kk;
+  B = b;
+  v = vv;
+  nan = nn;
+}
+
+struct BigArgs {
+  const double* ain;      // m x n input (column-major)
+  double* A;              // m x n working copy
+  double* fact;           // m x n factors in physical order, then int32 rowperm[m], colperm[n]
+  char* res;              // result record (tci_result_head, rowp[kcap], colp[kcap], diag[kcap])
+  BigPartial* parts;      // gridDim.x partials
+  BigBar* bar;
+  int m, n, kmax, kcap, leftorth;
+  double reltol, abstol;
+};
+
+__global__ void __launch_bounds__(NT, 1) rrlu_big_kernel(BigArgs P) {
+  extern __shared__ __align__(16) char smem[];
+  __shared__ Ctl ctl;
+  const int tid = threadIdx.x, G = gridDim.x, b = blockIdx.x, m = P.m, n = P.n;
+  const bool leftorth = P.leftorth != 0;
+  double* x = (double*)smem;  // pivot column, m
+  int* stor = (int*)(x + m);  // physical position -> column, n
+  int* pos = stor + n;        // column -> physical position, n
+  int* rowperm = pos + n;     // m
+  unsigned gen = 0;
+  for (int j = tid; j < n; j += NT) {
+    stor[j] = j;
+    pos[j] = j;
+  }
+  for (int i = tid; i < m; i += NT) rowperm[i] = i;
+  if (tid == 0) {
+    ctl.maxerror = 0.0;
+    ctl.err = __longlong_as_double(0x7ff8000000000000LL);
+    ctl.stop = 0;
+    P.parts[b].nan = 0;
+  }
+  // copy own columns, first argmax
+  BigTrack bt;
+  bt.init();
+  for (int j = b; j < n; j += G)
+    for (int i = tid; i < m; i += NT) {
+      const double v = P.ain[i + (size_t)j * m];
+      P.A[i + (size_t)j * m] = v;
+      bt.push(v, pack_key(i, j));
+    }
+  block_track(bt, ctl, &P.parts[b]);
+  bool ok = big_barrier(P.bar, G, gen, ctl);
+  int K = 0;
+  tci_result_head* head = (tci_result_head*)P.res;
+  const int kcap = P.kcap;
+  int* rowp = (int*)(P.res + sizeof(tci_result_head));
+  int* colp = (int*)(P.res + sizeof(tci_result_head) + align_up((size_t)kcap * 4, 8));
+  double* diag = (double*)(P.res + sizeof(tci_result_head) + 2 * align_up((size_t)kcap * 4, 8));
+  while (ok) {
+    // ---- the pivot: argmax of abs2 over the trailing block, from the partials
+    if (tid < 32) {
+      uint64_t A, B;
+      uint32_t k;
+      double v;
+      unsigned nn;
+      big_reduce(P.parts, G, A, k, B, v, nn);
+      if (tid == 0) {
+        const uint64_t Mstar = A ? A - 1 : 0;
+        const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
+        const bool close = B != 0 && (B - 1) + 16 >= Mstar;
+        ctl.red_u[NW] = Mstar;
+        ctl.need_exact = (A != 0 && !(safe && !close)) ? 1 : 0;
+        if (A == 0) {  // every element NaN: the scan keeps its start
+          ctl.r = K;
+          ctl.c = K;
+          ctl.piv = __ldcg(&P.A[K + (size_t)stor[K] * m]);
+        } else {
+          ctl.r = (int)(k & 0xffffu);
+          ctl.c = (int)(k >> 16);
+          ctl.piv = v;
+        }
+      }
+    }
+    __syncthreads();
+    if (ctl.need_exact) {  // squares of the elements near the maximum (rare)
+      const uint64_t Mstar = ctl.red_u[NW];
+      ArgBest ab;
+      ab.init();
+      for (int j = b; j < n; j += G) {
+        const int pj = pos[j];
+        if (pj < K) continue;
+        for (int i = K + tid; i < m; i += NT) {
+          const double v = P.A[i + (size_t)j * m];
+          if (near_max(abs_bits(v), Mstar)) ab.consider(v, pack_key(i, pj));
+        }
+      }
+      BigTrack et;
+      et.A = ab.s;
+      et.B = 0;
+      et.k = ab.key;
+      et.v = ab.val;
+      ok = big_barrier(P.bar, G, gen, ctl);  // everyone has read the partials
+      if (!ok) break;
+      block_track(et, ctl, &P.parts[b]);
+      ok = big_barrier(P.bar, G, gen, ctl);
+      if (!ok) break;
+      if (tid < 32) {
+        uint64_t A, B;
+        uint32_t k;
+        double v;
+        unsigned nn;
+        big_reduce(P.parts, G, A, k, B, v, nn);
+        if (tid == 0 && A) {
+          ctl.r = (int)(k & 0xffffu);
+          ctl.c = (int)(k >> 16);
+          ctl.piv = v;
+        }
+      }
+      __syncthreads();
+    }
+    // ---- decision (every CTA computes the same)
+    const int r = ctl.r, cp = ctl.c, cs = stor[cp];
+    const double piv = ctl.piv;
+    if (tid == 0) {
+      const double e = fabs(piv);
+      ctl.err = e;
+      ctl.stop = ((e < P.reltol * ctl.maxerror || e < P.abstol) && K > 0) ? 1 : 0;
+      if (!ctl.stop) {
+        ctl.maxerror = jmax(ctl.maxerror, e);
+        if (b == 0) diag[K] = e;
+        int t = rowperm[K];
+        rowperm[K] = rowperm[r];
+        rowperm[r] = t;
+        const int sk = stor[K];
+        stor[K] = cs;
+        stor[cp] = sk;
+        pos[cs] = K;
+        pos[sk] = cp;
+      }
+    }
+    __syncthreads();
+    if (ctl.stop) break;
+    // ---- swaprow! in own columns, then the scaling (matrixlu.jl:98-104, 114-124)
+    if (r != K)
+      for (int j = b + tid * G; j < n; j += NT * G) {
+        double* col = P.A + (size_t)j * m;
+        const double a = col[K];
+        col[K] = col[r];
+        col[r] = a;
+      }
+    __syncthreads();
+    if (leftorth) {
+      if (cs % G == b) {
+        double* col = P.A + (size_t)cs * m;
+        for (int i = K + 1 + tid; i < m; i += NT) col[i] = __ddiv_rn(col[i], piv);
+      }
+    } else {
+      for (int j = b + tid * G; j < n; j += NT * G)
+        if (pos[j] > K) P.A[K + (size_t)j * m] = __ddiv_rn(P.A[K + (size_t)j * m], piv);
+    }
+    ++K;
+    if (K == P.kmax) break;  // the trailing update after the last pivot is not observable
+    ok = big_barrier(P.bar, G, gen, ctl);
+    if (!ok) break;
+    // ---- rank-1 update of own trailing columns, fused with the argmax
+    const double* xs = P.A + (size_t)cs * m;
+    for (int i = K + tid; i < m; i += NT) x[i] = __ldcg(&xs[i]);
+    __syncthreads();
+    bt.init();
+    for (int j = b; j < n; j += G) {
+      const int pj = pos[j];
+      if (pj < K) continue;
+      double* col = P.A + (size_t)j * m;
+      const double y = col[K - 1];
+      for (int i = K + tid; i < m; i += NT) {
+        const double v = __dsub_rn(col[i], __dmul_rn(x[i], y));
+        col[i] = v;
+        bt.push(v, pack_key(i, pj));
+      }
+    }
+    block_track(bt, ctl, &P.parts[b]);
+    ok = big_barrier(P.bar, G, gen, ctl);
+  }
+  if (!ok) {
+    if (b == 0 && tid == 0) head->status = TCI_ST_TOO_LARGE;
+    return;
+  }
+  __syncthreads();  // the last pivot's scaling (other threads' columns / rows) is in place
+  // ---- NaN scan of L and U (matrixlu.jl:162-169), the factors in physical order
+  int bad = 0;
+  for (int j = b; j < n; j += G) {
+    const int pj = pos[j];
+    const double* col = P.A + (size_t)j * m;
+    double* dst = P.fact + (size_t)pj * m;
+    for (int i = tid; i < m; i += NT) {
+      const double v = col[i];
+      const bool inL = pj < K && i >= pj;
+      const bool inU = i < K && i <= pj;
+      if ((inL || inU) && v != v) bad = 1;
+      dst[i] = v;
+    }
+  }
+  bad = __syncthreads_or(bad);
+  if (tid == 0) P.parts[b].nan = bad;
+  ok = big_barrier(P.bar, G, gen, ctl);
+  if (!ok) {
+    if (b == 0 && tid == 0) head->status = TCI_ST_TOO_LARGE;
+    return;
+  }
+  if (b == 0) {
+    if (tid < 32) {
+      uint64_t A, B;
+      uint32_t k;
+      double v;
+      unsigned nn;
+      big_reduce(P.parts, G, A, k, B, v, nn);
+      if (tid == 0) ctl.status = nn ? 1 : 0;
+    }
+    __syncthreads();
+    int* fr = (int*)(P.fact + (size_t)m * n);
+    for (int i = tid; i < m; i += NT) fr[i] = rowperm[i];
+    for (int j = tid; j < n; j += NT) fr[m + j] = stor[j];
+    for (int q = tid; q < K; q += NT) {
+      rowp[q] = rowperm[q];
+      colp[q] = stor[q];
+    }
+    if (tid == 0) {
+      head->status = ctl.status ? TCI_ST_NAN : 0;
+      head->npivot = K;
+      head->error = K >= min(m, n) ? 0.0 : ctl.err;
+      head->maxabs = 0.0;
+      head->maxabs_nan = 0;
+      head->lut_used = 0;
+    }
+  }
+}
+
 }  // namespace
 
 // Shared-memory budget of one CTA of the step kernel.
@@ -1330,8 +1760,47 @@ cudaError_t tci_step_configure() {
   cudaError_t e = cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)tci_step_smem_bytes());
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(tci_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tci_resident_smem_bytes());
+  e = cudaFuncSetAttribute(tci_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tci_resident_smem_bytes());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(rrlu_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tci_step_smem_bytes());
+}
+
+// Multi-CTA rrLU (rrlu_big_kernel): shared memory per CTA, and whether a matrix
+// qualifies (keys pack 16-bit rows and columns; the CTA keeps the pivot column,
+// both column maps and the row permutation on chip).
+size_t tci_rrlu_big_smem(int64_t m, int64_t n) { return (size_t)(12 * m + 8 * n + 64); }
+bool tci_rrlu_big_fits(int64_t m, int64_t n) {
+  return m >= 1 && n >= 1 && m <= 65535 && n <= 65535 && tci_rrlu_big_smem(m, n) <= tci_step_smem_bytes();
+}
+size_t tci_rrlu_big_scratch_bytes(int grid) { return 64 + (size_t)grid * sizeof(BigPartial); }
+
+// Launch on `grid` CTAs (all co-resident: cooperative launch).  scratch holds
+// the grid barrier and the partials (tci_rrlu_big_scratch_bytes); it is
+// cleared here.  res is a device result record with room for kcap pivots.
+cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, char* res, void* scratch, int m,
+                                int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
+                                cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(scratch, 0, tci_rrlu_big_scratch_bytes(grid), stream);
+  if (e != cudaSuccess) return e;
+  BigArgs a;
+  a.ain = ain;
+  a.A = work;
+  a.fact = fact;
+  a.res = res;
+  a.bar = (BigBar*)scratch;
+  a.parts = (BigPartial*)((char*)scratch + 64);
+  a.m = m;
+  a.n = n;
+  a.kmax = kmax;
+  a.kcap = kcap;
+  a.leftorth = leftorth;
+  a.reltol = reltol;
+  a.abstol = abstol;
+  void* args[] = {(void*)&a};
+  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(grid), dim3(NT), args,
+                                     tci_rrlu_big_smem(m, n), stream);
 }
 
 // Launch the resident kernel: one CTA per SM, all resident at once

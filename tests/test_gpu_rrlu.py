@@ -143,3 +143,43 @@ def test_batched_matches_oracle(T, oracle):
         assert np.array_equal(rows - 1, r["rowpermutation"][:K])
         assert np.array_equal(cols - 1, r["colpermutation"][:K])
         assert err == r["error"]
+
+
+@pytest.mark.parametrize("leftorth", [True, False])
+def test_multi_cta_path(T, oracle, leftorth):
+    """Matrices of 2^18 elements and more run on the multi-CTA kernel (column
+    permutation kept as a map, pivot search over every SM): still bit-exact."""
+    rng = np.random.default_rng(7)
+    m, n, r = 600, 520, 40
+    A = rng.standard_normal((m, r)) @ rng.standard_normal((r, n)) + 1e-9 * rng.standard_normal((m, n))
+    _same(T.rrlu(A, maxrank=60, leftorthogonal=leftorth), oracle.rrlu(A, maxrank=60, leftorthogonal=leftorth))
+    s = 10.0 ** (-np.arange(n) / 40)
+    U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    B = (U * s) @ V.T
+    _same(T.rrlu(B, reltol=1e-10, leftorthogonal=leftorth), oracle.rrlu(B, reltol=1e-10, leftorthogonal=leftorth))
+
+
+def test_multi_cta_ties_and_tiny_magnitudes(T, oracle):
+    rng = np.random.default_rng(8)
+    # many exactly equal |values|: first key in column-major order must win
+    A = rng.integers(-2, 3, size=(530, 500)).astype(np.float64)
+    _same(T.rrlu(A, maxrank=40), oracle.rrlu(A, maxrank=40))
+    # magnitudes where squares underflow: the exact pass decides every pivot
+    B = 1e-170 * rng.standard_normal((520, 520))
+    _same(T.rrlu(B, maxrank=20), oracle.rrlu(B, maxrank=20))
+    # wide and tall shapes
+    C = rng.standard_normal((300, 1200)) @ np.diag(10.0 ** (-np.arange(1200) / 100))
+    _same(T.rrlu(C, reltol=1e-8), oracle.rrlu(C, reltol=1e-8))
+    D = C.T.copy()
+    _same(T.rrlu(D, reltol=1e-8, leftorthogonal=False), oracle.rrlu(D, reltol=1e-8, leftorthogonal=False))
+
+
+def test_multi_cta_nan(T, oracle):
+    A = np.ones((520, 520))
+    A[3, 0] = np.nan
+    with pytest.raises(T.TCIError) as e:
+        T.rrlu(A)
+    assert e.value.code == T.TCI_ERR_NAN
+    with pytest.raises(oracle.OracleError):
+        oracle.rrlu(A)
