@@ -146,6 +146,74 @@ def cpu_baseline(reqs, seconds=20.0):
                       f"oracle on {cores} threads, {dt:.1f} s"}
 
 
+def _best_of(fn, reps=3):
+    best = None
+    out = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = fn()
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return best, out
+
+
+def single_solve_configs(T, ctx, with_cpu=True):
+    """The single-solve configurations, each on the GPU (plain path) and, as the
+    baseline, by the oracle on one host thread: the 8-site Lorentzian, the R = 40
+    quantics-1D function with a 1e6-point evaluation and its sum, the 30-site
+    2-D quantics function and its zipup contraction with a seeded random
+    operator (bond 64, 4 x 4 sites, N(0, 1/64) entries)."""
+    import numpy as np
+
+    O = None
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+    out = {}
+    # 8-site Lorentzian, tol 1e-8, maxbonddim 200
+    kw = dict(tolerance=1e-8, maxbonddim=200, maxiter=20)
+    f = T.DeviceFunction("lorentz")
+    t, (tci, ranks, _) = _best_of(lambda: T.crossinterpolate2(float, f, [10] * 8, ctx=ctx, **kw))
+    c = {"gpu_s": t, "rank": int(tci.rank())}
+    if O:
+        tc, (ref, rr, _) = _best_of(lambda: O.crossinterpolate2([10] * 8, O.F_LORENTZ, [], None, **kw))
+        c.update(cpu_s=tc, cpu_threads=1, same_ranks=list(rr) == list(ranks))
+    out["lorentz8"] = c
+    # quantics 1-D, R = 40, tol 1e-10, maxbonddim 128; 1e6 seeded points
+    kw = dict(tolerance=1e-10, maxbonddim=128, maxiter=20)
+    f = T.DeviceFunction("qtt1d", [0])
+    t, (tci, ranks, _) = _best_of(lambda: T.crossinterpolate2(float, f, [2] * 40, ctx=ctx, **kw))
+    pts = np.random.default_rng(2024).integers(1, 3, size=(1000000, 40))
+    te, vals = _best_of(lambda: tci.evaluate(pts), reps=2)
+    ts, sm = _best_of(lambda: tci.sum(), reps=2)
+    c = {"gpu_s": t, "rank": int(tci.rank()), "eval_points": 1000000, "gpu_eval_s": te,
+         "gpu_eval_points_per_s": 1e6 / te, "gpu_sum_s": ts}
+    if O:
+        tc, (ref, rr, _) = _best_of(lambda: O.crossinterpolate2([2] * 40, O.F_QTT1D, [0], None, **kw))
+        sample = pts[:100000]
+        tce, rv = _best_of(lambda: ref.evaluate(sample), reps=1)
+        c.update(cpu_s=tc, cpu_threads=1, same_ranks=list(rr) == list(ranks), cpu_eval_points_per_s=1e5 / tce,
+                 eval_max_abs_diff=float(np.abs(rv - vals[:100000]).max()))
+    out["quantics1d_R40"] = c
+    # 2-D quantics, 30 sites, d = 4, tol 1e-9, maxbonddim 512, then zipup contraction
+    kw = dict(tolerance=1e-9, maxbonddim=512, maxiter=20)
+    f = T.DeviceFunction("qtt2d")
+    t, (tci, ranks, _) = _best_of(lambda: T.crossinterpolate2(float, f, [4] * 30, ctx=ctx, **kw))
+    c = {"gpu_s": t, "rank": int(tci.rank())}
+    if O:
+        tc, (ref, rr, _) = _best_of(lambda: O.crossinterpolate2([4] * 30, O.F_QTT2D, [], None, **kw), reps=1)
+        c.update(cpu_s=tc, cpu_threads=1, same_ranks=list(rr) == list(ranks))
+    mps = T.tensortrains([tci], ctx=ctx)[0]
+    rng = np.random.default_rng(55)
+    bonds = [1] + [64] * 29 + [1]
+    op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 8.0 for i in range(30)]
+    tz, res = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, ctx=ctx),
+                       reps=1)
+    c.update(zipup_gpu_s=tz, zipup_rank=int(res.rank()))
+    out["quantics2d_30"] = c
+    return out
+
+
 def rrlu_batch_bench(T, ctx, peak_sep, with_cpu=True, reps=3):
     """The batched-rrLU configuration: 4096 matrices (2r)x(2r), r in [8, 128], seed 0,
     reltol 1e-10, maxrank 256, one launch.  Device time from CUDA events around the
@@ -219,6 +287,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
+    ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
     ap.add_argument("--only", default="", help="'rrlu': run only the batched-rrLU configuration")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -322,6 +391,7 @@ def main():
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(make_requests(4096, seed=31), seconds=20.0)
     rrlu_line = None if args.no_rrlu else rrlu_batch_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
+    single = None if args.no_single else single_solve_configs(T, ctx, with_cpu=not args.no_cpu)
 
     line = {
         "metric": METRIC, "value": value * world, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -351,6 +421,8 @@ def main():
         line["cpu_baseline"] = cpu
     if rrlu_line:
         line["rrlu_batch"] = rrlu_line
+    if single:
+        line["single_solves"] = single
     if rank == 0:
         print(json.dumps(line))
 

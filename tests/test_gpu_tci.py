@@ -125,6 +125,22 @@ def test_quantics_1d(T, oracle):
     assert abs(tci.sum() - ref.sum()) <= 1e-12 * abs(ref.sum()) + 1e-15
 
 
+def test_quantics_2d_config(T, oracle):
+    """The 30-site 2-D quantics function (d = 4, tol 1e-9, maxbonddim 512): ranks
+    near 80, Pi up to 320 x 320 (global-memory rrLU)."""
+    kw = dict(tolerance=1e-9, maxbonddim=512, maxiter=20)
+    tci, ranks, _ = T.crossinterpolate2(float, T.DeviceFunction("qtt2d"), [4] * 30, **kw)
+    ref, rranks, _ = oracle.crossinterpolate2([4] * 30, oracle.F_QTT2D, [], None, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    pts = np.random.default_rng(9).integers(1, 5, size=(10000, 30))
+    assert np.allclose(tci.evaluate(pts), ref.evaluate(pts), rtol=0, atol=1e-12)
+    # the sum over 4^30 points of this oscillating function is ~ -199 out of terms
+    # of size 1: cancellation amplifies the last-bit differences of the site
+    # tensors (LU solve order) to ~1e-5 relative in both implementations
+    assert abs(tci.sum() - ref.sum()) <= 1e-4 * abs(ref.sum())
+
+
 def test_batched_equals_alone(T):
     """Each solve gives the same pivots alone and in a batch with others."""
     rng = np.random.default_rng(3)
