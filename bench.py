@@ -157,6 +157,32 @@ def _best_of(fn, reps=3):
     return best, out
 
 
+def large_rrlu_bench(T, ctx, peak_sep, with_cpu=True, n=2048, k=512):
+    """One rank-revealing LU of a dense n x n Gaussian matrix (seed 3) to maxrank k
+    on the multi-CTA kernel; FP64 rate of its rank-1 updates; the oracle on one
+    host thread beside it."""
+    import numpy as np
+
+    A = np.random.default_rng(3).standard_normal((n, n))
+    T.rrlu(A[:600, :600].copy(), maxrank=8, ctx=ctx)  # warm-up
+    ctx.stats(reset=True)
+    t, g = _best_of(lambda: T.rrlu(A, maxrank=k, ctx=ctx), reps=3)
+    st = ctx.stats(reset=True)
+    kern_s = st["kernel_ms"] / 3e3
+    ops = 2.0 * sum((n - q) * (n - q) for q in range(1, k))
+    out = {"workload": f"rrlu of a {n}x{n} N(0,1) matrix (seed 3), maxrank {k}, multi-CTA kernel",
+           "e2e_s": t, "kernel_s": kern_s, "fp64_tflops": ops / kern_s / 1e12,
+           "fp64_frac_of_measured": ops / kern_s / peak_sep}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as O
+
+        tc, r = _best_of(lambda: O.rrlu(A, maxrank=k), reps=1)
+        out.update(cpu_s=tc, cpu_threads=1,
+                   same_pivots=bool(np.array_equal(g.rowpermutation - 1, r["rowpermutation"])))
+    return out
+
+
 def single_solve_configs(T, ctx, with_cpu=True):
     """The single-solve configurations, each on the GPU (plain path) and, as the
     baseline, by the oracle on one host thread: the 8-site Lorentzian, the R = 40
@@ -288,7 +314,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
-    ap.add_argument("--only", default="", help="'rrlu': run only the batched-rrLU configuration")
+    ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -301,6 +327,9 @@ def main():
     peak_sep, peak_fma = T.fp64_peak(ctx)
     if args.only == "rrlu":  # the batched-rrLU configuration alone (one warm-up launch, then --steps)
         print(json.dumps(rrlu_batch_bench(T, ctx, peak_sep, with_cpu=False, reps=max(1, args.steps))))
+        return
+    if args.only == "big-rrlu":  # the multi-CTA rrLU alone
+        print(json.dumps(large_rrlu_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)))
         return
 
     def specs_for(step):
@@ -392,6 +421,7 @@ def main():
         cpu = cpu_baseline(make_requests(4096, seed=31), seconds=20.0)
     rrlu_line = None if args.no_rrlu else rrlu_batch_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
     single = None if args.no_single else single_solve_configs(T, ctx, with_cpu=not args.no_cpu)
+    large = None if args.no_rrlu else large_rrlu_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
 
     line = {
         "metric": METRIC, "value": value * world, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -423,6 +453,8 @@ def main():
         line["rrlu_batch"] = rrlu_line
     if single:
         line["single_solves"] = single
+    if large:
+        line["rrlu_large"] = large
     if rank == 0:
         print(json.dumps(line))
 

@@ -144,6 +144,8 @@ int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
     if (const char* s = std::getenv("TCI_RESIDENT_IDLE_US")) idle_us = std::max(100, std::atoi(s));
     int rc = c->rq->init(device, c->pool[0]->num_sms, idle_us);
     if (rc) return rc;
+    // single solves and the API calls on them run on the resident kernel too
+    c->pool[0]->attach_ring(c->rq.get(), c->hpools[0].get(), c->spools[0].get());
   }
   if (hbm_budget == 0) {
     size_t fr = 0, tot = 0;

@@ -1023,10 +1023,54 @@ int Engine::run_big(Req& r) {
 int Engine::run_tasks(std::vector<Req*>& reqs) {
   if (reqs.size() == 1 && big_eligible(*reqs[0], resident())) return run_big(*reqs[0]);
   CoTask t = co_tasks(*this, reqs);
-  return run(t);
+  return run(t, false);
 }
 
-int Engine::run(CoTask& t) {
+int Engine::run_resident(CoTask& t) {
+  int rc = att_rq_->start();
+  if (rc) return rc;
+  set_resident(att_rq_, att_h_, att_s_);
+  t.h.resume();
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  auto last_progress = now(), last_done = now();
+  while (!t.h.done()) {
+    rc = submit();
+    if (rc) break;
+    bool progressed = false;
+    rc = poll(progressed);
+    if (rc) break;
+    const auto tnow = now();
+    if (progressed) {
+      last_progress = last_done = tnow;
+      continue;
+    }
+    if (!has_flights()) {
+      if (idle()) {
+        rc = fail(TCI_ERR_GENERIC, "engine stalled");
+        break;
+      }
+      continue;
+    }
+    if (tnow - last_progress > std::chrono::milliseconds(2)) {  // the kernel may have left on its idle limit
+      rc = att_rq_->ensure_alive();
+      if (rc) break;
+      last_progress = tnow;
+    }
+    if (tnow - last_done > std::chrono::seconds(120)) {
+      rc = fail(TCI_ERR_TIMEOUT, "resident mode: no task finished for 120 s");
+      break;
+    }
+  }
+  const int src = att_rq_->stop();
+  abandon();
+  set_resident(nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  if (src) return src;
+  return t.h.promise().rc;
+}
+
+int Engine::run(CoTask& t, bool allow_resident) {
+  if (allow_resident && att_rq_ && !resident()) return run_resident(t);
   t.h.resume();
   while (!t.h.done()) {
     if (idle()) return fail(TCI_ERR_GENERIC, "engine stalled");

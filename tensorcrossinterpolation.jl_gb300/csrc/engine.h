@@ -244,7 +244,14 @@ class Engine {
   bool ready() const;
   bool inflight() const { return inflight_; }
   // Drive a single coroutine (and any others already queued) to completion.
-  int run(CoTask& t);
+  // With a ring attached (attach_ring) it runs on the resident kernel, which is
+  // started for the call and stopped at its end; otherwise by batched launches.
+  int run(CoTask& t, bool allow_resident = true);
+  void attach_ring(ResidentQueue* q, BlockPool* host_pool, BlockPool* scratch_pool) {
+    att_rq_ = q;
+    att_h_ = host_pool;
+    att_s_ = scratch_pool;
+  }
 
   // Resident mode: tasks go to the context's ring as soon as they are queued
   // (submit) and each solve resumes as soon as its own tasks are done (poll),
@@ -294,6 +301,9 @@ class Engine {
     std::vector<void*> hblocks, dblocks;
   };
   ResidentQueue* rq_ = nullptr;
+  ResidentQueue* att_rq_ = nullptr;
+  BlockPool *att_h_ = nullptr, *att_s_ = nullptr;
+  int run_resident(CoTask& t);
   BlockPool* hpool_ = nullptr;
   BlockPool* spool_ = nullptr;  // device scratch of this engine's tasks (this thread only)
   BlockPool* dpool_ = nullptr;

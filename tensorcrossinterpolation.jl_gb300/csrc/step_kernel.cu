@@ -259,9 +259,14 @@ __device__ void exact_argmax(const double* A, int lda, int r0, int rows, int c0,
 // ends with a barrier.  One integer reduction decides it unless some element
 // other than the largest |v| lies within 16 ulps of it (its square could tie)
 // or the magnitude is where squares underflow or overflow; then the exact
-// second pass runs.
+// second pass runs.  `decide` runs on the one thread that sets ctl.r / ctl.c,
+// before the final barrier (the next pivot's decision without a barrier of its own).
+struct NoDecide {
+  __device__ void operator()() const {}
+};
+template <class Decide = NoDecide>
 __device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int r0, int rows, int c0, int cols,
-                               Ctl& ctl) {
+                               Ctl& ctl, const Decide& decide = Decide()) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t a = t.A, b = t.B;
   uint32_t k = t.k;
@@ -297,10 +302,12 @@ __device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int 
         ctl.r = r0;
         ctl.c = c0;
         ctl.need_exact = 0;
+        decide();
       } else if (safe && !close) {
         ctl.r = (int)(k & 0xffffu);
         ctl.c = (int)(k >> 16);
         ctl.need_exact = 0;
+        decide();
       } else {
         ctl.need_exact = 1;
       }
@@ -316,6 +323,7 @@ __device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int 
     if (threadIdx.x == 0) {
       ctl.r = s ? (int)(key & 0xffffu) : r0;
       ctl.c = s ? (int)(key >> 16) : c0;
+      decide();
     }
     __syncthreads();
   }
@@ -516,8 +524,86 @@ __device__ ResPtrs res_ptrs(char* resb, const tci_task& T) {
   return p;
 }
 
+// Pivot decision of _optimizerrlu! (matrixlu.jl:150-158) for the pivot at
+// (ctl.r, ctl.c): lu.error, the stopping rule, and the permutation bookkeeping of
+// addpivot!.  One thread.
+__device__ void rr_decide(Ctl& ctl, const double* A, int lda, int K, double reltol, double abstol, double* diag_out,
+                          int* rowperm, int* colperm) {
+  const int r = ctl.r, c = ctl.c;
+  const double piv = A[r + (size_t)c * lda];
+  const double e = fabs(piv);
+  ctl.err = e;
+  const int stop = ((e < reltol * ctl.maxerror || e < abstol) && K > 0) ? 1 : 0;
+  ctl.stop = stop;
+  if (!stop) {
+    ctl.maxerror = jmax(ctl.maxerror, e);
+    ctl.piv = piv;
+    diag_out[K] = e;
+    int t = rowperm[K];
+    rowperm[K] = rowperm[r];
+    rowperm[r] = t;
+    t = colperm[K];
+    colperm[K] = colperm[c];
+    colperm[c] = t;
+  }
+}
+
+// swaprow!(K, R), swapcol!(K, C) and the scaling of addpivot! (matrixlu.jl:98-124)
+// in one pass: new(i, j) = old(pr(i), pc(j)) with pr, pc the two transpositions,
+// divided by the pivot in column K below the diagonal (leftorthogonal) or in row
+// K right of it.  The moved elements form disjoint pairs -- rows K/R outside
+// columns K/C, columns K/C outside rows K/R, and the corners -- and each pair is
+// read and written by one thread.  Ends with a barrier.
+__device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C, double piv, bool leftorth) {
+  const int tid = threadIdx.x;
+  for (int w = tid; w < n + m + 1; w += NT) {
+    if (w < n) {  // row pair (K, j) <-> (R, j)
+      const int j = w;
+      if (j == K || j == C) continue;
+      double* col = A + (size_t)j * lda;
+      if (R != K) {
+        const double a = col[K], b = col[R];
+        col[K] = (!leftorth && j > K) ? __ddiv_rn(b, piv) : b;
+        col[R] = a;
+      } else if (!leftorth && j > K) {
+        col[K] = __ddiv_rn(col[K], piv);
+      }
+    } else if (w < n + m) {  // column pair (i, K) <-> (i, C)
+      const int i = w - n;
+      if (i == K || i == R) continue;
+      double* ck = A + (size_t)K * lda;
+      if (C != K) {
+        double* cc = A + (size_t)C * lda;
+        const double a = ck[i], b = cc[i];
+        ck[i] = (leftorth && i > K) ? __ddiv_rn(b, piv) : b;
+        cc[i] = a;
+      } else if (leftorth && i > K) {
+        ck[i] = __ddiv_rn(ck[i], piv);
+      }
+    } else {  // the corners (K, K), (K, C), (R, K), (R, C)
+      const int rows[2] = {K, R}, cols[2] = {K, C};
+      const int nr = R != K ? 2 : 1, nc = C != K ? 2 : 1;
+      double old[2][2];
+      for (int p = 0; p < nr; ++p)
+        for (int q = 0; q < nc; ++q) old[p][q] = A[rows[p] + (size_t)cols[q] * lda];
+      for (int p = 0; p < nr; ++p)
+        for (int q = 0; q < nc; ++q) {
+          // source of (rows[p], cols[q]) is (rows[p^1], cols[q^1]) where swapped
+          const int sp = nr == 2 ? 1 - p : p, sq = nc == 2 ? 1 - q : q;
+          double v = old[sp][sq];
+          const int i = rows[p], j = cols[q];
+          if ((leftorth && j == K && i > K) || (!leftorth && i == K && j > K)) v = __ddiv_rn(v, piv);
+          A[i + (size_t)j * lda] = v;
+        }
+    }
+  }
+  __syncthreads();
+}
+
 // The rrLU main loop (matrixlu.jl:141-181) on A (m x n, leading dim lda) with the
 // first argmax already in ctl.r/ctl.c.  rowperm/colperm are full permutations.
+// Per pivot: one swap/scale pass, the rank-1 update fused with the next argmax,
+// whose resolving thread also takes the next decision -- three barriers.
 __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
                           bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
   const int tid = threadIdx.x;
@@ -527,69 +613,18 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
     ctl.maxerror = 0.0;
     ctl.err = __longlong_as_double(0x7ff8000000000000LL);
     ctl.kmax = kmax;
+    ctl.stop = 1;
+    if (kmax > 0) rr_decide(ctl, A, lda, 0, reltol, abstol, diag_out, rowperm, colperm);
   }
   __syncthreads();
   int K = 0;
-  while (K < kmax) {
-    TCI_PHASE(0);
-    if (tid == 0) {
-      const int r = ctl.r, c = ctl.c;
-      double piv = A[r + (size_t)c * lda];
-      double e = fabs(piv);
-      ctl.err = e;
-      int stop = ((e < reltol * ctl.maxerror || e < abstol) && K > 0) ? 1 : 0;
-      ctl.stop = stop;
-      if (!stop) {
-        ctl.maxerror = jmax(ctl.maxerror, e);
-        ctl.piv = piv;
-        diag_out[K] = e;
-        int t = rowperm[K];
-        rowperm[K] = rowperm[r];
-        rowperm[r] = t;
-        t = colperm[K];
-        colperm[K] = colperm[c];
-        colperm[c] = t;
-      }
-    }
-    __syncthreads();
+  while (!ctl.stop) {
     TCI_PHASE(1);
-    if (ctl.stop) break;
-    const int r = ctl.r, c = ctl.c;
-    const double piv = ctl.piv;
-    // swaprow! (matrixlu.jl:98-104): whole rows K and r
-    if (r != K)
-      for (int j = tid; j < n; j += NT) {
-        double* col = A + (size_t)j * lda;
-        double a = col[K];
-        col[K] = col[r];
-        col[r] = a;
-      }
-    __syncthreads();
-    TCI_PHASE(2);
-    // swapcol! (matrixlu.jl:106-112) and, for leftorthogonal, A[K+1:end, K] ./= A[K, K]
-    {
-      double* ck = A + (size_t)K * lda;
-      double* cc = A + (size_t)c * lda;
-      for (int i = tid; i < m; i += NT) {
-        double a = ck[i];
-        if (c != K) {
-          double b = cc[i];
-          cc[i] = a;
-          a = b;
-        }
-        if (leftorth && i > K) a = __ddiv_rn(a, piv);
-        ck[i] = a;
-      }
-    }
-    __syncthreads();
-    if (!leftorth) {  // A[K, K+1:end] ./= A[K, K]
-      for (int j = K + 1 + tid; j < n; j += NT) A[K + (size_t)j * lda] = __ddiv_rn(A[K + (size_t)j * lda], piv);
-      __syncthreads();
-    }
+    swap_scale(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth);
     TCI_PHASE(3);
     ++K;
     if (K == kmax) break;  // the trailing update after the last pivot is not observable
-    // A[K:, K:] -= x * y^T fused with the argmax of abs2 for the next pivot
+    // A[K:, K:] -= x * y^T fused with the argmax of abs2 for the next pivot.
     // The trailing block is walked as one column-major sequence so that every
     // lane of every warp has an element (no half-empty warps at column ends).
     ArgTrack at;
@@ -615,7 +650,9 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
       }
     }
     TCI_PHASE(4);
-    argmax_resolve(at, A, lda, K, m - K, K, n - K, ctl);
+    const int Kc = K;
+    argmax_resolve(at, A, lda, K, m - K, K, n - K, ctl,
+                   [&] { rr_decide(ctl, A, lda, Kc, reltol, abstol, diag_out, rowperm, colperm); });
     TCI_PHASE(6);
   }
   if (tid == 0) {
