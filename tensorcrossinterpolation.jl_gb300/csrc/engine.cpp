@@ -481,7 +481,7 @@ int Engine::launch() {
 
   // ---- upload, launch, download
   CUDA_TRY(cudaMemcpyAsync(dblob_, hblob_, blob_total, cudaMemcpyHostToDevice, stream_));
-  const int grid = std::max(1, std::min<int>((int)nt, num_sms));
+  const int grid = std::max(1, std::min<int>((int)nt, num_sms * TCI_CTAS_PER_SM));
   if (timing) CUDA_TRY(cudaEventRecord(ev0_, stream_));
   CUDA_TRY(tci_step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid,
                            stream_));
@@ -654,7 +654,7 @@ void BlockPool::free(void* p) {
 // ---------------------------------------------------------------- resident ring
 int ResidentQueue::init(int dev, int num_sms, int idle_us) {
   device = dev;
-  grid = num_sms;
+  grid = num_sms * TCI_CTAS_PER_SM;
   nslots = 1u << 15;
   mask = nslots - 1;
   CUDA_TRY(cudaSetDevice(dev));
@@ -972,7 +972,7 @@ static bool big_eligible(const Req& r, bool resident) {
 int Engine::run_big(Req& r) {
   tci_task& t = r.t;
   const int64_t m = t.m, n = t.n;
-  const int grid = num_sms;
+  const int grid = num_sms * TCI_CTAS_PER_SM;
   const size_t rb = result_bytes(t);
   const size_t scratch = tci_rrlu_big_scratch_bytes(grid);
   // one device block: result record, scratch, input copy (if host), working matrix

@@ -1189,7 +1189,7 @@ __device__ void run_task(const tci_task& T, const char* blob, char* resb, char* 
   }
 }
 
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     tci_step_kernel(const char* __restrict__ blob, char* __restrict__ resb, const int* __restrict__ order,
                     int ntasks, int* counter, size_t smem_bytes) {
   extern __shared__ __align__(16) char smem[];
@@ -1307,7 +1307,7 @@ __device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmas
 // with one atomic, waits until it is dispatched (or the dispatcher has left:
 // tickets past the last dispatched one are never used), runs the task and
 // publishes the result record to the host.
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     tci_resident_kernel(tci_queue_slot* __restrict__ hslots, uint32_t hmask, tci_resident_state* st,
                         tci_queue_ctl* qc, size_t smem_bytes) {
   if (blockIdx.x == 0) {
@@ -1567,7 +1567,7 @@ struct BigArgs {
   double reltol, abstol;
 };
 
-__global__ void __launch_bounds__(NT, 1) rrlu_big_kernel(BigArgs P) {
+__global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Ctl ctl;
   const int tid = threadIdx.x, G = gridDim.x, b = blockIdx.x, m = P.m, n = P.n;
@@ -1787,7 +1787,10 @@ __global__ void __launch_bounds__(NT, 1) rrlu_big_kernel(BigArgs P) {
 }  // namespace
 
 // Shared-memory budget of one CTA of the step kernel.
-size_t tci_step_smem_bytes() { return 227 * 1024 - 2048; }
+size_t tci_step_smem_bytes() {
+  // 228 KB per SM, 1 KB reserved per CTA, ~2 KB of static shared memory per CTA
+  return (size_t)(228 * 1024) / TCI_CTAS_PER_SM - 3 * 1024 - 1024 * (TCI_CTAS_PER_SM - 1);
+}
 
 // Dynamic shared memory of the resident kernel (its static shared memory holds
 // the task record and the f parameters as well).
@@ -1901,7 +1904,7 @@ constexpr int64_t NOALLOC_SCRATCH_DOUBLES = NOALLOC_MAX_ELEMS + NOALLOC_FACT_DOU
 
 static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
 
-__global__ void __launch_bounds__(NT, 1) rrlu_noalloc_kernel(const tci_task T, char* resb) {
+__global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_noalloc_kernel(const tci_task T, char* resb) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Ctl ctl;
   task_rrlu(T, nullptr, resb, smem, ctl);

@@ -112,4 +112,7 @@ typedef struct tci_resident_state {
   tci_queue_slot ring[TCI_DRING];
 } tci_resident_state;
 
+// Threads of one task CTA, and CTAs resident per SM (the shared-memory budget of
+// a CTA is the SM's divided among them).
 #define TCI_STEP_THREADS 512
+#define TCI_CTAS_PER_SM 1
