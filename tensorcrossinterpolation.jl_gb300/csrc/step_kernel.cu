@@ -554,9 +554,10 @@ __device__ void rr_decide(Ctl& ctl, const double* A, int lda, int K, double relt
 // K right of it.  The moved elements form disjoint pairs -- rows K/R outside
 // columns K/C, columns K/C outside rows K/R, and the corners -- and each pair is
 // read and written by one thread.  Ends with a barrier.
-__device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C, double piv, bool leftorth) {
-  const int tid = threadIdx.x;
-  for (int w = tid; w < n + m + 1; w += NT) {
+// The body for threads t = 0, stride, ... of a group (no barrier).
+__device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n, int K, int R, int C, double piv,
+                                                bool leftorth, int t, int stride) {
+  for (int w = t; w < n + m + 1; w += stride) {
     if (w < n) {  // row pair (K, j) <-> (R, j)
       const int j = w;
       if (j == K || j == C) continue;
@@ -597,7 +598,109 @@ __device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C
         }
     }
   }
+}
+__device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C, double piv, bool leftorth) {
+  swap_scale_body(A, lda, m, n, K, R, C, piv, leftorth, threadIdx.x, NT);
   __syncthreads();
+}
+
+// Trailing blocks of at most this many elements are finished by warp 0 alone:
+// with one warp no CTA barrier is needed per pivot.  Measured on the served
+// stream (whose SITE tasks factor pivot matrices of up to ~32 x 32 to full rank)
+// 1024 gave the highest throughput and 192 the lowest per-task time for 32 x 32
+// matrices with 12 pivots; 512 sits between.
+constexpr int WARP_TAIL = 512;
+
+// rrlu_loop from pivot K on (decision for K already taken, not stopped), warp 0
+// only; same arithmetic and argmax as the CTA path.  Returns the final K on
+// every lane of warp 0.
+__device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax, double reltol, double abstol,
+                              bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
+  const int lane = threadIdx.x & 31;
+  while (true) {
+    swap_scale_body(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth, lane, 32);
+    __syncwarp();
+    ++K;
+    if (K == kmax) break;
+    ArgTrack at;
+    at.init();
+    {
+      const double* x = A + (size_t)(K - 1) * lda;
+      const int rows = m - K;
+      const int total = rows * (n - K);
+      const int sq = 32 / rows, sr = 32 % rows;
+      int jj = lane / rows, ii = lane % rows;
+      for (int e = lane; e < total; e += 32) {
+        const int i = K + ii, j = K + jj;
+        double* col = A + (size_t)j * lda;
+        const double v = __dsub_rn(col[i], __dmul_rn(x[i], col[K - 1]));
+        col[i] = v;
+        at.push(v, pack_key(i, j));
+        ii += sr;
+        jj += sq;
+        if (ii >= rows) {
+          ii -= rows;
+          jj += 1;
+        }
+      }
+    }
+    uint64_t a = at.A, b = at.B;
+    uint32_t k = at.k;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+      const uint32_t k2 = __shfl_down_sync(FULL, k, off);
+      track_combine(a, k, b, a2, k2, b2);
+    }
+    a = __shfl_sync(FULL, a, 0);
+    b = __shfl_sync(FULL, b, 0);
+    k = __shfl_sync(FULL, k, 0);
+    __syncwarp();  // every lane's update is in place before the exact pass / decision
+    const uint64_t Mstar = a ? a - 1 : 0;
+    const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
+    const bool close = b != 0 && (b - 1) + 16 >= Mstar;
+    int r, c;
+    if (a == 0) {
+      r = K;
+      c = K;
+    } else if (safe && !close) {
+      r = (int)(k & 0xffffu);
+      c = (int)(k >> 16);
+    } else {  // squares of the elements near the maximum
+      ArgBest ab;
+      ab.init();
+      const int rows = m - K, total = rows * (n - K);
+      for (int e = lane; e < total; e += 32) {
+        const int i = K + e % rows, j = K + e / rows;
+        const double v = A[i + (size_t)j * lda];
+        if (near_max(abs_bits(v), Mstar)) ab.consider(v, pack_key(i, j));
+      }
+      uint64_t sv = ab.s;
+      uint32_t key = ab.key;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const uint64_t os = __shfl_down_sync(FULL, sv, off);
+        const uint32_t ok = __shfl_down_sync(FULL, key, off);
+        if (os > sv || (os == sv && ok < key)) {
+          sv = os;
+          key = ok;
+        }
+      }
+      sv = __shfl_sync(FULL, sv, 0);
+      key = __shfl_sync(FULL, key, 0);
+      r = sv ? (int)(key & 0xffffu) : K;
+      c = sv ? (int)(key >> 16) : K;
+    }
+    if (lane == 0) {
+      ctl.r = r;
+      ctl.c = c;
+      rr_decide(ctl, A, lda, K, reltol, abstol, diag_out, rowperm, colperm);
+    }
+    __syncwarp();
+    if (ctl.stop) break;
+  }
+  return K;
 }
 
 // The rrLU main loop (matrixlu.jl:141-181) on A (m x n, leading dim lda) with the
@@ -618,8 +721,13 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
   }
   __syncthreads();
   int K = 0;
+  bool tail = false;
   while (!ctl.stop) {
     TCI_PHASE(1);
+    if ((m - K) * (n - K) <= WARP_TAIL) {
+      tail = true;
+      break;
+    }
     swap_scale(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth);
     TCI_PHASE(3);
     ++K;
@@ -655,6 +763,8 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
                    [&] { rr_decide(ctl, A, lda, Kc, reltol, abstol, diag_out, rowperm, colperm); });
     TCI_PHASE(6);
   }
+  if (tail && tid < 32) K = rrlu_warp_tail(A, lda, m, n, K, kmax, reltol, abstol, leftorth, rowperm, colperm,
+                                           diag_out, ctl);
   if (tid == 0) {
     ctl.K = K;
     if (K >= min(m, n)) ctl.err = 0.0;
