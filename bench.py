@@ -308,7 +308,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--batch", type=int, default=10000)
     ap.add_argument("--live", type=int, default=1024)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu", action="store_true")

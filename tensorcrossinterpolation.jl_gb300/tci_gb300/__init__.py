@@ -479,13 +479,32 @@ class TensorTrain:
             if sitetensors[i].shape[-1] != sitetensors[i + 1].shape[0]:
                 raise ArgumentError(TCI_ERR_ARG, f"The tensors at {i + 1} and {i + 2} must have consistent "
                                     "dimensions for a tensor train.")
-        self.sitetensors = [np.asarray(t, dtype=np.float64) for t in sitetensors]
+        self._cores = [np.asarray(t, dtype=np.float64) for t in sitetensors]
+        self._buf = None
+
+    @classmethod
+    def _from_buffer(cls, buf, dims, offsets):
+        """Cores stored one after the other (column-major) in a host buffer; the
+        array views are made on first access."""
+        t = cls.__new__(cls)
+        t._cores = None
+        t._buf, t._dims, t._offs = buf, dims, offsets
+        return t
+
+    @property
+    def sitetensors(self):
+        if self._cores is None:
+            self._cores = [self._buf[o:o + a * b * c].reshape((a, b, c), order="F")
+                           for (a, b, c), o in zip(self._dims, self._offs)]
+        return self._cores
 
     def __len__(self):
-        return len(self.sitetensors)
+        return len(self._dims) if self._cores is None else len(self._cores)
 
     def linkdims(self):
-        return [t.shape[0] for t in self.sitetensors[1:]]
+        if self._cores is None:
+            return [d[0] for d in self._dims[1:]]
+        return [t.shape[0] for t in self._cores[1:]]
 
     def rank(self):
         return max(self.linkdims())
@@ -519,7 +538,7 @@ def _as_tt4(t, left_operand):
     """Cores of a tensor train as 4-leg tensors; 3-leg cores get a unit leg
     (TensorTrain{4}(A, [(1, s...)]) for the left operand, (s..., 1) for the
     right one, contraction.jl:548-560)."""
-    cores = t.sitetensors if isinstance(t, TensorTrain) else (t.sitetensors() if isinstance(t, TensorCI2) else t)
+    cores = t.sitetensors if isinstance(t, (TensorTrain, TensorCI2)) else t
     cores = [np.asarray(c, dtype=np.float64) for c in cores]
     three = all(c.ndim == 3 for c in cores)
     if three:
@@ -653,16 +672,10 @@ def tensortrains(tcis, ctx=None):
     offs = np.ascontiguousarray(core_off[solve_first[:-1]])
     out = np.empty(max(int(core_off[-1]), 1))
     _check(lib.tci_get_cores_batched(ctx.h, len(tcis), handles, _p(out, F64P), _p(offs, I64P)))
-    res = []
     d3l = d3.tolist()
     col = core_off.tolist()
-    for i in range(len(tcis)):
-        cores = []
-        for q in range(int(solve_first[i]), int(solve_first[i + 1])):
-            a, b, c = d3l[q]
-            cores.append(out[col[q]:col[q + 1]].reshape((a, b, c), order="F"))
-        res.append(TensorTrain(cores))
-    return res
+    sf = solve_first.tolist()
+    return [TensorTrain._from_buffer(out, d3l[sf[i]:sf[i + 1]], col[sf[i]:sf[i + 1]]) for i in range(len(tcis))]
 
 
 def serve(specs, arrival, max_live=0, ctx=None):

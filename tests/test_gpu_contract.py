@@ -74,6 +74,20 @@ def test_mpo_mps(T, oracle, algorithm):
     assert np.allclose(got[:, 0], ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
 
 
+def test_contract_with_tci_result(T, oracle):
+    """contract(TT4 operator, TensorCI2) -> TT3, the MPO-MPS case of the 2-D
+    quantics configuration at a small size."""
+    rng = np.random.default_rng(17)
+    tci, _, _ = T.crossinterpolate2(float, T.DeviceFunction("qtt2d"), [4] * 6, tolerance=1e-9, maxbonddim=64)
+    bonds = [1, 3, 3, 3, 3, 3, 1]
+    op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 2.0 for i in range(6)]
+    ab = T.contract(op, tci, algorithm="zipup", tolerance=1e-12)
+    v4 = [c.reshape(c.shape[0], 4, 1, c.shape[2], order="F") for c in tci.sitetensors]
+    ref = (oracle.tt4_full(op) @ oracle.tt4_full(v4))[:, 0]
+    got = oracle.tt4_full([c.reshape(c.shape[0], c.shape[1], 1, c.shape[2], order="F") for c in ab.sitetensors])
+    assert np.allclose(got[:, 0], ref, rtol=1e-9, atol=1e-11 * np.abs(ref).max())
+
+
 def test_contract_errors_like_reference(T):
     rng = np.random.default_rng(16)
     a = _rand_tt(rng, [1, 2, 2, 1], [2] * 3, [3] * 3)
