@@ -146,6 +146,41 @@ def cpu_baseline(reqs, seconds=20.0):
                       f"oracle on {cores} threads, {dt:.1f} s"}
 
 
+def dist_setup(world):
+    """torch.distributed for N > 1 replicas (one process per GPU): NCCL when the
+    ranks have GPUs, else gloo.  Returns None for a single process."""
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+
+    if not dist.is_initialized():
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    return dist
+
+
+def max_over_ranks(values, dist):
+    """Elementwise maximum of a list of floats over all ranks (the slowest replica
+    sets the whole-job time)."""
+    if dist is None:
+        return list(values)
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor(list(values), dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.cpu()]
+
+
+def barrier(dist):
+    if dist is not None:
+        import torch
+
+        if dist.get_backend() == "nccl":
+            torch.cuda.synchronize()
+        dist.barrier()
+
+
 def _best_of(fn, reps=3):
     best = None
     out = None
@@ -354,7 +389,12 @@ def main():
         _, specs = specs_for(s)
         T.crossinterpolate2_batched(specs, max_live=args.live, ctx=ctx)
 
-    # timed: device throughput (events on the engine stream around each batch)
+    # timed: device throughput (events on the engine stream around each batch);
+    # replicas: barrier + device sync on both sides, the slowest rank's time
+    dist = dist_setup(world)
+    barrier(dist)
+    if tstream is not None:
+        torch.cuda.synchronize()
     clocks = ClockSampler()
     clocks.start()
     ctx.stats(reset=True)
@@ -381,12 +421,16 @@ def main():
         e2e_s.append(time.perf_counter() - t0)
         nsolves += len(res)
         del res
+    if tstream is not None:
+        torch.cuda.synchronize()
+    barrier(dist)
     st = ctx.stats(reset=True)
     clk = clocks.stop()
     kernel_ms = st["kernel_ms"]
     total_dev_s = sum(dev_ms) / 1e3 if dev_ms else sum(e2e_s)
-    value = nsolves / total_dev_s
-    e2e = nsolves / sum(e2e_s)
+    total_dev_s, total_e2e_s = max_over_ranks([total_dev_s, sum(e2e_s)], dist)
+    value = nsolves * world / total_dev_s
+    e2e = nsolves * world / total_e2e_s
     # FP64 operations: the rank-1 updates (multiply + subtract), f from tables
     # (one operation per element) and f evaluated directly
     ops = (2.0 * st["lu_updates"] + 1.0 * st["feval_tabulated"] +
@@ -406,7 +450,7 @@ def main():
     plain = nplain / (time.perf_counter() - t0)
 
     # latency under Poisson arrivals at 80% of the measured batched rate
-    lam = 0.8 * e2e
+    lam = 0.8 * e2e / world  # this replica's share
     rng = np.random.default_rng(77)
     nserve = min(2000, max(200, int(lam * 5)))
     reqs_s, specs_s = specs_for(5555)
@@ -424,7 +468,7 @@ def main():
     large = None if args.no_rrlu else large_rrlu_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
 
     line = {
-        "metric": METRIC, "value": value * world, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": (total_dev_s * 1e3) / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"served-stream family: {args.batch} crossinterpolate2 requests per step "
@@ -433,11 +477,11 @@ def main():
                    "max_live": args.live,
                    "global_batch": args.batch, "parallelism": f"replicas{args.gpus}",
                    "l2": "inputs are per-step index lists; Pi matrices stay on chip"},
-        "e2e": {"value": e2e * world, "unit": UNIT, "h2d_bytes_per_step": st["h2d_bytes"] // max(args.steps, 1),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": st["h2d_bytes"] // max(args.steps, 1),
                 "d2h_bytes_per_step": st["d2h_bytes"] // max(args.steps, 1)},
         "gpu_launches": st["launches"],
         "plain_solves_per_s": plain,
-        "batched_over_plain": e2e / plain,
+        "batched_over_plain": e2e / world / plain,
         "serve_p50_ms": float(np.percentile(lat, 50) * 1e3), "serve_p99_ms": float(np.percentile(lat, 99) * 1e3),
         "serve_rate_per_s": lam,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
