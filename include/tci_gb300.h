@@ -49,7 +49,8 @@ enum {
   TCI_F_SERVED = 2,  /* "served" : 1/(1+a v.v) + b exp(-g|v-c|^2)  params [a, b, g, c_1..c_L] */
   TCI_F_QTT1D = 3,   /* "qtt1d"  : quantics 1-D                    params [kind]             */
   TCI_F_QTT2D = 4,   /* "qtt2d"  : quantics 2-D, d = 4             params []                 */
-  TCI_F_DENSE = 5    /* "dense"  : table lookup                    params [L, strides, data] */
+  TCI_F_DENSE = 5,   /* "dense"  : table lookup                    params [L, strides, data] */
+  TCI_F_PRODUCT = 6  /* "product": C prod_n t[n, v_n] (integrate)  params [L, D, C, log|t|, t<0] */
 };
 
 /* Sweep strategies (sweepstrategies.jl:1-6). */

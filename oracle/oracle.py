@@ -13,8 +13,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-F_LORENTZ, F_SERVED, F_QTT1D, F_QTT2D, F_DENSE = 1, 2, 3, 4, 5
-FUNCTION_IDS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5}
+F_LORENTZ, F_SERVED, F_QTT1D, F_QTT2D, F_DENSE, F_PRODUCT = 1, 2, 3, 4, 5, 6
+FUNCTION_IDS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5, "product": 6}
 
 I64P = ctypes.POINTER(ctypes.c_int64)
 F64P = ctypes.POINTER(ctypes.c_double)

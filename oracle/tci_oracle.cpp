@@ -52,7 +52,7 @@ double jmax(double a, double b) {
 }
 
 // ---------------------------------------------------------------- functions
-enum { F_LORENTZ = 1, F_SERVED = 2, F_QTT1D = 3, F_QTT2D = 4, F_DENSE = 5 };
+enum { F_LORENTZ = 1, F_SERVED = 2, F_QTT1D = 3, F_QTT2D = 4, F_DENSE = 5, F_PRODUCT = 6 };
 
 struct Func {
   int fid = 0;
@@ -100,6 +100,16 @@ struct Func {
         double dx = x - 0.5, dy = y - 0.5;
         double g = tci_exp(-(dx * dx + dy * dy) / 0.01);
         return g * tci_cos(1256.6370614359173 * (x + y));
+      }
+      case F_PRODUCT: {  // C (-1)^(sum neg) exp(sum q); q are multiples of 2^-40, sums exact
+        const i64 D = (i64)params[1];
+        double q = 0.0, ng = 0.0;
+        for (int p = 0; p < L; ++p) {
+          q = q + params[3 + p * D + (v[p] - 1)];
+          ng = ng + params[3 + L * D + p * D + (v[p] - 1)];
+        }
+        const double e = params[2] * tci_exp(q);
+        return (((long long)ng) & 1) ? -e : e;
       }
       case F_DENSE: {  // params = [L, strides..., values...]
         i64 off = 0;

@@ -107,7 +107,7 @@ int tci_f_lookup(const char* name, int* fid) {
     const char* n;
     int id;
   } tab[] = {{"lorentz", TCI_F_LORENTZ}, {"served", TCI_F_SERVED}, {"qtt1d", TCI_F_QTT1D},
-             {"qtt2d", TCI_F_QTT2D},     {"dense", TCI_F_DENSE}};
+             {"qtt2d", TCI_F_QTT2D},     {"dense", TCI_F_DENSE}, {"product", TCI_F_PRODUCT}};
   for (auto& e : tab)
     if (std::strcmp(e.n, name) == 0) {
       *fid = e.id;

@@ -1123,7 +1123,7 @@ i64 solve_rank(const Solve& s) {
 int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
                int64_t nparams, const int64_t*, int64_t) {
   if (L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
-  if (fid < TCI_F_LORENTZ || fid > TCI_F_DENSE) return fail(TCI_ERR_ARG, "unknown function id");
+  if (fid < TCI_F_LORENTZ || fid > TCI_F_PRODUCT) return fail(TCI_ERR_ARG, "unknown function id");
   s.L = L;
   s.d.assign(localdims, localdims + L);
   for (int x : s.d)
@@ -1135,6 +1135,13 @@ int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double*
   if (fid == TCI_F_QTT1D)
     for (int x : s.d)
       if (x != 2) return fail(TCI_ERR_ARG, "qtt1d needs local dimension 2");
+  if (fid == TCI_F_PRODUCT) {
+    if (nparams < 3 || (int)params[0] != L) return fail(TCI_ERR_ARG, "product f parameter block");
+    const int D = (int)params[1];
+    for (int x : s.d)
+      if (x > D) return fail(TCI_ERR_ARG, "product f tables narrower than a local dimension");
+    if (nparams < 3 + 2 * (int64_t)L * D) return fail(TCI_ERR_ARG, "product f tables too short");
+  }
   if (fid == TCI_F_DENSE) {
     if (nparams < 1 + L || (int)params[0] != L) return fail(TCI_ERR_ARG, "dense f parameter block");
     int64_t total = 1;

@@ -20,6 +20,7 @@ enum {
   TCI_F_QTT1D = 3,    // quantics 1-D, x = sum_i b_i 2^-i
   TCI_F_QTT2D = 4,    // quantics 2-D, d = 4: x bit = low bit, y bit = high bit
   TCI_F_DENSE = 5,    // table lookup: f(v) = T[v] (column-major over localdims)
+  TCI_F_PRODUCT = 6,  // f(v) = C * prod_n t[n, v_n] from log|t| and sign tables
 };
 
 // Parameter layouts (double array `params`):
@@ -30,6 +31,10 @@ enum {
 //                     kind 2: exp(-x) + 1e-4 exp(-2x)
 //   QTT2D  : []       exp(-((x-.5)^2 + (y-.5)^2)/0.01) cos(400 pi (x + y))
 //   DENSE  : [L, stride_1 .. stride_L, values ...]
+//   PRODUCT: [L, D, C, q[L x D], neg[L x D]] (site-major): q = log|t| rounded to a
+//            multiple of 2^-40, neg = 1 where t < 0; f = C (-1)^(sum neg) exp(sum q).
+//            The rounding makes the sums exact, so f does not depend on how a
+//            multi-index is split into row and column parts.
 
 #define TCI_TWO_THOUSAND_PI 6283.185307179587   /* 2000*pi rounded to double */
 #define TCI_FOUR_HUNDRED_PI 1256.6370614359173  /* 400*pi rounded to double  */
@@ -56,6 +61,11 @@ TCI_HD void tci_f_term(int fid, const double* params, int site, int v,
     } break;
     case TCI_F_DENSE: {
       *acc0 = *acc0 + (double)v * params[1 + site];
+    } break;
+    case TCI_F_PRODUCT: {
+      const int L = (int)params[0], D = (int)params[1];
+      *acc0 = *acc0 + params[3 + site * D + v];
+      *acc1 = *acc1 + params[3 + L * D + site * D + v];
     } break;
     default: break;
   }
@@ -134,6 +144,10 @@ TCI_HD double tci_f_finish(int fid, const double* params, int nparams, double ac
     case TCI_F_DENSE: {
       int L = (int)params[0];
       return params[1 + L + (int64_t)acc0];
+    }
+    case TCI_F_PRODUCT: {
+      const double e = params[2] * tci_exp(acc0);
+      return (((long long)acc1) & 1) ? -e : e;
     }
     default:
       return 0.0;

@@ -25,7 +25,7 @@ TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
 TCI_CONTRACT_NAIVE, TCI_CONTRACT_ZIPUP = 1, 2
 SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
-FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5}
+FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5, "product": 6}
 
 
 class TCIError(RuntimeError):
@@ -596,6 +596,65 @@ def compress(tt, method="LU", tolerance=1e-12, maxbonddim=None, normalizeerror=T
     if three:
         out = [c.reshape((c.shape[0], c.shape[2], c.shape[3]), order="F") for c in out]
     return TensorTrain(out)
+
+
+class ProductIntegrand:
+    """An integrand f(x) = prod_n g_n(x_n) for integrate(): `g` is one callable
+    used at every coordinate, or a list of one callable per coordinate.  It is
+    evaluated on the host at the quadrature nodes only; the interpolation of the
+    integrand runs on the device (registered function "product")."""
+
+    def __init__(self, g):
+        self.g = g
+
+    def factor(self, n):
+        return self.g[n] if isinstance(self.g, (list, tuple)) else self.g
+
+
+def product_function(tables, C=1.0):
+    """DeviceFunction f(v) = C * prod_n tables[n][v_n] (tables: L x D).  log|t| is
+    rounded to a multiple of 2^-40 so that the device sums it exactly."""
+    t = np.asarray(tables, dtype=np.float64)
+    L, D = t.shape
+    with np.errstate(divide="ignore"):
+        q = np.log(np.abs(t))
+    q = np.where(q < -745.0, -np.inf, np.round(q * 2.0 ** 40) / 2.0 ** 40)
+    finite = np.abs(q[np.isfinite(q)])
+    if finite.size and L * finite.max() >= 8192.0:
+        raise ArgumentError(TCI_ERR_ARG, "product f: factors too far from 1 for exact log sums")
+    neg = (t < 0).astype(np.float64)
+    return DeviceFunction("product", np.concatenate([[L, D, C], q.reshape(-1), neg.reshape(-1)]))
+
+
+def integrate(ValueType, f, a, b, GKorder=15, ctx=None, **kwargs):
+    """integrate(ValueType, f, a, b; GKorder, kwargs...) (integration.jl:20-58):
+    Gauss--Kronrod nodes per coordinate, crossinterpolate2 of
+    F(i) = prod_n w[n, i_n] * f(x(i)) * GKorder^N with nsearchglobalpivot = 10,
+    then sum(tci) / GKorder^N.  f must be a ProductIntegrand."""
+    from .quadrature import kronrod
+
+    if ValueType not in (float, np.float64, "Float64"):
+        raise ArgumentError(TCI_ERR_ARG, "only Float64 is supported")
+    if GKorder % 2 == 0:
+        raise TCIError(TCI_ERR_GENERIC, "Gauss--Kronrod order must be odd, e.g. 15 or 61.")
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    if a.size != b.size:
+        raise TCIError(TCI_ERR_GENERIC, "Integral bounds must have the same dimensionality, but got "
+                       f"{a.size} lower bounds and {b.size} upper bounds.")
+    if not isinstance(f, ProductIntegrand):
+        raise ArgumentError(TCI_ERR_ARG, "integrate on the device needs a ProductIntegrand "
+                            "(f(x) = prod_n g_n(x_n))")
+    x1, w1, _ = kronrod(GKorder // 2)
+    N = a.size
+    nodes = (b - a)[:, None] * (x1[None, :] + 1.0) / 2.0 + a[:, None]
+    weights = (b - a)[:, None] * w1[None, :] / 2.0
+    norm = float(GKorder) ** N
+    tables = np.array([[weights[n, i] * f.factor(n)(nodes[n, i]) for i in range(x1.size)] for n in range(N)])
+    kw = dict(nsearchglobalpivot=10)
+    kw.update(kwargs)
+    tci, _, _ = crossinterpolate2(ValueType, product_function(tables, norm), [x1.size] * N, ctx=ctx, **kw)
+    return tci.sum() / norm
 
 
 def crossinterpolate2(ValueType, f, localdims, initialpivots=None, ctx=None, **kwargs):

@@ -1,8 +1,9 @@
 """Extract the reference's own known-answer data for the TCI2 path into JSON.
 
 Reads the literal matrices of TensorCrossInterpolation.jl's tests as text
-(test/test_matrixlu.jl, test/test_matrixluci.jl) and records, beside each, the
-assertion the reference test makes about it.  Run in a checkout that has the
+(test/test_matrixlu.jl, test/test_matrixluci.jl, and the polynomial coefficients
+of test/test_integration.jl) and records, beside each, the assertion the
+reference test makes about it.  Run in a checkout that has the
 reference:
 
     python tests/golden/make_golden.py /path/to/TensorCrossInterpolation.jl
@@ -96,8 +97,14 @@ def main(ref):
                  "maxbonddim": 2, "ncheck": 3, "expect": True},
             ]},
     }
+    integ_text = open(os.path.join(ref, "test", "test_integration.jl")).read()
+    m = re.search(r"coefficients\s*=\s*\[(.*?)\]", integ_text, re.S)
+    coeffs = [float(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+    integration = {"source": "test/test_integration.jl:6-28", "coefficients": coeffs, "N": 5,
+                   "expect": "integrate(f, a, b) ≈ prod(P(b) - P(a)) for f(x) = prod(p.(x)), P' = p; "
+                             "[0,1]^5 and a random box"}
     out = {"reference": "TensorCrossInterpolation.jl 0.9.19", "rrlu": cases, "rrlu_lowrank": lowrank,
-           "luci": luci_case, "tci2": tci}
+           "luci": luci_case, "tci2": tci, "integration": integration}
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")
     with open(dst, "w") as fh:
         json.dump(out, fh, indent=1)
