@@ -707,8 +707,12 @@ __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax,
 // first argmax already in ctl.r/ctl.c.  rowperm/colperm are full permutations.
 // Per pivot: one swap/scale pass, the rank-1 update fused with the next argmax,
 // whose resolving thread also takes the next decision -- three barriers.
+// xy: optional shared-memory copy (m + n doubles) of the pivot column and row
+// for a matrix in global memory, so that each element of the update costs one
+// load and one store.
 __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
-                          bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
+                          bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl,
+                          double* xy = nullptr) {
   const int tid = threadIdx.x;
   const int kmax = min(maxrank, min(m, n));
   if (tid == 0) {
@@ -737,11 +741,32 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
     // lane of every warp has an element (no half-empty warps at column ends).
     ArgTrack at;
     at.init();
-    {
+    const int rows = m - K;
+    const long long total = (long long)rows * (n - K);
+    const int sq = NT / rows, sr = NT % rows;  // stride NT as (columns, rows)
+    if (xy) {
+      // x = A[K:, K-1] and y = A[K-1, K:] on chip, indexed from K
+      double* xs = xy;
+      double* ys = xy + m;
+      for (int i = K + tid; i < m; i += NT) xs[i] = A[i + (size_t)(K - 1) * lda];
+      for (int j = K + tid; j < n; j += NT) ys[j] = A[(K - 1) + (size_t)j * lda];
+      __syncthreads();
+      int jj = tid / rows, ii = tid % rows;
+      for (long long e = tid; e < total; e += NT) {
+        const int i = K + ii, j = K + jj;
+        double* col = A + (size_t)j * lda;
+        const double v = __dsub_rn(col[i], __dmul_rn(xs[i], ys[j]));
+        col[i] = v;
+        at.push(v, pack_key(i, j));
+        ii += sr;
+        jj += sq;
+        if (ii >= rows) {
+          ii -= rows;
+          jj += 1;
+        }
+      }
+    } else {
       const double* x = A + (size_t)(K - 1) * lda;
-      const int rows = m - K;
-      const long long total = (long long)rows * (n - K);
-      const int sq = NT / rows, sr = NT % rows;  // stride NT as (columns, rows)
       int jj = tid / rows, ii = tid % rows;
       for (long long e = tid; e < total; e += NT) {
         const int i = K + ii, j = K + jj;
@@ -872,7 +897,7 @@ struct SmemCursor {
 };
 
 // ---------------------------------------------------------------- RRLU task
-__device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
+__device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl, size_t smem_bytes) {
   const int m = T.m, n = T.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   ResPtrs rp = res_ptrs(resb, T);
   SmemCursor cur{smem};
@@ -928,7 +953,9 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   if (tid == 0) ctl.status = 0;
   argmax_resolve(am, A, lda, 0, m, 0, n, ctl);
   const bool leftorth = T.leftorth != 0;
-  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl);
+  double* xy = nullptr;
+  if (!T.smem_mode && (size_t)(cur.p - smem) + (size_t)(m + n) * 8 <= smem_bytes) xy = (double*)cur.take((size_t)(m + n) * 8);
+  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl, xy);
   const int K = ctl.K;
   int nan = lu_has_nan(A, lda, m, n, K, ctl);
   if (T.post == TCI_POST_LEFT && !nan) post_left(A, lda, m, n, K, leftorth, rowperm, T.core_out);
@@ -1289,7 +1316,7 @@ __device__ void task_sum(const tci_task& T, const char* blob, char* resb, char* 
 __device__ void run_task(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl,
                          size_t smem_bytes) {
   switch (T.kind) {
-    case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl); break;
+    case TCI_TASK_RRLU: task_rrlu(T, blob, resb, smem, ctl, smem_bytes); break;
     case TCI_TASK_SITE: task_site(T, blob, resb, smem, ctl, smem_bytes); break;
     case TCI_TASK_CORE: task_core(T, blob, resb, smem, ctl); break;
     case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
@@ -2017,7 +2044,7 @@ static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLE
 __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_noalloc_kernel(const tci_task T, char* resb) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Ctl ctl;
-  task_rrlu(T, nullptr, resb, smem, ctl);
+  task_rrlu(T, nullptr, resb, smem, ctl, 0);
 }
 
 // Copies the result record and the factors from the scratch array to the

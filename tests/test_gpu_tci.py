@@ -253,3 +253,33 @@ def test_resident_relaunch_after_idle(T, monkeypatch):
         f, dims, kw = specs[i]
         ta, _, _ = T.crossinterpolate2(float, f, dims, ctx=ctx, **kw)
         assert ta.rank() == rank[i]
+
+
+OPTION_CASES = [
+    dict(sweepstrategy="forward"),
+    dict(sweepstrategy="backward"),
+    dict(strictlynested=True),
+    dict(normalizeerror=False, tolerance=1e-6),
+    dict(maxnglobalpivot=0),
+    dict(nsearchglobalpivot=0),
+    dict(checkconvglobalpivot=False, ncheckhistory=1),
+    dict(tolmarginglobalsearch=1.0, nsearchglobalpivot=8, maxnglobalpivot=2),
+    dict(maxbonddim=5, maxiter=6),
+    dict(seed=12345),
+]
+
+
+@pytest.mark.parametrize("opts", OPTION_CASES, ids=[",".join(f"{k}={v}" for k, v in o.items()) for o in OPTION_CASES])
+def test_optimize_options_parity(T, oracle, opts):
+    """The optimize! keyword arguments (tensorci2.jl:700-720) change the sweeps the
+    same way on both sides: identical ranks history and pivot sets."""
+    rng = np.random.default_rng(31)
+    L, d = 6, 5
+    prm = _served(rng, L, d)
+    kw = dict(tolerance=1e-9, maxiter=12)
+    kw.update(opts)
+    tci, ranks, errs = T.crossinterpolate2(float, T.DeviceFunction("served", prm), [d] * L, **kw)
+    ref, rranks, rerrs = oracle.crossinterpolate2([d] * L, oracle.F_SERVED, prm, None, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    assert np.allclose(errs, rerrs, rtol=1e-12, atol=0)
