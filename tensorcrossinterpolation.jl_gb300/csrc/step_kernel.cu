@@ -605,11 +605,12 @@ __device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C
 }
 
 // Trailing blocks of at most this many elements are finished by warp 0 alone:
-// with one warp no CTA barrier is needed per pivot.  Measured on the served
-// stream (whose SITE tasks factor pivot matrices of up to ~32 x 32 to full rank)
-// 1024 gave the highest throughput and 192 the lowest per-task time for 32 x 32
-// matrices with 12 pivots; 512 sits between.
-constexpr int WARP_TAIL = 512;
+// with one warp no CTA barrier is needed per pivot.  Measured: up to ~6 elements
+// per lane one warp beats the barriers of the whole CTA (192, RRLU tasks); the
+// full-rank factorization of a SITE task's pivot matrix (at most ~32 x 32 on the
+// served stream) is fastest entirely in one warp (1024).
+constexpr int WARP_TAIL_RRLU = 192;
+constexpr int WARP_TAIL_SITE = 1024;
 
 // rrlu_loop from pivot K on (decision for K already taken, not stopped), warp 0
 // only; same arithmetic and argmax as the CTA path.  Returns the final K on
@@ -712,7 +713,7 @@ __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax,
 // load and one store.
 __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
                           bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl,
-                          double* xy = nullptr) {
+                          double* xy = nullptr, int warp_tail = WARP_TAIL_RRLU) {
   const int tid = threadIdx.x;
   const int kmax = min(maxrank, min(m, n));
   if (tid == 0) {
@@ -728,7 +729,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
   bool tail = false;
   while (!ctl.stop) {
     TCI_PHASE(1);
-    if ((m - K) * (n - K) <= WARP_TAIL) {
+    if ((m - K) * (n - K) <= warp_tail) {
       tail = true;
       break;
     }
@@ -1022,7 +1023,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
       am.push(v, pack_key(i, j));
     }
   argmax_resolve(am, P, r, 0, r, 0, r, ctl);
-  rrlu_loop(P, r, r, r, r, 0.0, 0.0, true, rowperm, colperm, rp.diag, ctl);
+  rrlu_loop(P, r, r, r, r, 0.0, 0.0, true, rowperm, colperm, rp.diag, ctl, nullptr, WARP_TAIL_SITE);
   int singular = 0;
   if (tid == 0) {
     for (int k = 0; k < r; ++k)
