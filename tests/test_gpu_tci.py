@@ -283,3 +283,21 @@ def test_optimize_options_parity(T, oracle, opts):
     assert list(ranks) == list(rranks)
     _same_sets(tci, ref)
     assert np.allclose(errs, rerrs, rtol=1e-12, atol=0)
+
+
+def test_batch_with_a_failing_request(T):
+    """A request whose f makes lu.L NaN fails with the reference's error; the other
+    solves of the batch and later calls are unaffected (the resident kernel is
+    stopped cleanly and the context stays usable)."""
+    rng = np.random.default_rng(41)
+    bad = np.ones((3, 3))
+    bad[1, 0] = np.nan
+    good = _served_specs(T, 42, 6, 32)
+    specs = good[:3] + [(T.DeviceFunction.dense(bad), [3, 3], dict(tolerance=1e-8))] + good[3:]
+    with pytest.raises(T.TCIError, match="NaN"):
+        T.crossinterpolate2_batched(specs, max_live=4)
+    again = T.crossinterpolate2_batched(good, max_live=4)
+    for (f, dims, kw), tb in zip(good, again):
+        ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
+        assert list(tb.linkdims()) == list(ta.linkdims())
+    del rng
