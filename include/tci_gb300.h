@@ -149,6 +149,12 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims);
 /* The (r0, d, r1) of every site tensor of n solves, concatenated (3 * sum of
  * the lengths entries); one call instead of one tci_get_core per site. */
 int tci_get_core_dims_batched(int64_t n, tci_solve* const* solves, int64_t* dims);
+/* Every site tensor of n solves, concatenated in solve then site order, in a
+ * pinned host buffer that the library allocates and its gather kernel writes
+ * directly (no staging copy).  *total_elems doubles; the caller hands the
+ * buffer back with tci_host_free (buffers are pooled and reused). */
+int tci_get_cores_pinned(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double** out, int64_t* total_elems);
+int tci_host_free(tci_ctx* ctx, void* p);
 int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
                           const int64_t* out_offsets);
 /* pivoterrors (length *npe) and bonderrors (L-1) (tensorci2.jl:13-16). */

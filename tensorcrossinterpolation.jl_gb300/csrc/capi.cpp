@@ -26,6 +26,7 @@ struct tci_ctx {
   // the ring, then the pools their blocks came from
   std::unique_ptr<BlockPool> dpool;
   std::vector<std::unique_ptr<BlockPool>> hpools, spools;  // per engine: task records, task scratch
+  std::unique_ptr<BlockPool> xpool;                        // pinned export buffers handed to the caller
   std::unique_ptr<ResidentQueue> rq;  // null: batched launches only
   std::vector<std::unique_ptr<Engine>> pool;
   Engine* engp = nullptr;
@@ -127,6 +128,7 @@ int tci_ctx_create(int device, size_t hbm_budget, tci_ctx** out) {
   if (const char* s = std::getenv("TCI_ENGINES")) neng = std::max(1, std::min(32, std::atoi(s)));
   std::unique_ptr<tci_ctx> c(new tci_ctx());
   c->dpool.reset(new BlockPool(BlockPool::DEVICE, device, true));
+  c->xpool.reset(new BlockPool(BlockPool::HOST, device, true));
   for (int i = 0; i < neng; ++i) {
     c->pool.emplace_back(new Engine(device));
     int rc = c->pool.back()->init();  // fails first when there is no device
@@ -380,6 +382,39 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
     if (e != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(e));
     s->ctx->eng_ref().stats.d2h_bytes += (int64_t)(c.elems() * sizeof(double));
   }
+  return 0;
+}
+
+int tci_get_cores_pinned(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double** out, int64_t* total_elems) {
+  *out = nullptr;
+  *total_elems = 0;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::vector<const double*> src;
+  std::vector<int64_t> len;
+  int64_t total = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const Solve& s = solves[i]->s;
+    if (!s.cores_valid) return fail(TCI_ERR_GENERIC, "site tensors are not available");
+    for (const Core& c : s.cores) {
+      src.push_back(c.p);
+      len.push_back((int64_t)c.elems());
+      total += (int64_t)c.elems();
+    }
+  }
+  double* buf = (double*)ctx->xpool->alloc((size_t)std::max<int64_t>(total, 1) * sizeof(double));
+  if (!buf) return fail(TCI_ERR_OOM, "pinned host memory for the export");
+  int rc = ctx->eng_ref().gather_to_pinned(src, len, buf);
+  if (rc) {
+    ctx->xpool->free(buf);
+    return rc;
+  }
+  *out = buf;
+  *total_elems = total;
+  return 0;
+}
+
+int tci_host_free(tci_ctx* ctx, void* p) {
+  ctx->xpool->free(p);
   return 0;
 }
 

@@ -896,6 +896,43 @@ int Engine::poll(bool& progressed) {
   return 0;
 }
 
+// Gather straight into mapped pinned host memory (the kernel writes across the
+// host link; no staging copy and no host memcpy).
+int Engine::gather_to_pinned(const std::vector<const double*>& src, const std::vector<int64_t>& len,
+                             double* pinned_out) {
+  const size_t n = src.size();
+  if (n == 0) return 0;
+  size_t total = 0;
+  std::vector<int64_t> off(n);
+  for (size_t i = 0; i < n; ++i) {
+    off[i] = (int64_t)total;
+    total += (size_t)len[i];
+  }
+  const size_t table = a16(n * (sizeof(void*) + 2 * sizeof(int64_t)));
+  if (table > hgat_cap_) {
+    if (hgat_) cudaFreeHost(hgat_);
+    hgat_ = nullptr;
+    CUDA_TRY(cudaHostAlloc(&hgat_, table, cudaHostAllocDefault));
+    hgat_cap_ = table;
+  }
+  if (table > dgat_cap_) {
+    if (dgat_) cudaFree(dgat_);
+    dgat_ = nullptr;
+    CUDA_TRY(cudaMalloc(&dgat_, table));
+    dgat_cap_ = table;
+  }
+  std::memcpy(hgat_, src.data(), n * sizeof(void*));
+  std::memcpy(hgat_ + n * sizeof(void*), len.data(), n * sizeof(int64_t));
+  std::memcpy(hgat_ + n * (sizeof(void*) + sizeof(int64_t)), off.data(), n * sizeof(int64_t));
+  CUDA_TRY(cudaMemcpyAsync(dgat_, hgat_, table, cudaMemcpyHostToDevice, stream_));
+  CUDA_TRY(tci_gather_launch(dgat_, (int)n, pinned_out, std::min<int>((int)n, 4 * num_sms), stream_));
+  CUDA_TRY(cudaStreamSynchronize(stream_));
+  stats.launches += 1;
+  stats.h2d_bytes += (int64_t)table;
+  stats.d2h_bytes += (int64_t)(total * sizeof(double));
+  return 0;
+}
+
 int Engine::gather_to_host(const std::vector<const double*>& src, const std::vector<int64_t>& len,
                            double* host_out) {
   const size_t n = src.size();

@@ -278,6 +278,9 @@ class Engine {
   // contiguous staging buffer, then a single device-to-host copy.
   int gather_to_host(const std::vector<const double*>& src, const std::vector<int64_t>& len,
                      double* host_out);
+  // The same into mapped pinned host memory, written by the gather kernel itself.
+  int gather_to_pinned(const std::vector<const double*>& src, const std::vector<int64_t>& len,
+                       double* pinned_out);
 
   tci_stats stats{};
   bool timing = true;

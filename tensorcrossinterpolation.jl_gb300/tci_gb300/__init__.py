@@ -11,6 +11,7 @@ Indices are 1-based, as in Julia.  Matrices are numpy arrays; site tensors are
 returned as (r_{b-1}, d_b, r_b) arrays.
 """
 import ctypes
+import weakref
 import os
 
 import numpy as np
@@ -157,6 +158,9 @@ _SIGNATURES = {
     "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
     "tci_tt4_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tci_get_core_dims_batched": (ctypes.c_int, [ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), I64P]),
+    "tci_get_cores_pinned": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p),
+                                            ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64)]),
+    "tci_host_free": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -716,6 +720,17 @@ def core_dims(tci):
     return dims
 
 
+class _PinnedBlock:
+    """A pinned host buffer of the library seen as a float64 array; given back to
+    the library's pool when the last array view of it is gone."""
+
+    def __init__(self, ctx, addr, n):
+        self.ctx = ctx  # the context owns the pool: keep it alive
+        self.__array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (addr, False), "version": 3}
+        fin = weakref.finalize(self, load_library().tci_host_free, ctx.h, ctypes.c_void_p(addr))
+        fin.atexit = False  # at exit the process releases everything; the context may be gone
+
+
 def tensortrains(tcis, ctx=None):
     """TensorTrain(tci) for many solves with one device-to-host copy."""
     ctx = ctx or default_context()
@@ -728,9 +743,10 @@ def tensortrains(tcis, ctx=None):
     elems = d3.prod(axis=1)
     core_off = np.concatenate([[0], np.cumsum(elems)]).astype(np.int64)
     solve_first = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
-    offs = np.ascontiguousarray(core_off[solve_first[:-1]])
-    out = np.empty(max(int(core_off[-1]), 1))
-    _check(lib.tci_get_cores_batched(ctx.h, len(tcis), handles, _p(out, F64P), _p(offs, I64P)))
+    ptr = ctypes.c_void_p()
+    total = ctypes.c_int64()
+    _check(lib.tci_get_cores_pinned(ctx.h, len(tcis), handles, ctypes.byref(ptr), ctypes.byref(total)))
+    out = np.asarray(_PinnedBlock(ctx, ptr.value, max(int(total.value), 1)))
     d3l = d3.tolist()
     col = core_off.tolist()
     sf = solve_first.tolist()
