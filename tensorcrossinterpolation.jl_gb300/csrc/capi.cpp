@@ -231,7 +231,7 @@ int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t 
     rc = ctx->eng_ref().run(t);
   }
   if (rc) {
-    ctx->eng_ref().release_cores((*out)->s);
+    ctx->eng_ref().release_solve((*out)->s);
     delete *out;
     *out = nullptr;
   }
@@ -241,7 +241,7 @@ int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t 
 int tci_solve_destroy(tci_solve* s) {
   if (!s) return 0;
   std::lock_guard<std::mutex> lk(s->ctx->mu);
-  s->ctx->eng_ref().release_cores(s->s);
+  s->ctx->eng_ref().release_solve(s->s);
   delete s;
   return 0;
 }
@@ -269,7 +269,7 @@ int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int
     rc = ctx->eng_ref().run(t);
   }
   if (rc) {
-    ctx->eng_ref().release_cores((*out)->s);
+    ctx->eng_ref().release_solve((*out)->s);
     delete *out;
     *out = nullptr;
   }
@@ -552,7 +552,7 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
       j.rc = j.task->h.promise().rc;
       std::string msg = j.rc ? std::string(last_message()) : std::string();
       j.task.reset();
-      if (!keep) e.release_cores(j.solve->s);
+      if (!keep) e.release_solve(j.solve->s);
       std::lock_guard<std::mutex> lk(sh.mu);
       if (j.rc && !sh.first_rc) {
         sh.first_rc = j.rc;

@@ -212,6 +212,11 @@ void Engine::free_core(double* p) {
   else
     cudaFreeAsync(p, stream_);
 }
+void Engine::release_solve(Solve& s) {
+  release_cores(s);
+  if (s.lut_dev) free_core(s.lut_dev);
+  s.lut_dev = nullptr;
+}
 void Engine::release_cores(Solve& s) {
   for (auto& c : s.cores) {
     if (c.p) free_core(c.p);
@@ -306,6 +311,9 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
     case TCI_TASK_SUM:
       t.smem_mode = 1;
       return 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
+    case TCI_TASK_TABLE:
+      t.smem_mode = 1;
+      return t.lut != nullptr;
     case TCI_TASK_SEARCH:  // t.n = sum of the left and right bond sizes
       t.smem_mode = 1;
       return a16((size_t)3 * (t.L + 1) * 4) + (size_t)t.n * 8 <= smem;
@@ -341,6 +349,8 @@ static int64_t task_cost(const tci_task& t) {
       return m * (40 + (int64_t)t.L * t.r * t.r);
     case TCI_TASK_SEARCH:
       return (m + 2 * (int64_t)t.L) * (int64_t)t.r * t.r * 2 + m * 40;
+    case TCI_TASK_TABLE:
+      return ((int64_t)t.lutcap0 + t.lutcap1) * 40;
     default:
       return 1;
   }
@@ -439,7 +449,7 @@ int Engine::launch() {
     res_total += r.res_bytes;
     o_work[i] = work_total;
     work_total += we;
-    if (r.t.lutcap0 > 0) work_total += (size_t)r.t.lutcap0 + (size_t)std::max(r.t.lutcap1, 0);
+    if (r.t.lutcap0 > 0 && !r.t.lut_full) work_total += (size_t)r.t.lutcap0 + (size_t)std::max(r.t.lutcap1, 0);
   }
   const size_t blob_total = off;
   int rc = ensure(blob_total, res_total, work_total);
@@ -464,7 +474,7 @@ int Engine::launch() {
     t.cores = r.ncores ? (int64_t)o_cores[i] : 0;
     t.res = (int64_t)o_res[i];
     t.work = t.smem_mode ? nullptr : dwork_ + o_work[i];
-    t.lut = t.lutcap0 > 0 ? dwork_ + o_work[i] + wel[i] : nullptr;
+    if (!t.lut_full) t.lut = t.lutcap0 > 0 ? dwork_ + o_work[i] + wel[i] : nullptr;
     if (r.ain_host) t.ain = (const double*)(dblob_ + o_ain[i]);
     t.cost = task_cost(t);
     tasks[i] = t;
@@ -819,9 +829,9 @@ int Engine::submit() {
       // the block may hold anything from an earlier use: clear the done word so
       // that a stale value can never read as this task's completion
       ((tci_result_head*)r.res)->done = 0;
-      const size_t lut = t.lutcap0 > 0 ? (size_t)t.lutcap0 + (size_t)std::max(t.lutcap1, 0) : 0;
+      const size_t lut = (t.lutcap0 > 0 && !t.lut_full) ? (size_t)t.lutcap0 + (size_t)std::max(t.lutcap1, 0) : 0;
       t.work = nullptr;
-      t.lut = nullptr;
+      if (!t.lut_full) t.lut = nullptr;
       if (we + lut > 0) {
         double* d = (double*)spool_->alloc((we + lut) * sizeof(double));
         if (!d) {
@@ -1144,6 +1154,11 @@ static void fill_f(Req& r, const Solve& s) {
   r.params = s.params.data();
   r.t.lutcap0 = s.lutcap0;
   r.t.lutcap1 = s.lutcap1;
+  if (s.lut_dev) {
+    r.t.lut = s.lut_dev;
+    r.t.lut_full = 1;
+    r.t.lut_base0 = s.L;
+  }
 }
 
 static int clamp_rank(i64 maxrank, size_t m, size_t n) {
@@ -1242,14 +1257,22 @@ CoTask co_construct(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivot
   if (rc) co_return rc;
   std::vector<uint8_t> pts;
   for (const auto& p : pivots) pts.insert(pts.end(), p.begin(), p.end());
-  Req r;
+  // the solve's f tables, once: every later task of the solve looks f up
+  if (s.lutcap0 > 0 && !s.lut_dev) s.lut_dev = e.alloc_core((size_t)s.lutcap0 + (size_t)std::max(s.lutcap1, 0));
+  Req r, tab;
   r.t.kind = TCI_TASK_EVAL;
   fill_f(r, s);
   r.t.m = (int32_t)pivots.size();
   r.t.nl = s.L;
   r.rows = pts.data();
   r.rows_bytes = pts.size();
-  GpuOp op{&e, {&r}};
+  std::vector<Req*> reqs{&r};
+  if (s.lut_dev) {
+    tab.t.kind = TCI_TASK_TABLE;
+    fill_f(tab, s);
+    reqs.push_back(&tab);
+  }
+  GpuOp op{&e, reqs};
   co_await op;
   if (op.status) co_return op.status;
   double ms = -std::numeric_limits<double>::infinity();
@@ -1696,8 +1719,12 @@ CoTask co_optimize(Engine& e, Solve& s, tci_opts o) {
 // crossinterpolate2 (tensorci2.jl:943-953)
 CoTask co_crossinterpolate2(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots, tci_opts o) {
   CO_TRY(co_construct(e, s, std::move(pivots)));
-  CO_TRY(co_optimize(e, s, o));
-  co_return 0;
+  const int rc = co_await co_optimize(e, s, o);
+  // the f tables serve the sweeps only; a finished solve keeps just its cores
+  // (later calls on it build per-task tables again)
+  if (s.lut_dev) e.free_core(s.lut_dev);
+  s.lut_dev = nullptr;
+  co_return rc;
 }
 
 }  // namespace tci

@@ -216,6 +216,7 @@ struct Solve {
   i64 nfeval = 0;
   tci_rng rng;
   int lutcap0 = 0, lutcap1 = 0;  // capacities of the f tables (tci_f_tables)
+  double* lut_dev = nullptr;     // the tables over the whole range (device pool), built once
   tci_opts opts{};
   // bookkeeping for serving
   int rc = 0;
@@ -270,6 +271,7 @@ class Engine {
   double* alloc_core(size_t elems);
   void free_core(double* p);
   void release_cores(Solve& s);
+  void release_solve(Solve& s);  // cores and the f tables: the solve is going away
   // Run a list of tasks outside any solve (rrLU entry points).  A single large
   // rrLU of a given matrix runs on the multi-CTA kernel (run_big).
   int run_tasks(std::vector<Req*>& reqs);

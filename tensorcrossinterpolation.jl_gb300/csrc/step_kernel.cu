@@ -94,21 +94,6 @@ struct ArgTrack {
     A = B = 0;
     k = 0xffffffffu;
   }
-  // elements visited in any key order: equal maxima keep the smaller key
-  __device__ __forceinline__ void push_any(double v, uint32_t key) {
-    uint64_t b = abs_bits(v);
-    if (b > NAN_FLOOR) return;
-    b += 1;
-    if (b > A) {
-      B = A;
-      A = b;
-      k = key;
-    } else if (b == A) {
-      k = key < k ? key : k;
-    } else if (b > B) {
-      B = b;
-    }
-  }
   __device__ __forceinline__ void push(double v, uint32_t key) {
     uint64_t b = abs_bits(v);
     if (b > NAN_FLOOR) return;
@@ -442,6 +427,13 @@ __device__ Filler make_filler(const tci_task& T, const double* prm, double* cons
   F.lo0 = F.lo1 = 0;
   if (!int_states(T)) return F;
   const int tables = tci_f_tables(T.fid);
+  if (T.lut_full) {  // the solve's tables, built once by its TABLE task
+    F.lut0 = T.lut;
+    F.lut1 = tables > 1 ? T.lut + T.lutcap0 : nullptr;
+    F.lo0 = T.lut_base0;
+    F.lo1 = 0;
+    return F;
+  }
   // max / -min of the row and column sums
   long long v[4] = {LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN};  // max r0, max r1, -min r0, -min r1
   long long w[4] = {LLONG_MIN, LLONG_MIN, LLONG_MIN, LLONG_MIN};
@@ -1314,6 +1306,25 @@ __device__ void task_sum(const tci_task& T, const char* blob, char* resb, char* 
   __syncthreads();
 }
 
+// TABLE task: part0 over [lut_base0, lut_base0 + lutcap0) and scale1(part1)
+// over [0, lutcap1) of the solve's f into T.lut -- the same functions the
+// per-element path calls, so table entries equal direct evaluation bit for bit.
+__device__ void task_table(const tci_task& T, const char* blob, char* resb) {
+  const double* prm = (const double*)at(blob, T.params);
+  for (int k = threadIdx.x; k < T.lutcap0; k += NT)
+    T.lut[k] = tci_f_part0(T.fid, prm, T.nparams, (double)(T.lut_base0 + k));
+  if (tci_f_tables(T.fid) > 1)
+    for (int k = threadIdx.x; k < T.lutcap1; k += NT)
+      T.lut[T.lutcap0 + k] = tci_f_scale1(T.fid, prm, tci_f_part1(T.fid, prm, (double)k));
+  if (threadIdx.x == 0) {
+    tci_result_head* h = (tci_result_head*)(atw(resb, T.res));
+    h->status = 0;
+    h->npivot = 0;
+    h->lut_used = 1;
+  }
+  __syncthreads();
+}
+
 __device__ void run_task(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl,
                          size_t smem_bytes) {
   switch (T.kind) {
@@ -1323,6 +1334,7 @@ __device__ void run_task(const tci_task& T, const char* blob, char* resb, char* 
     case TCI_TASK_EVAL: task_eval(T, blob, resb, smem, ctl); break;
     case TCI_TASK_SUM: task_sum(T, blob, resb, smem); break;
     case TCI_TASK_SEARCH: task_search(T, blob, resb, smem); break;
+    case TCI_TASK_TABLE: task_table(T, blob, resb); break;
     default: break;
   }
 }
@@ -1408,9 +1420,15 @@ __device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmas
     const int p = okm == FULL ? 32 : __ffs(~okm) - 1;
     if (p > 0) {
       if (lane < p) {
-        const volatile uint64_t* src = (const volatile uint64_t*)&h->t;
-        uint64_t* dst = (uint64_t*)&d->t;
-        for (int w = 0; w < TASK_WORDS; ++w) dst[w] = src[w];
+        // all loads first (independent, uncached: one trip over the host link),
+        // then the stores; ordered after this lane's acquire of `seq`
+        const unsigned long long* src = (const unsigned long long*)&h->t;
+        unsigned long long* dst = (unsigned long long*)&d->t;
+        unsigned long long w[TASK_WORDS];
+#pragma unroll
+        for (int q = 0; q < TASK_WORDS; ++q) w[q] = __ldcv(src + q);
+#pragma unroll
+        for (int q = 0; q < TASK_WORDS; ++q) dst[q] = w[q];
         st_release_sys(&h->taken, hp + 1);
         st_release_gpu(&d->seq, dk + 1);
       }

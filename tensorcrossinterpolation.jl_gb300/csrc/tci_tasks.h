@@ -22,7 +22,8 @@ enum {
   TCI_TASK_CORE = 3,  // core = Pi1 (last site of fillsitetensors!/sweep1site!)
   TCI_TASK_EVAL = 4,  // f and the tensor train at a list of points
   TCI_TASK_SUM = 5,   // sum of the tensor train over all sites
-  TCI_TASK_SEARCH = 6 // line scans of the global pivot search from one start point
+  TCI_TASK_SEARCH = 6, // line scans of the global pivot search from one start point
+  TCI_TASK_TABLE = 7   // a solve's f parts tabulated over the whole range of its integer sums
 };
 
 enum {
@@ -62,6 +63,8 @@ typedef struct tci_task {
   double* lut;                 // scratch for tabulated f parts (lutcap0 + lutcap1 doubles)
   int32_t lutcap0, lutcap1;    // table capacities (0: evaluate f directly)
   uint64_t ticket;             // resident mode: host-ring ticket (the record's done word = ticket + 1)
+  int32_t lut_full;            // lut holds the solve's tables over the whole range (no per-task build)
+  int32_t lut_base0;           // the integer sum at table0[0] (table1 starts at 0)
 } tci_task;
 
 // Result record: fixed header followed by per-task arrays.
