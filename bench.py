@@ -17,7 +17,8 @@ Reported (one JSON line):
   e2e    solves/s through the public C ABI (host request buffers in, every
          solve's site tensors and pivot sets copied back to host), wall clock;
   plain_solves_per_s   the one-solve-at-a-time GPU path on a subset;
-  serve_p50_ms / serve_p99_ms   latency under Poisson arrivals;
+  serve_p50_ms / serve_p99_ms   latency under Poisson arrivals at 80 % of the rate;
+  serve_sweep  p50 / p99 at Poisson rates 50 ... 2000 requests/s;
   roofline  FP64 pipe of the step kernel vs the measured FP64 peak;
   cpu_baseline  the CPU oracle (C++ restatement of the reference) solving a
          bounded sample of the same requests on all host cores.
@@ -349,6 +350,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the latency sweep over arrival rates")
     ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -459,6 +461,16 @@ def main():
     specs_s = specs_s[:nserve]
     arrival = np.cumsum(rng.exponential(1.0 / lam, size=nserve))
     lat, rk, wall = T.serve(specs_s, arrival, ctx=ctx)
+    # the served configuration's arrival rates: p50 / p99 latency at each
+    sweep = []
+    if not args.no_sweep:
+        for rate in (50, 200, 500, 1000, 2000):
+            n_r = int(min(2000, max(100, rate * 2.0)))
+            arr_r = np.cumsum(np.random.default_rng(rate).exponential(1.0 / rate, size=n_r))
+            sp = (specs_s * (n_r // len(specs_s) + 1))[:n_r]
+            lat_r, _, wall_r = T.serve(sp, arr_r, ctx=ctx)
+            sweep.append({"rate_per_s": rate, "requests": n_r, "p50_ms": float(np.percentile(lat_r, 50) * 1e3),
+                          "p99_ms": float(np.percentile(lat_r, 99) * 1e3), "served_per_s": n_r / wall_r})
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -484,6 +496,7 @@ def main():
         "batched_over_plain": e2e / world / plain,
         "serve_p50_ms": float(np.percentile(lat, 50) * 1e3), "serve_p99_ms": float(np.percentile(lat, 99) * 1e3),
         "serve_rate_per_s": lam,
+        "serve_sweep": sweep,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": None,
                      "peak_source": "measured FP64 mul+sub throughput (tci_fp64_peak), this run",
