@@ -139,6 +139,11 @@ double tci_maxsamplevalue(const tci_solve* s);
 /* Iset[b], Jset[b] for 1-based site b: I is nI x (b-1), J is nJ x (L-b), row-major,
  * 1-based.  Pass NULL arrays to query nI/nJ only. */
 int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t* J, int64_t* nJ);
+/* Replace Iset[b] / Jset[b] (1-based multi-indices, row-major); invalidates the
+ * site tensors. */
+int tci_set_sets(tci_solve* s, int32_t b, const int64_t* I, int64_t nI, const int64_t* J, int64_t nJ);
+/* bonderrors (tensorci2.jl:132-139), L-1 doubles. */
+int tci_bonderrors(const tci_solve* s, double* out);
 /* Site tensor b (1-based), column-major r_{b-1} x d_b x r_b; dims[3] out.
  * Pass NULL `out` to query dims.  Fails if site tensors are invalidated. */
 int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims);
@@ -270,6 +275,29 @@ typedef struct tci_stats {
   int64_t feval_tabulated;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
+
+/* evaluate / sum (abstracttensortrain.jl:124-199) of a tensor train the caller
+ * gives: cores[b] is r0 x d x r1 column-major, dims[3*b + 0..2] its sizes;
+ * points np x L, 1-based, row-major. */
+int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, const int64_t* points,
+                    int64_t np, double* out);
+int tci_tt_sum(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double* out);
+
+/* ---- incremental server: requests are submitted one at a time while the
+ * context serves them with continuous batching (host threads + the resident
+ * kernel); completed requests are polled.  The server owns the context until
+ * tci_serve_stop returns (other calls on the context wait). */
+typedef struct tci_server tci_server;
+int tci_serve_start(tci_ctx* ctx, int64_t max_live, tci_server** out);
+/* Copies the request's arrays; *id = 0, 1, 2, ... in submission order. */
+int tci_serve_submit(tci_server* s, const tci_request* req, int64_t* id);
+/* Up to cap completed requests since the last poll (waits up to timeout_ms
+ * for the first): id, status (0 or a TCI_ERR_* code), rank (max bond
+ * dimension, -1 on error), latency from submit to completion in seconds. */
+int tci_serve_poll(tci_server* s, int64_t cap, int64_t* ids, int32_t* status, int64_t* ranks, double* latency,
+                   int64_t* n, int32_t timeout_ms);
+/* Finishes every submitted request, then stops; results not polled are dropped. */
+int tci_serve_stop(tci_server* s);
 
 /* ---- tensor trains with 4-leg cores (link, s_in, s_out, link'), column-major,
  * and their contraction (contraction.jl) and recompression (tensortrain.jl).

@@ -10,6 +10,9 @@
 #include <thread>
 #include <cstdlib>
 #include <algorithm>
+#include <condition_variable>
+#include <deque>
+#include <functional>
 #include <numeric>
 
 #include "contract.h"
@@ -368,6 +371,46 @@ int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t
   return 0;
 }
 
+// Iset[b] / Jset[b] <- the given multi-indices (1-based, row-major: nI x (b-1)
+// and nJ x (L-b)); the site tensors are invalidated (tensorci2.jl:528-529 style
+// replacement of the index sets, as a restart would do).
+int tci_set_sets(tci_solve* s, int32_t b, const int64_t* I, int64_t nI, const int64_t* J, int64_t nJ) {
+  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  Solve& v = s->s;
+  if (b < 1 || b > v.L) return fail(TCI_ERR_ARG, "site index out of range");
+  if (nI < 0 || nJ < 0) return fail(TCI_ERR_ARG, "negative set size");
+  IndexSet Is, Js;
+  Is.len = b - 1;
+  Js.len = v.L - b;
+  std::vector<uint8_t> buf((size_t)std::max(v.L, 1));
+  for (int64_t i = 0; i < nI; ++i) {
+    for (int q = 0; q < Is.len; ++q) {
+      const int64_t x = I[i * Is.len + q];
+      if (x < 1 || x > v.d[q]) return fail(TCI_ERR_ARG, "index out of range");
+      buf[q] = (uint8_t)(x - 1);
+    }
+    if (Is.len == 0) ++Is.n; else Is.push(buf.data());
+  }
+  for (int64_t j = 0; j < nJ; ++j) {
+    for (int q = 0; q < Js.len; ++q) {
+      const int64_t x = J[j * Js.len + q];
+      if (x < 1 || x > v.d[b + q]) return fail(TCI_ERR_ARG, "index out of range");
+      buf[q] = (uint8_t)(x - 1);
+    }
+    if (Js.len == 0) ++Js.n; else Js.push(buf.data());
+  }
+  v.Iset[b - 1] = std::move(Is);
+  v.Jset[b - 1] = std::move(Js);
+  s->ctx->eng_ref().release_cores(v);
+  return 0;
+}
+
+// bonderrors (tensorci2.jl:132-139): L-1 doubles
+int tci_bonderrors(const tci_solve* s, double* out) {
+  std::copy(s->s.bonderrors.begin(), s->s.bonderrors.end(), out);
+  return 0;
+}
+
 int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
   if (b < 1 || b > s->s.L) return fail(TCI_ERR_ARG, "site index out of range");
   if (!s->s.cores_valid) return fail(TCI_ERR_GENERIC, "site tensors are not available");
@@ -501,8 +544,22 @@ struct Job {
   tci_solve* solve = nullptr;
   std::optional<CoTask> task;
   bool started = false, done = false;
-  double arrival = 0, t_start = 0, t_done = 0;
+  double arrival = 0, t_start = 0, t_done = 0;  // seconds since the drive started
   int rc = 0;
+  tci_request req{};  // the request (its arrays owned below for server jobs)
+  std::vector<int64_t> dims_own;
+  std::vector<double> params_own;
+  double est = 0;     // HBM estimate
+  int64_t id = -1;    // server request id
+  double t_submit = 0;  // server: absolute submit time
+};
+
+// Source of jobs beyond the initial list (the server's queue): pull appends
+// newly submitted jobs and their admission order and tells whether more may
+// come; on_done reports a finished job.  Both are called under the drive lock.
+struct JobFeed {
+  std::function<bool(std::deque<Job>&, std::vector<int64_t>&)> pull;
+  std::function<void(Job&)> on_done;
 };
 
 // Drive jobs with continuous batching, one host thread per engine of the
@@ -522,31 +579,30 @@ struct DriveShared {
   std::string fatal_msg;
 };
 
-int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
-          std::vector<Job>& jobs, bool keep) {
+int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_live, bool keep, JobFeed* feed) {
   auto& pool = ctx->pool;
   const int G = (int)pool.size();
-  jobs.clear();
-  jobs.resize((size_t)n);
-  if (max_live <= 0) max_live = n;
+  int64_t n = (int64_t)jobs.size();
+  if (max_live <= 0) max_live = feed ? 1024 : std::max<int64_t>(n, 1);
   const double t0 = now_s();
   const double budget = (double)pool[0]->hbm_budget;
-  std::vector<double> est(n);
-  for (int64_t i = 0; i < n; ++i) est[i] = solve_estimate_bytes(reqs[i]);
+  for (auto& j : jobs) j.est = solve_estimate_bytes(j.req);
   // Admission order: by arrival when there are arrival times; otherwise the
   // largest solves first, so that the longest serial chains do not start last
-  // and leave the device with a tail of a few live solves.
+  // and leave the device with a tail of a few live solves.  Jobs from the feed
+  // are admitted in submission order.
   std::vector<int64_t> order(n);
   std::iota(order.begin(), order.end(), 0);
-  if (!arrival)
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return est[a] > est[b]; });
+  if (!use_arrival)
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return jobs[a].est > jobs[b].est; });
   DriveShared sh;
+  bool feed_open = feed != nullptr;
 
   auto worker = [&](int g) {
     Engine& e = *pool[g];
-    std::vector<int64_t> mine;  // live job ids on this engine
-    auto finish = [&](int64_t i) {
-      Job& j = jobs[i];
+    std::vector<Job*> mine;  // live jobs on this engine (deque elements do not move)
+    auto finish = [&](Job* jp) {
+      Job& j = *jp;
       j.done = true;
       j.t_done = now_s() - t0;
       j.rc = j.task->h.promise().rc;
@@ -554,22 +610,23 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
       j.task.reset();
       if (!keep) e.release_solve(j.solve->s);
       std::lock_guard<std::mutex> lk(sh.mu);
-      if (j.rc && !sh.first_rc) {
+      if (j.rc && !sh.first_rc && !feed) {  // a server reports errors per request
         sh.first_rc = j.rc;
         sh.first_msg = msg;
       }
       --sh.live;
       ++sh.finished;
-      sh.live_bytes -= est[i];
+      sh.live_bytes -= j.est;
+      if (feed) feed->on_done(j);
     };
     auto reap = [&]() {
       size_t w = 0;
       for (size_t k = 0; k < mine.size(); ++k) {
-        Job& j = jobs[mine[k]];
-        if (j.task && j.task->h.done())
-          finish(mine[k]);
+        Job* jp = mine[k];
+        if (jp->task && jp->task->h.done())
+          finish(jp);
         else
-          mine[w++] = mine[k];
+          mine[w++] = jp;
       }
       mine.resize(w);
     };
@@ -579,42 +636,47 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
     for (;;) {
       // admission
       for (;;) {
-        int64_t idx = -1;
+        Job* jp = nullptr;
         {
           std::lock_guard<std::mutex> lk(sh.mu);
           if (sh.fatal) return;
+          if (feed_open && sh.next >= (int64_t)order.size()) {
+            const size_t before = jobs.size();
+            feed_open = feed->pull(jobs, order);
+            for (size_t q = before; q < jobs.size(); ++q) jobs[q].est = solve_estimate_bytes(jobs[q].req);
+          }
           double t = now_s() - t0;
-          if (sh.next < n && sh.live < max_live && (int64_t)mine.size() < share &&
-              (!arrival || arrival[sh.next] <= t) &&
-              (sh.live == 0 || sh.live_bytes + est[order[sh.next]] <= budget)) {
-            idx = order[sh.next++];
+          if (sh.next < (int64_t)order.size() && sh.live < max_live && (int64_t)mine.size() < share &&
+              (!use_arrival || jobs[order[sh.next]].arrival <= t) &&
+              (sh.live == 0 || sh.live_bytes + jobs[order[sh.next]].est <= budget)) {
+            jp = &jobs[order[sh.next++]];
             ++sh.live;
-            sh.live_bytes += est[idx];
+            sh.live_bytes += jp->est;
           }
         }
-        if (idx < 0) break;
-        Job& j = jobs[idx];
-        j.arrival = arrival ? arrival[idx] : 0.0;
+        if (!jp) break;
+        Job& j = *jp;
         j.t_start = now_s() - t0;
-        const tci_request& r = reqs[idx];
+        const tci_request& r = j.req;
         int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
         if (rc) {
           j.started = j.done = true;
           j.rc = rc;
           std::lock_guard<std::mutex> lk(sh.mu);
-          if (!sh.first_rc) {
+          if (!sh.first_rc && !feed) {
             sh.first_rc = rc;
             sh.first_msg = last_message();
           }
           --sh.live;
           ++sh.finished;
-          sh.live_bytes -= est[idx];
+          sh.live_bytes -= j.est;
+          if (feed) feed->on_done(j);
           continue;
         }
         std::vector<std::vector<uint8_t>> piv(1, std::vector<uint8_t>(r.L, 0));
         j.task.emplace(co_crossinterpolate2(e, j.solve->s, piv, r.opts));
         j.started = true;
-        mine.push_back(idx);
+        mine.push_back(jp);
         j.task->h.resume();
       }
       reap();
@@ -680,8 +742,13 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
       double wait = 0;
       {
         std::lock_guard<std::mutex> lk(sh.mu);
-        if (sh.next >= n || sh.fatal) return;  // nothing left for this engine
-        if (arrival) wait = arrival[sh.next] - (now_s() - t0);
+        if (sh.fatal) return;
+        if (sh.next >= (int64_t)order.size()) {
+          if (!feed_open) return;  // nothing left for this engine
+          wait = 2e-4;             // the server's queue is empty: look again shortly
+        } else if (use_arrival) {
+          wait = jobs[order[sh.next]].arrival - (now_s() - t0);
+        }
       }
       if (wait > 0)
         std::this_thread::sleep_for(std::chrono::duration<double>(std::min(wait, 1e-3)));
@@ -717,8 +784,9 @@ int drive(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arriva
 int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* reqs, int64_t max_live,
                                   tci_solve** out) {
   std::lock_guard<std::mutex> lk(ctx->mu);
-  std::vector<Job> jobs;
-  int rc = drive(ctx, n, reqs, nullptr, max_live, jobs, true);
+  std::deque<Job> jobs((size_t)n);
+  for (int64_t i = 0; i < n; ++i) jobs[i].req = reqs[i];
+  int rc = drive(ctx, jobs, false, max_live, true, nullptr);
   for (int64_t i = 0; i < n; ++i) out[i] = jobs[i].solve;
   return rc;
 }
@@ -726,9 +794,13 @@ int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* re
 int tci_serve_run(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
                   double* latency, int64_t* rank, double* wall) {
   std::lock_guard<std::mutex> lk(ctx->mu);
-  std::vector<Job> jobs;
+  std::deque<Job> jobs((size_t)n);
+  for (int64_t i = 0; i < n; ++i) {
+    jobs[i].req = reqs[i];
+    jobs[i].arrival = arrival ? arrival[i] : 0.0;
+  }
   double t0 = now_s();
-  int rc = drive(ctx, n, reqs, arrival, max_live, jobs, false);
+  int rc = drive(ctx, jobs, arrival != nullptr, max_live, false, nullptr);
   if (wall) *wall = now_s() - t0;
   for (int64_t i = 0; i < n; ++i) {
     if (latency) latency[i] = jobs[i].t_done - jobs[i].arrival;
@@ -736,6 +808,128 @@ int tci_serve_run(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double
     if (jobs[i].solve) delete jobs[i].solve;
   }
   return rc;
+}
+
+// ---------------------------------------------------------------- incremental server
+}  // extern "C"
+
+struct tci_server {
+  tci_ctx* ctx = nullptr;
+  int64_t max_live = 0;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<Job> incoming;  // submitted, not yet handed to the drive
+  struct Done {
+    int64_t id, rank;
+    int32_t status;
+    double latency;
+  };
+  std::vector<Done> completed;
+  bool stopping = false;
+  int64_t next_id = 0;
+  int rc = 0;
+  std::string msg;
+  std::thread th;
+};
+
+namespace {
+void server_main(tci_server* srv) {
+  tci_ctx* ctx = srv->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);  // the server owns the context until it stops
+  std::deque<Job> jobs;
+  JobFeed feed;
+  feed.pull = [srv](std::deque<Job>& js, std::vector<int64_t>& order) {
+    std::lock_guard<std::mutex> l(srv->mu);
+    while (!srv->incoming.empty()) {
+      js.push_back(std::move(srv->incoming.front()));
+      srv->incoming.pop_front();
+      Job& j = js.back();
+      j.req.localdims = j.dims_own.data();  // the arrays moved with the job
+      j.req.fparams = j.params_own.empty() ? nullptr : j.params_own.data();
+      order.push_back((int64_t)js.size() - 1);
+    }
+    return !srv->stopping;
+  };
+  feed.on_done = [srv](Job& j) {
+    tci_server::Done d;
+    d.id = j.id;
+    d.status = j.rc;
+    d.rank = (j.solve && !j.rc) ? solve_rank(j.solve->s) : -1;
+    d.latency = now_s() - j.t_submit;
+    if (j.solve) {
+      delete j.solve;  // its device memory went back at the end of the solve
+      j.solve = nullptr;
+    }
+    std::lock_guard<std::mutex> l(srv->mu);
+    srv->completed.push_back(d);
+    srv->cv.notify_all();
+  };
+  int rc = drive(ctx, jobs, false, srv->max_live, false, &feed);
+  std::lock_guard<std::mutex> l(srv->mu);
+  srv->rc = rc;
+  if (rc) srv->msg = last_message();
+  srv->cv.notify_all();
+}
+}  // namespace
+
+extern "C" {
+
+int tci_serve_start(tci_ctx* ctx, int64_t max_live, tci_server** out) {
+  auto* srv = new tci_server();
+  srv->ctx = ctx;
+  srv->max_live = max_live;
+  srv->th = std::thread(server_main, srv);
+  *out = srv;
+  return 0;
+}
+
+int tci_serve_submit(tci_server* srv, const tci_request* req, int64_t* id) {
+  if (req->L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
+  Job j;
+  j.req = *req;
+  j.dims_own.assign(req->localdims, req->localdims + req->L);
+  if (req->nparams > 0) j.params_own.assign(req->fparams, req->fparams + req->nparams);
+  j.req.localdims = j.dims_own.data();
+  j.req.fparams = j.params_own.empty() ? nullptr : j.params_own.data();
+  j.t_submit = now_s();
+  std::lock_guard<std::mutex> l(srv->mu);
+  if (srv->stopping) return fail(TCI_ERR_ARG, "the server is stopping");
+  j.id = srv->next_id++;
+  *id = j.id;
+  srv->incoming.push_back(std::move(j));
+  return 0;
+}
+
+int tci_serve_poll(tci_server* srv, int64_t cap, int64_t* ids, int32_t* status, int64_t* ranks, double* latency,
+                   int64_t* n, int32_t timeout_ms) {
+  std::unique_lock<std::mutex> l(srv->mu);
+  if (timeout_ms > 0 && srv->completed.empty())
+    srv->cv.wait_for(l, std::chrono::milliseconds(timeout_ms), [&] { return !srv->completed.empty() || srv->rc; });
+  const int64_t k = std::min<int64_t>(cap, (int64_t)srv->completed.size());
+  for (int64_t q = 0; q < k; ++q) {
+    const auto& d = srv->completed[(size_t)q];
+    if (ids) ids[q] = d.id;
+    if (status) status[q] = d.status;
+    if (ranks) ranks[q] = d.rank;
+    if (latency) latency[q] = d.latency;
+  }
+  srv->completed.erase(srv->completed.begin(), srv->completed.begin() + k);
+  *n = k;
+  if (srv->rc) return fail(srv->rc, srv->msg);
+  return 0;
+}
+
+int tci_serve_stop(tci_server* srv) {
+  {
+    std::lock_guard<std::mutex> l(srv->mu);
+    srv->stopping = true;
+  }
+  if (srv->th.joinable()) srv->th.join();
+  const int rc = srv->rc;
+  const std::string msg = srv->msg;
+  delete srv;
+  if (rc) return fail(rc, msg);
+  return 0;
 }
 
 // ---------------------------------------------------------------- f and host helpers
@@ -996,6 +1190,87 @@ int tci_tt4_destroy(tci_tt4* t) {
   }
   delete t;
   return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- tensor trains given by the caller
+namespace {
+// A solve holding only uploaded cores (no f): evaluate/sum run on its tables.
+int upload_tt3(Engine& e, int32_t L, const int64_t* dims, const double* const* cores, Solve& s) {
+  s.L = L;
+  s.d.assign((size_t)L, 1);
+  s.cores.assign((size_t)L, Core());
+  for (int32_t b = 0; b < L; ++b) {
+    Core& c = s.cores[b];
+    c.d0 = dims[3 * b];
+    c.d1 = dims[3 * b + 1];
+    c.d2 = dims[3 * b + 2];
+    if (c.d0 < 1 || c.d1 < 1 || c.d2 < 1 || c.d1 > 256 || (b > 0 && s.cores[b - 1].d2 != c.d0) ||
+        (b == 0 && c.d0 != 1) || (b == L - 1 && c.d2 != 1)) {
+      e.release_cores(s);
+      return fail(TCI_ERR_DIM, "inconsistent tensor-train dimensions");
+    }
+    s.d[b] = (int)c.d1;
+    c.p = e.alloc_core(c.elems());
+    if (!c.p) {
+      e.release_cores(s);
+      return fail(TCI_ERR_OOM, "device memory for the cores");
+    }
+    cudaError_t ce = cudaMemcpyAsync(c.p, cores[b], c.elems() * sizeof(double), cudaMemcpyHostToDevice, e.stream());
+    if (ce != cudaSuccess) {
+      e.release_cores(s);
+      return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+    }
+  }
+  cudaError_t ce = cudaStreamSynchronize(e.stream());
+  if (ce != cudaSuccess) {
+    e.release_cores(s);
+    return fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  }
+  s.cores_valid = true;
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, const int64_t* points,
+                    int64_t np, double* out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  Solve s;
+  int rc = upload_tt3(e, L, dims, cores, s);
+  if (rc) return rc;
+  auto piv = to_pivots(points, np, L, s.d, &rc);
+  if (!rc) {
+    std::vector<uint8_t> pts;
+    pts.reserve((size_t)np * L);
+    for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
+    const int64_t chunk = 1 << 20;
+    for (int64_t b = 0; b < np && !rc; b += chunk) {
+      const int64_t n = std::min(chunk, np - b);
+      std::vector<uint8_t> sub(pts.begin() + b * L, pts.begin() + (b + n) * L);
+      CoTask t = co_evaluate(e, s, sub, n, nullptr, out + b);
+      rc = e.run(t);
+    }
+  }
+  e.release_cores(s);
+  return rc;
+}
+
+int tci_tt_sum(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double* out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  Solve s;
+  int rc = upload_tt3(e, L, dims, cores, s);
+  if (rc) return rc;
+  CoTask t = co_sum(e, s, out);
+  rc = e.run(t);
+  e.release_cores(s);
+  return rc;
 }
 
 }  // extern "C"

@@ -161,6 +161,16 @@ _SIGNATURES = {
     "tci_get_cores_pinned": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p),
                                             ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_int64)]),
     "tci_host_free": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "tci_serve_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_serve_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "tci_serve_poll": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, I64P, ctypes.POINTER(ctypes.c_int32), I64P,
+                                      F64P, ctypes.POINTER(ctypes.c_int64), ctypes.c_int32]),
+    "tci_serve_stop": (ctypes.c_int, [ctypes.c_void_p]),
+    "tci_set_sets": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_int64, I64P, ctypes.c_int64]),
+    "tci_bonderrors": (ctypes.c_int, [ctypes.c_void_p, F64P]),
+    "tci_tt_evaluate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P, ctypes.c_int64,
+                                       F64P]),
+    "tci_tt_sum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, F64P]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -422,6 +432,15 @@ class TensorCI2:
     def sitetensors(self):
         return [self.sitetensor(b) for b in range(1, len(self) + 1)]
 
+    def set_sets(self, b, I, J):
+        """Replace Iset[b] and Jset[b] (1-based multi-indices); invalidates the site tensors."""
+        L = len(self)
+        I = np.ascontiguousarray(np.asarray(I, dtype=np.int64).reshape(-1, b - 1) if b > 1
+                                 else np.zeros((len(I), 0), np.int64))
+        J = np.ascontiguousarray(np.asarray(J, dtype=np.int64).reshape(-1, L - b) if b < L
+                                 else np.zeros((len(J), 0), np.int64))
+        _check(load_library().tci_set_sets(self.h, b, _p(I, I64P), I.shape[0], _p(J, I64P), J.shape[0]))
+
     def errors(self):
         lib = load_library()
         n = ctypes.c_int64()
@@ -512,6 +531,33 @@ class TensorTrain:
 
     def rank(self):
         return max(self.linkdims())
+
+    def _args(self):
+        cores = [np.asfortranarray(c, dtype=np.float64) for c in self.sitetensors]
+        if not all(c.ndim == 3 for c in cores):
+            raise ArgumentError(TCI_ERR_ARG, "evaluate/sum need 3-leg site tensors")
+        dims = np.ascontiguousarray([list(c.shape) for c in cores], dtype=np.int64).reshape(-1)
+        return cores, dims, (ctypes.c_void_p * len(cores))(*[c.ctypes.data for c in cores])
+
+    def evaluate(self, points, ctx=None):
+        """evaluate(tt, indexset) (abstracttensortrain.jl:124-162) on the device, 1-based."""
+        ctx = ctx or default_context()
+        cores, dims, ptrs = self._args()
+        pts = np.asarray(points, dtype=np.int64)
+        single = pts.ndim == 1
+        pts = np.ascontiguousarray(pts.reshape(-1, len(cores)))
+        out = np.zeros(pts.shape[0])
+        _check(load_library().tci_tt_evaluate(ctx.h, len(cores), _p(dims, I64P), ptrs, _p(pts, I64P), pts.shape[0],
+                                              _p(out, F64P)))
+        return float(out[0]) if single else out
+
+    def sum(self, ctx=None):
+        """sum(tt) (abstracttensortrain.jl:164-199) on the device."""
+        ctx = ctx or default_context()
+        cores, dims, ptrs = self._args()
+        out = ctypes.c_double()
+        _check(load_library().tci_tt_sum(ctx.h, len(cores), _p(dims, I64P), ptrs, ctypes.byref(out)))
+        return out.value
 
 
 def _tt4_args(cores):
@@ -764,6 +810,39 @@ def serve(specs, arrival, max_live=0, ctx=None):
     _check(load_library().tci_serve_run(ctx.h, len(specs), arr, _p(arrival, F64P), int(max_live), _p(lat, F64P),
                                         _p(rank, I64P), ctypes.byref(wall)))
     return lat, rank, wall.value
+
+
+class Server:
+    """Incremental server (tci_serve_start/submit/poll/stop): requests go in one at
+    a time while earlier ones are being solved with continuous batching; the
+    context is reserved for the server until stop()."""
+
+    def __init__(self, max_live=0, ctx=None):
+        self.ctx = ctx or default_context()
+        self.h = ctypes.c_void_p()
+        _check(load_library().tci_serve_start(self.ctx.h, int(max_live), ctypes.byref(self.h)))
+
+    def submit(self, f, localdims, **kwargs):
+        arr, keep = make_requests([(f, localdims, kwargs)])
+        rid = ctypes.c_int64()
+        _check(load_library().tci_serve_submit(self.h, ctypes.byref(arr[0]), ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, cap=4096, timeout_ms=0):
+        """[(id, status, rank, latency_s), ...] of the requests finished since the last poll."""
+        ids = np.zeros(cap, np.int64)
+        st = np.zeros(cap, np.int32)
+        rk = np.zeros(cap, np.int64)
+        lat = np.zeros(cap)
+        n = ctypes.c_int64()
+        _check(load_library().tci_serve_poll(self.h, cap, _p(ids, I64P), st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                             _p(rk, I64P), _p(lat, F64P), ctypes.byref(n), int(timeout_ms)))
+        return [(int(ids[i]), int(st[i]), int(rk[i]), float(lat[i])) for i in range(n.value)]
+
+    def stop(self):
+        if self.h:
+            h, self.h = self.h, None
+            _check(load_library().tci_serve_stop(h))
 
 
 def feval(f, localdims, points, ctx=None):

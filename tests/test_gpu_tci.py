@@ -301,3 +301,60 @@ def test_batch_with_a_failing_request(T):
         ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
         assert list(tb.linkdims()) == list(ta.linkdims())
     del rng
+
+
+def test_tt_evaluate_and_sum_of_given_trains(T, oracle):
+    """evaluate / sum of a tensor train the caller gives (not from a solve)."""
+    rng = np.random.default_rng(51)
+    bonds = [1, 3, 4, 2, 1]
+    cores = [rng.standard_normal((bonds[n], 3, bonds[n + 1])) for n in range(4)]
+    tt = T.TensorTrain(cores)
+    pts = rng.integers(1, 4, size=(500, 4))
+    ref = oracle.tt_evaluate(cores, pts)
+    assert np.allclose(tt.evaluate(pts), ref, rtol=1e-13, atol=1e-14)
+    assert tt.sum() == pytest.approx(oracle.tt_sum(cores), rel=1e-13)
+
+
+def test_set_sets_and_bonderrors(T, oracle):
+    f = T.DeviceFunction("lorentz")
+    tci, _, _ = T.crossinterpolate2(float, f, [6] * 4, tolerance=1e-10)
+    I, J = tci.sets(2)
+    be = np.zeros(3)
+    T.load_library().tci_bonderrors(tci.h, be.ctypes.data_as(T.F64P))
+    assert np.all(be >= 0)
+    tci.set_sets(2, I, J)  # same sets back: nothing changes but the cores are rebuilt on demand
+    I2, J2 = tci.sets(2)
+    assert np.array_equal(I, I2) and np.array_equal(J, J2)
+    with pytest.raises(T.ArgumentError):
+        tci.set_sets(2, np.array([[7]]), J)
+
+
+def test_incremental_server(T):
+    """tci_serve_start / submit / poll / stop: requests submitted in bursts while
+    earlier ones run; every one completes with the rank it has alone."""
+    import time as _time
+
+    specs = _served_specs(T, 61, 16, 32)
+    srv = T.Server(max_live=8)
+    done = {}
+    ids = {}
+    try:
+        for k, (f, dims, kw) in enumerate(specs[:8]):
+            ids[srv.submit(f, dims, **kw)] = k
+        for rid, st, rank, lat in srv.poll(timeout_ms=50):
+            done[rid] = (st, rank, lat)
+        _time.sleep(0.05)
+        for k, (f, dims, kw) in enumerate(specs[8:], start=8):
+            ids[srv.submit(f, dims, **kw)] = k
+        t0 = _time.time()
+        while len(done) < len(specs) and _time.time() - t0 < 60:
+            for rid, st, rank, lat in srv.poll(timeout_ms=100):
+                done[rid] = (st, rank, lat)
+    finally:
+        srv.stop()
+    assert sorted(done) == list(range(len(specs)))
+    for rid, (st, rank, lat) in done.items():
+        f, dims, kw = specs[ids[rid]]
+        assert st == 0 and lat > 0
+        ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
+        assert ta.rank() == rank
