@@ -1,0 +1,28 @@
+"""Host logic of the engine on the CPU: the index-set operations (kronecker,
+union, select, pushunique!) through the library's own C++ symbols, built into
+a small checker (tests/host/indexset_check.cpp) linked against libtci_gpu.so."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+PKG = os.path.join(ROOT, "tensorcrossinterpolation.jl_gb300")
+
+
+def test_index_sets(T, tmp_path):
+    cxx = shutil.which(os.environ.get("CXX", "g++"))
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    lib = os.path.dirname(T.load_library()._name)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / "indexset_check")
+    cmd = [cxx, "-std=c++20", "-O1", "-I", os.path.join(PKG, "csrc"), "-I", os.path.join(cuda, "include"),
+           os.path.join(HERE, "host", "indexset_check.cpp"), "-o", exe, "-L", lib, "-ltci_gpu",
+           f"-Wl,-rpath,{lib}", "-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
