@@ -89,6 +89,30 @@ const char* tci_last_error(void);
 /* Name -> id of a registered device function ("lorentz", "served", ...). */
 int tci_f_lookup(const char* name, int* fid);
 
+/* ---- Caller-supplied f ---------------------------------------------------
+ * The BatchEvaluator plugin point (cachedtensortrain.jl:1, batcheval.jl:67-83)
+ * for functions that are not registered on the device, with the value cache of
+ * CachedFunction (cachedfunction.jl:8-184) kept in device memory.  The callback
+ * fills values[k] = f(points[k, :]) for npoints multi-indices (npoints x L,
+ * row-major, 1-based) and returns 0, or nonzero to make the library call that
+ * asked for the values fail with TCI_ERR_GENERIC.  f must be a pure function of
+ * the multi-index: each solve asks for every distinct point at most once and
+ * serves repeats from its device hash table (keys are the mixed-radix number of
+ * the multi-index, so prod(localdims) must stay below 2^104).  The callback runs
+ * on the thread that made the library call, between device steps.
+ * tci_f_register returns an id >= TCI_F_USER that the solve entry points
+ * (tci_solve_create, tci_crossinterpolate2, tci_feval) take in place of a
+ * registered function's id; the batched and serving entry points accept only
+ * registered device functions. */
+typedef int (*tci_batch_fn)(void* user, int32_t L, int64_t npoints, const int64_t* points,
+                            double* values);
+#define TCI_F_USER 1024
+int tci_f_register(tci_batch_fn fn, void* user, int32_t* fid);
+int tci_f_unregister(int32_t fid);
+/* Cache counters of a solve with a caller-supplied f: distinct points stored,
+ * points passed to the callback, callback invocations. */
+int tci_fcache_stats(const tci_solve* s, int64_t* entries, int64_t* evaluated, int64_t* calls);
+
 /* ---- TensorCI2 (tensorci2.jl:6-72) ------------------------------------- */
 /* TensorCI2{Float64}(f, localdims, initialpivots) (tensorci2.jl:42-53).
  * pivots: np x L row-major, 1-based. */

@@ -95,6 +95,8 @@ def lib():
                                             ctypes.c_int64, ctypes.POINTER(Opts),
                                             ctypes.POINTER(ctypes.c_int)]
         L.orc_tci_free.argtypes = [ctypes.c_void_p]
+        L.orc_register_fn.argtypes = [BATCH_FN, ctypes.c_void_p]
+        L.orc_register_fn.restype = ctypes.c_int
         L.orc_tci_optimize.argtypes = [ctypes.c_void_p, ctypes.POINTER(Opts)]
         L.orc_tci_updatepivots.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_int64]
@@ -240,6 +242,29 @@ def right(res):
     out = np.empty_like(res["U"])
     out[:, res["colpermutation"]] = res["U"]
     return out
+
+
+# orc_batch_fn: (user, L, npoints, points[npoints x L], values[npoints]) -> status
+BATCH_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, I64P, F64P)
+_registered = []
+
+
+def register_fn(f):
+    """Register a caller-supplied f (the BatchEvaluator plugin point): f gets an
+    (npoints, L) int64 array of 1-based multi-indices and returns npoints values.
+    Returns the oracle's function id."""
+
+    def _call(user, L, n, pts, vals):
+        try:
+            a = np.ctypeslib.as_array(pts, shape=(n, L)).copy()
+            np.ctypeslib.as_array(vals, shape=(n,))[:] = np.asarray(f(a), dtype=np.float64).reshape(-1)
+            return 0
+        except BaseException:
+            return 1
+
+    cb = BATCH_FN(_call)
+    _registered.append(cb)
+    return lib().orc_register_fn(cb, None)
 
 
 def feval(fid, params, points):

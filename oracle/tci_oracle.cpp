@@ -54,11 +54,30 @@ double jmax(double a, double b) {
 // ---------------------------------------------------------------- functions
 enum { F_LORENTZ = 1, F_SERVED = 2, F_QTT1D = 3, F_QTT2D = 4, F_DENSE = 5, F_PRODUCT = 6 };
 
+// A caller-supplied f (the BatchEvaluator plugin point, batcheval.jl:67-83):
+// values[k] = f(points[k, :]) for npoints row-major 1-based multi-indices.
+typedef int (*orc_batch_fn)(void* user, int32_t L, int64_t npoints, const int64_t* points, double* values);
+constexpr int F_USER = 1024;
+
 struct Func {
   int fid = 0;
   std::vector<double> params;
+  orc_batch_fn cb = nullptr;
+  void* user = nullptr;
+  // values at many points through one evaluator call (filltensor on a
+  // BatchEvaluator, batcheval.jl:67-83); NaN everywhere if the evaluator fails
+  void batch(int L, int64_t np, const int64_t* pts, double* out) const {
+    if (cb(user, L, np, pts, out) != 0)
+      for (int64_t k = 0; k < np; ++k) out[k] = NaN;
+  }
   double operator()(const MultiIndex& v) const {
     const int L = (int)v.size();
+    if (cb) {
+      std::vector<int64_t> p(v.begin(), v.end());
+      double out = NaN;
+      batch(L, 1, p.data(), &out);
+      return out;
+    }
     switch (fid) {
       case F_LORENTZ: {  // coeff ./ (sum(v .^ 2) + 1), test_tensorci2.jl:249
         i64 s = 0;
@@ -442,6 +461,18 @@ struct TCI2 {
 // batcheval.jl:32-61).  Column-major |I| x |J|.
 std::vector<double> fill(TCI2& t, const std::vector<MultiIndex>& I, const std::vector<MultiIndex>& J) {
   std::vector<double> out(I.size() * J.size());
+  if (t.f.cb) {  // one evaluator call for the whole block, column-major
+    std::vector<int64_t> pts;
+    pts.reserve(out.size() * (size_t)t.L);
+    for (size_t j = 0; j < J.size(); ++j)
+      for (size_t i = 0; i < I.size(); ++i) {
+        pts.insert(pts.end(), I[i].begin(), I[i].end());
+        pts.insert(pts.end(), J[j].begin(), J[j].end());
+      }
+    if (!out.empty()) t.f.batch(t.L, (int64_t)out.size(), pts.data(), out.data());
+    t.nfeval += (i64)out.size();
+    return out;
+  }
   MultiIndex v(t.L);
   for (size_t j = 0; j < J.size(); ++j)
     for (size_t i = 0; i < I.size(); ++i) {
@@ -844,10 +875,17 @@ int optimize(TCI2& t, const Opts& o) {
   return ORC_OK;
 }
 
+std::vector<std::pair<orc_batch_fn, void*>> user_fns;  // id F_USER + k
+
 Func make_func(int fid, const double* params, i64 nparams) {
   Func f;
   f.fid = fid;
-  f.params.assign(params, params + nparams);
+  if (params) f.params.assign(params, params + nparams);
+  const i64 k = (i64)fid - F_USER;
+  if (k >= 0 && k < (i64)user_fns.size()) {
+    f.cb = user_fns[(size_t)k].first;
+    f.user = user_fns[(size_t)k].second;
+  }
   return f;
 }
 
@@ -1119,10 +1157,20 @@ int orc_rrlu_batched(int64_t nmat, const double* A, const int64_t* offsets, cons
   return bad.load();
 }
 
+// Caller-supplied f under id F_USER + k (k = 0, 1, ... in order of registration).
+int orc_register_fn(orc_batch_fn fn, void* user) {
+  user_fns.emplace_back(fn, user);
+  return F_USER + (int)user_fns.size() - 1;
+}
+
 // Function values at points (row-major np x L, 1-based).
 int orc_feval(int fid, const double* params, int64_t nparams, int L, const int64_t* pts, int64_t np,
               double* out) {
   Func f = make_func(fid, params, nparams);
+  if (f.cb) {
+    if (np > 0) f.batch(L, np, pts, out);
+    return 0;
+  }
   MultiIndex v(L);
   for (int64_t p = 0; p < np; ++p) {
     for (int q = 0; q < L; ++q) v[q] = (int)pts[p * L + q];

@@ -28,9 +28,10 @@ CU_SOURCES = {
     "contract.cu": ["-fmad=false"],
     "peak.cu": [],
     "gather.cu": [],
+    "fcache.cu": [],
 }
-CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp"]
-HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h"]
+CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp"]
+HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "fcache.h", "fc_slot.h"]
 
 
 def _newer(target, deps):

@@ -33,7 +33,11 @@ struct tci_ctx {
   std::unique_ptr<ResidentQueue> rq;  // null: batched launches only
   std::vector<std::unique_ptr<Engine>> pool;
   Engine* engp = nullptr;
-  std::mutex mu;
+  // Recursive: a caller-supplied f runs while its call holds the lock, and a
+  // finalizer it triggers (a garbage collector releasing another solve) may
+  // destroy objects of the same context from inside it.  Entry points that
+  // compute refuse to run there (Engine::run / run_tasks).
+  std::recursive_mutex mu;
   Engine& eng_ref() { return *engp; }
 };
 
@@ -223,15 +227,27 @@ static int make_solve(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t
   return 0;
 }
 
+// A solve whose f is caller-supplied runs on plain step launches: its value
+// cache is filled by separate kernels between steps, which a persistent kernel
+// holding every SM would keep waiting.
+static int run_solve(tci_ctx* ctx, Solve& s, CoTask& t) {
+  if (!s.fcache) return ctx->eng_ref().run(t);
+  if (ctx->rq) {
+    int rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  return ctx->eng_ref().run(t, false);
+}
+
 int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid, const double* fparams,
                      int64_t nparams, const int64_t* pivots, int64_t np, tci_solve** out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   int rc = make_solve(ctx, L, localdims, fid, fparams, nparams, out);
   if (rc) return rc;
   auto piv = to_pivots(pivots, np, L, (*out)->s.d, &rc);
   if (!rc) {
     CoTask t = co_construct(ctx->eng_ref(), (*out)->s, piv);
-    rc = ctx->eng_ref().run(t);
+    rc = run_solve(ctx, (*out)->s, t);
   }
   if (rc) {
     ctx->eng_ref().release_solve((*out)->s);
@@ -243,16 +259,25 @@ int tci_solve_create(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t 
 
 int tci_solve_destroy(tci_solve* s) {
   if (!s) return 0;
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   s->ctx->eng_ref().release_solve(s->s);
   delete s;
+  return 0;
+}
+
+int tci_fcache_stats(const tci_solve* s, int64_t* entries, int64_t* evaluated, int64_t* calls) {
+  if (!s) return fail(TCI_ERR_ARG, "null solve");
+  const FCache* c = s->s.fcache.get();
+  if (entries) *entries = c ? (int64_t)c->count : 0;
+  if (evaluated) *evaluated = c ? c->evaluated : 0;
+  if (calls) *calls = c ? c->calls : 0;
   return 0;
 }
 
 int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int32_t fid,
                           const double* fparams, int64_t nparams, const int64_t* pivots, int64_t np,
                           const tci_opts* opts, tci_solve** out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   int rc = make_solve(ctx, L, localdims, fid, fparams, nparams, out);
   if (rc) return rc;
   std::vector<int64_t> ones;
@@ -269,7 +294,7 @@ int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int
     else
       tci_opts_default(&o);
     CoTask t = co_crossinterpolate2(ctx->eng_ref(), (*out)->s, piv, o);
-    rc = ctx->eng_ref().run(t);
+    rc = run_solve(ctx, (*out)->s, t);
   }
   if (rc) {
     ctx->eng_ref().release_solve((*out)->s);
@@ -280,49 +305,49 @@ int tci_crossinterpolate2(tci_ctx* ctx, int32_t L, const int64_t* localdims, int
 }
 
 int tci_optimize(tci_solve* s, const tci_opts* opts) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   tci_opts o;
   if (opts)
     o = *opts;
   else
     tci_opts_default(&o);
   CoTask t = co_optimize(s->ctx->eng_ref(), s->s, o);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 int tci_updatepivots(tci_solve* s, int32_t b, int32_t leftorthogonal, double reltol, double abstol,
                      int64_t maxbonddim) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   if (b < 1 || b > s->s.L - 1) return fail(TCI_ERR_ARG, "bond index out of range");
   CoTask t = co_updatepivots(s->ctx->eng_ref(), s->s, b - 1, leftorthogonal != 0, reltol, abstol,
                              maxbonddim <= 0 ? TYPEMAX : maxbonddim, nullptr, nullptr);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 int tci_sweep2site(tci_solve* s, int32_t niter, int32_t iter1, double abstol, int64_t maxbonddim,
                    int32_t sweepstrategy, int32_t strictlynested, int32_t fillsitetensors) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CoTask t = co_sweep2site(s->ctx->eng_ref(), s->s, niter, iter1, abstol, maxbonddim <= 0 ? TYPEMAX : maxbonddim,
                            sweepstrategy, strictlynested != 0, fillsitetensors != 0);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 int tci_sweep1site(tci_solve* s, int32_t forward, double reltol, double abstol, int64_t maxbonddim,
                    int32_t updatetensors) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CoTask t = co_sweep1site(s->ctx->eng_ref(), s->s, forward != 0, reltol, abstol,
                            maxbonddim <= 0 ? TYPEMAX : maxbonddim, updatetensors != 0);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 int tci_fillsitetensors(tci_solve* s) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CoTask t = co_fillsitetensors(s->ctx->eng_ref(), s->s);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 int tci_addglobalpivots(tci_solve* s, const int64_t* pivots, int64_t np) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   int rc = 0;
   auto piv = to_pivots(pivots, np, s->s.L, s->s.d, &rc);
   if (rc) return rc;
@@ -375,7 +400,7 @@ int tci_get_sets(const tci_solve* s, int32_t b, int64_t* I, int64_t* nI, int64_t
 // and nJ x (L-b)); the site tensors are invalidated (tensorci2.jl:528-529 style
 // replacement of the index sets, as a restart would do).
 int tci_set_sets(tci_solve* s, int32_t b, const int64_t* I, int64_t nI, const int64_t* J, int64_t nJ) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   Solve& v = s->s;
   if (b < 1 || b > v.L) return fail(TCI_ERR_ARG, "site index out of range");
   if (nI < 0 || nJ < 0) return fail(TCI_ERR_ARG, "negative set size");
@@ -431,7 +456,7 @@ int tci_get_core(const tci_solve* s, int32_t b, double* out, int64_t* dims) {
 int tci_get_cores_pinned(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double** out, int64_t* total_elems) {
   *out = nullptr;
   *total_elems = 0;
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   std::vector<const double*> src;
   std::vector<int64_t> len;
   int64_t total = 0;
@@ -477,7 +502,7 @@ int tci_get_core_dims_batched(int64_t n, tci_solve* const* solves, int64_t* dims
 
 int tci_get_cores_batched(tci_ctx* ctx, int64_t n, tci_solve* const* solves, double* out,
                           const int64_t* out_offsets) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   std::vector<const double*> src;
   std::vector<int64_t> len;
   int64_t expect = -1;
@@ -513,7 +538,7 @@ int tci_get_history(const tci_solve* s, int64_t* ranks, double* errors, int64_t*
 }
 
 int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   int rc = 0;
   auto piv = to_pivots(points, np, s->s.L, s->s.d, &rc);
   if (rc) return rc;
@@ -526,16 +551,16 @@ int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
     int64_t n = std::min(chunk, np - b);
     std::vector<uint8_t> sub(pts.begin() + b * s->s.L, pts.begin() + (b + n) * s->s.L);
     CoTask t = co_evaluate(s->ctx->eng_ref(), s->s, sub, n, nullptr, out + b);
-    rc = s->ctx->eng_ref().run(t);
+    rc = run_solve(s->ctx, s->s, t);
     if (rc) return rc;
   }
   return 0;
 }
 
 int tci_sum(tci_solve* s, double* out) {
-  std::lock_guard<std::mutex> lk(s->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CoTask t = co_sum(s->ctx->eng_ref(), s->s, out);
-  return s->ctx->eng_ref().run(t);
+  return run_solve(s->ctx, s->s, t);
 }
 
 // ---------------------------------------------------------------- batches / serving
@@ -658,7 +683,9 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
         Job& j = *jp;
         j.t_start = now_s() - t0;
         const tci_request& r = j.req;
-        int rc = make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
+        int rc = r.fid >= TCI_F_USER
+                     ? fail(TCI_ERR_ARG, "batched solves take registered device functions only")
+                     : make_solve(ctx, r.L, r.localdims, r.fid, r.fparams, r.nparams, &j.solve);
         if (rc) {
           j.started = j.done = true;
           j.rc = rc;
@@ -783,7 +810,7 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
 
 int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* reqs, int64_t max_live,
                                   tci_solve** out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   std::deque<Job> jobs((size_t)n);
   for (int64_t i = 0; i < n; ++i) jobs[i].req = reqs[i];
   int rc = drive(ctx, jobs, false, max_live, true, nullptr);
@@ -793,7 +820,7 @@ int tci_crossinterpolate2_batched(tci_ctx* ctx, int64_t n, const tci_request* re
 
 int tci_serve_run(tci_ctx* ctx, int64_t n, const tci_request* reqs, const double* arrival, int64_t max_live,
                   double* latency, int64_t* rank, double* wall) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   std::deque<Job> jobs((size_t)n);
   for (int64_t i = 0; i < n; ++i) {
     jobs[i].req = reqs[i];
@@ -835,7 +862,7 @@ struct tci_server {
 namespace {
 void server_main(tci_server* srv) {
   tci_ctx* ctx = srv->ctx;
-  std::lock_guard<std::mutex> lk(ctx->mu);  // the server owns the context until it stops
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);  // the server owns the context until it stops
   std::deque<Job> jobs;
   JobFeed feed;
   feed.pull = [srv](std::deque<Job>& js, std::vector<int64_t>& order) {
@@ -935,7 +962,7 @@ int tci_serve_stop(tci_server* srv) {
 // ---------------------------------------------------------------- f and host helpers
 int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,
               const int64_t* localdims, const int64_t* points, int64_t np, double* out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   Solve s;
   int rc = solve_init(s, L, localdims, fid, fparams, nparams, nullptr, 0);
   if (rc) return rc;
@@ -948,7 +975,7 @@ int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams,
     pts.reserve((size_t)n * L);
     for (int64_t i = b; i < b + n; ++i) pts.insert(pts.end(), piv[i].begin(), piv[i].end());
     CoTask t = co_evaluate(ctx->eng_ref(), s, pts, n, out + b, nullptr);
-    rc = ctx->eng_ref().run(t);
+    rc = run_solve(ctx, s, t);
     if (rc) return rc;
   }
   return 0;
@@ -966,7 +993,7 @@ int tci_convergencecriterion(const int64_t* ranks, const double* errors, const i
 int tci_rrlu(tci_ctx* ctx, const double* A, int64_t m, int64_t n, int64_t maxrank, double reltol,
              double abstol, int32_t leftorthogonal, int64_t* rowperm, int64_t* colperm, double* L, double* U,
              int64_t* npivot, double* error) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (m < 0 || n < 0 || m > INT32_MAX || n > INT32_MAX || m * n > INT32_MAX)
     return fail(TCI_ERR_ARG, "matrix size out of range");
   Engine& e = ctx->eng_ref();
@@ -1023,7 +1050,7 @@ int tci_rrlu(tci_ctx* ctx, const double* A, int64_t m, int64_t n, int64_t maxran
 int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t* offsets, const int64_t* ms,
                      const int64_t* ns, int64_t maxrank, double reltol, double abstol, int32_t leftorthogonal,
                      int64_t* piv, const int64_t* piv_offsets, int64_t* npivots, double* errors) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   Engine& e = ctx->eng_ref();
   std::vector<Req> rs((size_t)nmat);
   std::vector<Req*> ptrs;
@@ -1114,7 +1141,7 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
                      const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, double tolerance,
                      int64_t maxbonddim, tci_tt4** out) {
   *out = nullptr;
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (algorithm != TCI_CONTRACT_NAIVE && algorithm != TCI_CONTRACT_ZIPUP)
     return fail(TCI_ERR_ARG, "Unknown algorithm.");
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
@@ -1147,7 +1174,7 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
 int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double tolerance,
                      int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out) {
   *out = nullptr;
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
   Engine& e = ctx->eng_ref();
   std::unique_ptr<tci_tt4> res(new tci_tt4());
@@ -1173,7 +1200,7 @@ int tci_tt4_dims(const tci_tt4* t, int64_t* dims) {
 
 int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out) {
   if (b < 1 || b > (int32_t)t->tt.cores.size()) return fail(TCI_ERR_ARG, "site index out of range");
-  std::lock_guard<std::mutex> lk(t->ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(t->ctx->mu);
   Engine& e = t->ctx->eng_ref();
   const Tensor4& c = t->tt.cores[b - 1];
   cudaError_t ce = cudaMemcpyAsync(out, c.p, c.elems() * sizeof(double), cudaMemcpyDeviceToHost, e.stream());
@@ -1185,7 +1212,7 @@ int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out) {
 int tci_tt4_destroy(tci_tt4* t) {
   if (!t) return 0;
   {
-    std::lock_guard<std::mutex> lk(t->ctx->mu);
+    std::lock_guard<std::recursive_mutex> lk(t->ctx->mu);
     t->tt.release(t->ctx->eng_ref());
   }
   delete t;
@@ -1237,7 +1264,7 @@ extern "C" {
 
 int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, const int64_t* points,
                     int64_t np, double* out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
   Engine& e = ctx->eng_ref();
   Solve s;
@@ -1261,7 +1288,7 @@ int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* 
 }
 
 int tci_tt_sum(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double* out) {
-  std::lock_guard<std::mutex> lk(ctx->mu);
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
   Engine& e = ctx->eng_ref();
   Solve s;

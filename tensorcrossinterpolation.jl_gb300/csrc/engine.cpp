@@ -62,6 +62,10 @@ static int fail(int code, const std::string& msg) {
   return code;
 }
 
+static int reentry() {
+  return fail(TCI_ERR_GENERIC, "the library was called to compute from inside a caller-supplied f");
+}
+
 // ---------------------------------------------------------------- index sets
 bool IndexSet::contains(const uint8_t* v) const {
   for (size_t i = 0; i < n; ++i)
@@ -141,6 +145,17 @@ IndexSet select(const IndexSet& s, const int32_t* idx, int k) {
 }
 
 // ---------------------------------------------------------------- GpuOp
+bool GpuOp::await_ready() {
+  if (reqs.empty()) return true;
+  FCache* last = nullptr;
+  for (Req* r : reqs)
+    if (r->fcache && r->fcache != last) {
+      last = r->fcache;
+      status = r->fcache->prefill(*eng, reqs);
+      if (status) return true;
+    }
+  return false;
+}
 void GpuOp::await_suspend(std::coroutine_handle<> h) { eng->enqueue(reqs, h, this); }
 int GpuOp::await_resume() const noexcept { return status; }
 
@@ -216,6 +231,7 @@ void Engine::release_solve(Solve& s) {
   release_cores(s);
   if (s.lut_dev) free_core(s.lut_dev);
   s.lut_dev = nullptr;
+  if (s.fcache) s.fcache->release();
 }
 void Engine::release_cores(Solve& s) {
   for (auto& c : s.cores) {
@@ -1068,6 +1084,7 @@ int Engine::run_big(Req& r) {
 }
 
 int Engine::run_tasks(std::vector<Req*>& reqs) {
+  if (fc_callback_depth()) return reentry();
   if (reqs.size() == 1 && big_eligible(*reqs[0], resident())) return run_big(*reqs[0]);
   CoTask t = co_tasks(*this, reqs);
   return run(t, false);
@@ -1117,6 +1134,7 @@ int Engine::run_resident(CoTask& t) {
 }
 
 int Engine::run(CoTask& t, bool allow_resident) {
+  if (fc_callback_depth()) return reentry();
   if (allow_resident && att_rq_ && !resident()) return run_resident(t);
   t.h.resume();
   while (!t.h.done()) {
@@ -1154,6 +1172,7 @@ static void fill_f(Req& r, const Solve& s) {
   r.params = s.params.data();
   r.t.lutcap0 = s.lutcap0;
   r.t.lutcap1 = s.lutcap1;
+  r.fcache = s.fcache.get();
   if (s.lut_dev) {
     r.t.lut = s.lut_dev;
     r.t.lut_full = 1;
@@ -1175,6 +1194,31 @@ i64 solve_rank(const Solve& s) {
 int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
                int64_t nparams, const int64_t*, int64_t) {
   if (L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
+  if (fid >= TCI_F_USER) {  // caller-supplied f behind the device value cache
+    tci_batch_fn fn = nullptr;
+    void* user = nullptr;
+    if (!user_fn(fid, &fn, &user)) return fail(TCI_ERR_ARG, "unknown function id");
+    s.L = L;
+    s.d.assign(localdims, localdims + L);
+    for (int x : s.d)
+      if (x < 1 || x > 256) return fail(TCI_ERR_ARG, "local dimensions must be in 1..256");
+    s.fid = TCI_FID_CACHE;
+    s.params.assign(4 + (size_t)L, 0.0);
+    s.fcache = std::make_shared<FCache>();
+    int rc = s.fcache->init(L, s.d.data(), fn, user, s.params.data());
+    if (rc) return rc;
+    s.Iset.assign(L, IndexSet());
+    s.Jset.assign(L, IndexSet());
+    for (int b = 0; b < L; ++b) {
+      s.Iset[b].len = b;
+      s.Jset[b].len = L - 1 - b;
+    }
+    s.cores.assign(L, Core());
+    s.bonderrors.assign(L - 1, 0.0);
+    s.lutcap0 = s.lutcap1 = 0;
+    s.pivoterrors.clear();
+    return 0;
+  }
   if (fid < TCI_F_LORENTZ || fid > TCI_F_PRODUCT) return fail(TCI_ERR_ARG, "unknown function id");
   s.L = L;
   s.d.assign(localdims, localdims + L);
@@ -1550,6 +1594,10 @@ CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np,
     const i64 p0 = q * chunk, n = std::min(chunk, np - p0);
     r.t.kind = TCI_TASK_EVAL;
     fill_f(r, s);
+    if (!fout) {  // train values only: no f
+      r.t.fid = 0;
+      r.fcache = nullptr;
+    }
     r.t.m = (int32_t)n;
     r.t.nl = s.L;
     r.rows = pts.data() + (size_t)p0 * s.L;

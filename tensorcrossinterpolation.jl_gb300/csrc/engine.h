@@ -8,12 +8,14 @@
 #include <coroutine>
 #include <cstdio>
 #include <cstdint>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
 
 #include "../../include/tci_gb300.h"
+#include "fcache.h"
 #include "tci_rng.h"
 #include "tci_tasks.h"
 
@@ -109,6 +111,7 @@ struct Req {
   const char* res = nullptr;         // host copy of the result record after the step
   size_t res_bytes = 0;
   uint64_t ticket = 0;               // resident mode: ring ticket of the task
+  FCache* fcache = nullptr;          // caller-supplied f: values come from this cache
   const tci_result_head* head() const { return (const tci_result_head*)res; }
   const int32_t* rowperm() const { return (const int32_t*)(res + sizeof(tci_result_head)); }
   const int32_t* colperm() const {
@@ -185,7 +188,9 @@ struct ResidentQueue {
 struct GpuOp {
   Engine* eng;
   std::vector<Req*> reqs;
-  bool await_ready() const noexcept { return reqs.empty(); }
+  // Fills the value caches of caller-supplied f's first; a failure there
+  // completes the operation with that status.
+  bool await_ready();
   void await_suspend(std::coroutine_handle<> h);
   int await_resume() const noexcept;
   int status = 0;
@@ -217,6 +222,7 @@ struct Solve {
   tci_rng rng;
   int lutcap0 = 0, lutcap1 = 0;  // capacities of the f tables (tci_f_tables)
   double* lut_dev = nullptr;     // the tables over the whole range (device pool), built once
+  std::shared_ptr<FCache> fcache;  // caller-supplied f (fid TCI_F_CACHE)
   tci_opts opts{};
   // bookkeeping for serving
   int rc = 0;

@@ -12,6 +12,7 @@
 // one-pass evaluation the CPU oracle performs.  `v` below is the 0-based local
 // index (the reference's index minus one).
 #pragma once
+#include "fc_slot.h"
 #include "tci_math.h"
 
 enum {
@@ -21,6 +22,7 @@ enum {
   TCI_F_QTT2D = 4,    // quantics 2-D, d = 4: x bit = low bit, y bit = high bit
   TCI_F_DENSE = 5,    // table lookup: f(v) = T[v] (column-major over localdims)
   TCI_F_PRODUCT = 6,  // f(v) = C * prod_n t[n, v_n] from log|t| and sign tables
+  TCI_F_CACHE = TCI_FID_CACHE,  // caller-supplied f: values looked up in the solve's device hash table
 };
 
 // Parameter layouts (double array `params`):
@@ -35,6 +37,14 @@ enum {
 //            multiple of 2^-40, neg = 1 where t < 0; f = C (-1)^(sum neg) exp(sum q).
 //            The rounding makes the sums exact, so f does not depend on how a
 //            multi-index is split into row and column parts.
+//   CACHE  : [table >> 32, table & 0xffffffff, mask, split, w_1 .. w_L]: the key of v
+//            is (k0, k1) = (sum_{p<split} w_p v_p, sum_{p>=split} w_p v_p), mixed-radix
+//            weights restarting at 1 at `split`, each half below 2^53 (exact sums);
+//            f(v) is the value stored under that key in the open-addressing table
+//            of tci_fc_entry slots (linear probing, `mask` + 1 slots).  The host
+//            fills the table from the caller's evaluator before any task reads it;
+//            a key that is not there reads as NaN.
+
 
 #define TCI_TWO_THOUSAND_PI 6283.185307179587   /* 2000*pi rounded to double */
 #define TCI_FOUR_HUNDRED_PI 1256.6370614359173  /* 400*pi rounded to double  */
@@ -66,6 +76,13 @@ TCI_HD void tci_f_term(int fid, const double* params, int site, int v,
       const int L = (int)params[0], D = (int)params[1];
       *acc0 = *acc0 + params[3 + site * D + v];
       *acc1 = *acc1 + params[3 + L * D + site * D + v];
+    } break;
+    case TCI_F_CACHE: {
+      const double w = (double)v * params[4 + site];
+      if (site < (int)params[3])
+        *acc0 = *acc0 + w;
+      else
+        *acc1 = *acc1 + w;
     } break;
     default: break;
   }
@@ -148,6 +165,23 @@ TCI_HD double tci_f_finish(int fid, const double* params, int nparams, double ac
     case TCI_F_PRODUCT: {
       const double e = params[2] * tci_exp(acc0);
       return (((long long)acc1) & 1) ? -e : e;
+    }
+    case TCI_F_CACHE: {
+#ifdef __CUDA_ARCH__
+      const unsigned long long addr =
+          ((unsigned long long)params[0] << 32) | (unsigned long long)params[1];
+      const tci_fc_entry* tab = (const tci_fc_entry*)addr;
+      const unsigned long long mask = (unsigned long long)params[2];
+      const unsigned long long k0 = (unsigned long long)acc0, k1 = (unsigned long long)acc1;
+      unsigned long long h = tci_fc_hash(k0, k1) & mask;
+      for (unsigned long long q = 0; q <= mask; ++q) {
+        const unsigned long long e0 = __ldg(&tab[h].k0);
+        if (e0 == k0 && __ldg(&tab[h].k1) == k1) return __ldg(&tab[h].v);
+        if (e0 == TCI_FC_EMPTY) break;
+        h = (h + 1) & mask;
+      }
+#endif
+      return tci_bits_to_double(0x7ff8000000000000ull);
     }
     default:
       return 0.0;

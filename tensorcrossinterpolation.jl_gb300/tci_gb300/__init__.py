@@ -21,6 +21,8 @@ LIB_PATH = os.path.join(HERE, "libtci_gpu.so")
 
 I64P = ctypes.POINTER(ctypes.c_int64)
 F64P = ctypes.POINTER(ctypes.c_double)
+# tci_batch_fn: (user, L, npoints, points[npoints x L], values[npoints]) -> status
+BATCH_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, I64P, F64P)
 
 TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
@@ -103,6 +105,9 @@ _SIGNATURES = {
     "tci_ctx_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "tci_last_error": (ctypes.c_char_p, []),
     "tci_f_lookup": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int)]),
+    "tci_f_register": (ctypes.c_int, [BATCH_FN, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]),
+    "tci_f_unregister": (ctypes.c_int, [ctypes.c_int32]),
+    "tci_fcache_stats": (ctypes.c_int, [ctypes.c_void_p, I64P, I64P, I64P]),
     "tci_solve_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_int32, F64P,
                                         ctypes.c_int64, I64P, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
     "tci_solve_destroy": (ctypes.c_int, [ctypes.c_void_p]),
@@ -274,6 +279,56 @@ class DeviceFunction:
         dims = table.shape
         strides = np.cumprod((1,) + dims[:-1])
         return DeviceFunction("dense", np.concatenate([[len(dims)], strides, table.reshape(-1, order="F")]))
+
+
+class BatchFunction:
+    """A caller-supplied f: the BatchEvaluator plugin point (cachedtensortrain.jl:1,
+    batcheval.jl:67-83) for functions with no device implementation.
+
+    ``f(points)`` gets an (npoints, L) int64 array of 1-based multi-indices and
+    returns npoints float64 values; it must be a pure function of the
+    multi-index.  Each solve keeps the values it has asked for in a device hash
+    table (CachedFunction, cachedfunction.jl:8-184) and calls f only for points
+    it has not seen, once per device step that needs new values.  An exception
+    raised by f makes the library call fail; it is kept in ``self.error``."""
+
+    def __init__(self, f):
+        self.f = f
+        self.ncalls = 0
+        self.npoints = 0
+        self.error = None
+        self.params = np.zeros(0)
+        self.name = "batch"
+
+        def _call(user, L, n, pts, vals):
+            try:
+                a = np.ctypeslib.as_array(pts, shape=(n, L)).copy()
+                v = np.ascontiguousarray(self.f(a), dtype=np.float64).reshape(-1)
+                if v.size != n:
+                    raise ValueError(f"f returned {v.size} values for {n} points")
+                np.ctypeslib.as_array(vals, shape=(n,))[:] = v
+                self.ncalls += 1
+                self.npoints += n
+                return 0
+            except BaseException as e:  # reported through the library's error code
+                self.error = e
+                return 1
+
+        self._cb = BATCH_FN(_call)
+        fid = ctypes.c_int32()
+        _check(load_library().tci_f_register(self._cb, None, ctypes.byref(fid)))
+        self.fid = fid.value
+
+    def close(self):
+        if self.fid:
+            load_library().tci_f_unregister(self.fid)
+            self.fid = 0
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def make_opts(tolerance=None, maxbonddim=None, maxiter=20, sweepstrategy="backandforth", normalizeerror=True,
@@ -461,6 +516,13 @@ class TensorCI2:
     def pivoterror(self):
         """pivoterror(tci) = maximum(bonderrors) (tensorci2.jl:157-159)."""
         return float(self.bonderrors.max())
+
+    def fcache_stats(self):
+        """(distinct points stored, points passed to f, calls of f) of a solve
+        whose f is a BatchFunction; zeros otherwise."""
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _check(load_library().tci_fcache_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
 
     def history(self):
         lib = load_library()
