@@ -329,20 +329,25 @@ int tci_serve_stop(tci_server* s);
  * Results stay on the device behind a tci_tt4 handle. */
 typedef struct tci_tt4 tci_tt4;
 enum { TCI_CONTRACT_NAIVE = 1, TCI_CONTRACT_ZIPUP = 2 };
+/* Factorization of _factorize (tensortrain.jl:94-137): rrlu's left/right, or
+ * MatrixLUCI's (matrixluci.jl:40-84). */
+enum { TCI_FACTORIZE_LU = 0, TCI_FACTORIZE_CI = 1 };
 /* contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) for
  * algorithm = :naive (contract_naive, :351-372) and :zipup (contract_zipup,
- * :442-486).  A's s_out leg contracts with B's s_in leg.  Deviations from the
- * reference, which factorizes with LinearAlgebra.svd in both: :naive with
- * tolerance > 0 or maxbonddim > 0 recompresses with compress!(:LU), and :zipup
- * factorizes with rrlu (method = :LU, leftorthogonal = false, reltol =
- * tolerance).  maxbonddim <= 0 means typemax(Int).  Errors as the reference:
+ * :442-486) with method = :LU or :CI.  A's s_out leg contracts with B's s_in leg.
+ * Deviations from the reference, which factorizes with LinearAlgebra.svd by
+ * default: :naive with tolerance > 0 or maxbonddim > 0 recompresses with
+ * compress!(method), and :zipup factorizes with rrlu / MatrixLUCI
+ * (leftorthogonal = false, reltol = tolerance); method = :SVD is not on the
+ * device.  maxbonddim <= 0 means typemax(Int).  Errors as the reference:
  * different lengths -> TCI_ERR_ARG, unmatched site index -> TCI_ERR_GENERIC. */
 int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
-                     const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, double tolerance,
-                     int64_t maxbonddim, tci_tt4** out);
-/* compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183). */
-int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double tolerance,
-                     int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out);
+                     const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, int32_t method,
+                     double tolerance, int64_t maxbonddim, tci_tt4** out);
+/* compress!(tt, method; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
+ * with method = :LU or :CI. */
+int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, int32_t method,
+                     double tolerance, int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out);
 int32_t tci_tt4_length(const tci_tt4* t);
 int tci_tt4_dims(const tci_tt4* t, int64_t* dims);
 int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out); /* b is 1-based */

@@ -130,11 +130,11 @@ def lib():
         L.orc_solve_batch.argtypes = [ctypes.c_int64, I32P, I64P, I64P, I32P, F64P, I64P, I64P, F64P,
                                       I64P, ctypes.POINTER(Opts), I64P, F64P, ctypes.c_int]
         L.orc_tt4_contract.restype = ctypes.c_void_p
-        L.orc_tt4_contract.argtypes = [ctypes.c_int, I64P, F64P, I64P, F64P, ctypes.c_int, ctypes.c_double,
-                                       ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
+        L.orc_tt4_contract.argtypes = [ctypes.c_int, I64P, F64P, I64P, F64P, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_double, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]
         L.orc_tt4_compress.restype = ctypes.c_void_p
-        L.orc_tt4_compress.argtypes = [ctypes.c_int, I64P, F64P, ctypes.c_double, ctypes.c_int64, ctypes.c_int,
-                                       ctypes.POINTER(ctypes.c_int)]
+        L.orc_tt4_compress.argtypes = [ctypes.c_int, I64P, F64P, ctypes.c_int, ctypes.c_double, ctypes.c_int64,
+                                       ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
         L.orc_tt4_length.argtypes = [ctypes.c_void_p]
         L.orc_tt4_dims.argtypes = [ctypes.c_void_p, I64P]
         L.orc_tt4_core.argtypes = [ctypes.c_void_p, ctypes.c_int, F64P]
@@ -475,24 +475,28 @@ def _tt4_unpack(h, rc):
         L.orc_tt4_free(h)
 
 
-def tt4_contract(a, b, algorithm="zipup", tolerance=1e-12, maxbonddim=None):
-    """contract_naive / contract_zipup(:LU) (contraction.jl:351-372, 442-486) of two
-    trains of 4-leg cores; returns the list of cores."""
+METHODS = {"LU": 0, "CI": 1}
+
+
+def tt4_contract(a, b, algorithm="zipup", tolerance=1e-12, maxbonddim=None, method="LU"):
+    """contract_naive / contract_zipup(:LU or :CI) (contraction.jl:351-372, 442-486)
+    of two trains of 4-leg cores; returns the list of cores."""
     ad, av = _tt4_pack(a)
     bd, bv = _tt4_pack(b)
     rc = ctypes.c_int()
     h = lib().orc_tt4_contract(len(a), _p(ad, I64P), _p(av, F64P), _p(bd, I64P), _p(bv, F64P),
-                               1 if algorithm == "naive" else 2, float(tolerance), int(maxbonddim or 0),
-                               ctypes.byref(rc))
+                               1 if algorithm == "naive" else 2, METHODS[method], float(tolerance),
+                               int(maxbonddim or 0), ctypes.byref(rc))
     return _tt4_unpack(h, rc)
 
 
-def tt4_compress(cores, tolerance=1e-12, maxbonddim=None, normalizeerror=True):
-    """compress!(tt, :LU) (tensortrain.jl:149-183); returns the list of cores."""
+def tt4_compress(cores, method="LU", tolerance=1e-12, maxbonddim=None, normalizeerror=True):
+    """compress!(tt, method) with :LU or :CI (tensortrain.jl:149-183); returns the
+    list of cores."""
     d, v = _tt4_pack(cores)
     rc = ctypes.c_int()
-    h = lib().orc_tt4_compress(len(cores), _p(d, I64P), _p(v, F64P), float(tolerance), int(maxbonddim or 0),
-                               int(bool(normalizeerror)), ctypes.byref(rc))
+    h = lib().orc_tt4_compress(len(cores), _p(d, I64P), _p(v, F64P), METHODS[method], float(tolerance),
+                               int(maxbonddim or 0), int(bool(normalizeerror)), ctypes.byref(rc))
     return _tt4_unpack(h, rc)
 
 

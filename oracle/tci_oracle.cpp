@@ -961,21 +961,29 @@ void matmul(const double* A, i64 lda, const double* B, i64 ldb, double* C, i64 l
 
 // _factorize(A, :LU; tolerance, maxbonddim, leftorthogonal, normalizeerror)
 // (tensortrain.jl:95-110)
+// _factorize(A, :LU or :CI; tolerance, maxbonddim, leftorthogonal, normalizeerror)
+// (tensortrain.jl:94-110): left/right of the rrLU, or of MatrixLUCI over it.
 int factorize_lu(const std::vector<double>& A, i64 m, i64 n, double tolerance, i64 maxbonddim, bool leftorth,
-                 bool normalizeerror, std::vector<double>& left, std::vector<double>& right, i64& K) {
+                 bool normalizeerror, std::vector<double>& left, std::vector<double>& right, i64& K,
+                 bool ci = false) {
   const double reltol = normalizeerror ? tolerance : 1e-14;
   const double abstol = normalizeerror ? 0.0 : tolerance;
   RRLU lu;
   int rc = rrlu(A.data(), m, n, maxbonddim, reltol, abstol, leftorth, lu);
   if (rc) return rc;
-  lu_left(lu, left);
-  lu_right(lu, right);
+  if (ci) {
+    left = luci_left(lu);
+    right = luci_right(lu);
+  } else {
+    lu_left(lu, left);
+    lu_right(lu, right);
+  }
   K = lu.npivot;
   return ORC_OK;
 }
 
 // contract_zipup(A, B; tolerance, method=:LU, maxbonddim) (contraction.jl:442-486)
-int contract_zipup_lu(const TT4& A, const TT4& B, double tolerance, i64 maxbonddim, TT4& out) {
+int contract_zipup_lu(const TT4& A, const TT4& B, double tolerance, i64 maxbonddim, TT4& out, bool ci = false) {
   out.clear();
   const size_t L = A.size();
   std::vector<double> R(1, 1.0);  // (link_ab, link_an, link_bn)
@@ -1021,7 +1029,7 @@ int contract_zipup_lu(const TT4& A, const TT4& B, double tolerance, i64 maxbondd
     }
     std::vector<double> left, right;
     i64 K = 0;
-    int rc = factorize_lu(C, rows, cols, tolerance, maxbonddim, false, true, left, right, K);
+    int rc = factorize_lu(C, rows, cols, tolerance, maxbonddim, false, true, left, right, K, ci);
     if (rc) return rc;
     core.d[3] = K;
     core.v.swap(left);
@@ -1035,14 +1043,14 @@ int contract_zipup_lu(const TT4& A, const TT4& B, double tolerance, i64 maxbondd
 }
 
 // compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
-int compress_lu(TT4& tt, double tolerance, i64 maxbonddim, bool normalizeerror) {
+int compress_lu(TT4& tt, double tolerance, i64 maxbonddim, bool normalizeerror, bool ci = false) {
   const size_t L = tt.size();
   for (size_t l = 0; l + 1 < L; ++l) {
     Core4 &c = tt[l], &nx = tt[l + 1];
     const i64 m = c.d[0] * c.d[1] * c.d[2], ncol = c.d[3];
     std::vector<double> left, right;
     i64 K = 0;
-    int rc = factorize_lu(c.v, m, ncol, 0.0, TYPEMAX, true, true, left, right, K);
+    int rc = factorize_lu(c.v, m, ncol, 0.0, TYPEMAX, true, true, left, right, K, ci);
     if (rc) return rc;
     const i64 nrest = nx.d[1] * nx.d[2] * nx.d[3];
     std::vector<double> nt((size_t)(K * nrest));
@@ -1057,7 +1065,7 @@ int compress_lu(TT4& tt, double tolerance, i64 maxbonddim, bool normalizeerror) 
     const i64 mrow = c.d[0], ncol = c.d[1] * c.d[2] * c.d[3];
     std::vector<double> left, right;
     i64 K = 0;
-    int rc = factorize_lu(c.v, mrow, ncol, tolerance, maxbonddim, false, normalizeerror, left, right, K);
+    int rc = factorize_lu(c.v, mrow, ncol, tolerance, maxbonddim, false, normalizeerror, left, right, K, ci);
     if (rc) return rc;
     const i64 prow = pv.d[0] * pv.d[1] * pv.d[2];
     std::vector<double> nt((size_t)(prow * K));
@@ -1391,25 +1399,29 @@ int orc_solve_batch(int64_t nreq, const int32_t* Ls, const int64_t* dims, const 
 // column-major values after core b-1's); dims[4*b + q] is the size of leg q of
 // core b.  algorithm: 1 naive (recompressed with compress!(:LU) when tolerance
 // > 0 or maxbonddim > 0), 2 zipup with rrLU.  Returns a handle to read with
-// orc_tt4_* and free with orc_tt4_free.
+// orc_tt4_* and free with orc_tt4_free.  method: 0 = :LU, 1 = :CI factorization.
 void* orc_tt4_contract(int L, const int64_t* a_dims, const double* a_values, const int64_t* b_dims,
-                       const double* b_values, int algorithm, double tolerance, int64_t maxbonddim, int* rc) {
+                       const double* b_values, int algorithm, int method, double tolerance, int64_t maxbonddim,
+                       int* rc) {
   TT4 a = read_tt4(L, a_dims, a_values), b = read_tt4(L, b_dims, b_values);
   auto* out = new TT4();
   *rc = ORC_OK;
+  const bool ci = method == 1;
   if (algorithm == 1) {
     for (int n = 0; n < L; ++n) out->push_back(naive_site(a[n], b[n]));
-    if (tolerance > 0 || maxbonddim > 0) *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, true);
+    if (tolerance > 0 || maxbonddim > 0)
+      *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, true, ci);
   } else {
-    *rc = contract_zipup_lu(a, b, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, *out);
+    *rc = contract_zipup_lu(a, b, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, *out, ci);
   }
   return out;
 }
 
-void* orc_tt4_compress(int L, const int64_t* dims, const double* values, double tolerance, int64_t maxbonddim,
-                       int normalizeerror, int* rc) {
+// compress!(tt, method) with method 0 = :LU, 1 = :CI.
+void* orc_tt4_compress(int L, const int64_t* dims, const double* values, int method, double tolerance,
+                       int64_t maxbonddim, int normalizeerror, int* rc) {
   auto* out = new TT4(read_tt4(L, dims, values));
-  *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, normalizeerror != 0);
+  *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, normalizeerror != 0, method == 1);
   return out;
 }
 

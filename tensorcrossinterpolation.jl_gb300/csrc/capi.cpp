@@ -1138,12 +1138,14 @@ int upload_tt4(Engine& e, int32_t L, const int64_t* dims, const double* const* c
 extern "C" {
 
 int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
-                     const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, double tolerance,
-                     int64_t maxbonddim, tci_tt4** out) {
+                     const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, int32_t method,
+                     double tolerance, int64_t maxbonddim, tci_tt4** out) {
   *out = nullptr;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (algorithm != TCI_CONTRACT_NAIVE && algorithm != TCI_CONTRACT_ZIPUP)
     return fail(TCI_ERR_ARG, "Unknown algorithm.");
+  if (method != TCI_FACTORIZE_LU && method != TCI_FACTORIZE_CI) return fail(TCI_ERR_GENERIC, "Not implemented yet.");
+  const bool ci = method == TCI_FACTORIZE_CI;
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
   Engine& e = ctx->eng_ref();
   TT4 a, b;
@@ -1156,9 +1158,9 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
     if (algorithm == TCI_CONTRACT_NAIVE) {
       rc = tt4_contract_naive(e, a, b, res->tt);
       if (!rc && (tolerance > 0 || maxbonddim > 0))
-        rc = tt4_compress_lu(e, res->tt, tolerance, maxbonddim, true);
+        rc = tt4_compress(e, res->tt, tolerance, maxbonddim, true, ci);
     } else {
-      rc = tt4_contract_zipup(e, a, b, tolerance, maxbonddim, res->tt);
+      rc = tt4_contract_zipup(e, a, b, tolerance, maxbonddim, res->tt, ci);
     }
   }
   a.release(e);
@@ -1171,17 +1173,18 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
   return 0;
 }
 
-int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double tolerance,
-                     int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out) {
+int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, int32_t method,
+                     double tolerance, int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out) {
   *out = nullptr;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  if (method != TCI_FACTORIZE_LU && method != TCI_FACTORIZE_CI) return fail(TCI_ERR_GENERIC, "Not implemented yet.");
   Engine& e = ctx->eng_ref();
   std::unique_ptr<tci_tt4> res(new tci_tt4());
   res->ctx = ctx;
   int rc = upload_tt4(e, L, dims, cores, res->tt);
   if (!rc) rc = tt4_check(res->tt);
-  if (!rc) rc = tt4_compress_lu(e, res->tt, tolerance, maxbonddim, normalizeerror != 0);
+  if (!rc) rc = tt4_compress(e, res->tt, tolerance, maxbonddim, normalizeerror != 0, method == TCI_FACTORIZE_CI);
   if (rc) {
     res->tt.release(e);
     return rc;

@@ -1,6 +1,6 @@
 // Tensor-train contraction on the device: contract_naive (contraction.jl:351-372),
 // contract_zipup with rrLU factorization (contraction.jl:442-486 with
-// _factorize(:LU), tensortrain.jl:95-110) and compress!(:LU)
+// _factorize(:LU) or _factorize(:CI), tensortrain.jl:94-110) and compress!(:LU / :CI)
 // (tensortrain.jl:149-183).  The rank-revealing LUs are RRLU tasks of the step
 // kernel (bit-exact pivots); the contractions are the fixed-order kernels of
 // contract.cu, so every result equals the CPU oracle's bit for bit.
@@ -18,6 +18,8 @@ cudaError_t tci_zip_c_launch(const double* RA, const double* B, double* C, int n
                              int spp, int nbn2, cudaStream_t st);
 cudaError_t tci_lu_left_right_launch(const double* F, const int32_t* rowperm, const int32_t* colperm, int m, int n,
                                      int K, int leftorth, double* left, double* right, cudaStream_t st);
+cudaError_t tci_luci_left_right_launch(const double* F, const int32_t* rowperm, const int32_t* colperm, int m,
+                                       int n, int K, int leftorth, double* left, double* right, cudaStream_t st);
 cudaError_t tci_gemm_launch(const double* A, int64_t lda, const double* B, int64_t ldb, double* C, int64_t ldc,
                             int M, int N, int K, cudaStream_t st);
 
@@ -64,9 +66,11 @@ void TT4::release(Engine& e) {
 }
 
 // rrlu(A; maxrank, reltol, abstol, leftorthogonal) on a device matrix, then
-// left(lu) (m x K) and right(lu) (K x n) into new device arrays.
+// left (m x K) and right (K x n) into new device arrays: those of the rrLU
+// (matrixlu.jl:374-392), or with ci those of MatrixLUCI (matrixluci.jl:40-84).
 int device_rrlu_left_right(Engine& e, const double* A, int64_t m, int64_t n, int64_t maxrank, double reltol,
-                           double abstol, bool leftorth, double** left, double** right, int64_t* npivot) {
+                           double abstol, bool leftorth, double** left, double** right, int64_t* npivot,
+                           bool ci) {
   *left = *right = nullptr;
   if (m > 65535 || n > 65535 || m * n > INT_MAX)
     return fail(TCI_ERR_TOO_LARGE, "matrix too large for the rrLU kernel");
@@ -95,8 +99,12 @@ int device_rrlu_left_right(Engine& e, const double* A, int64_t m, int64_t n, int
   Buf L(e, (size_t)std::max<int64_t>(m * K, 1)), U(e, (size_t)std::max<int64_t>(K * n, 1));
   if (!L.p || !U.p) return fail(TCI_ERR_OOM, "device memory for the factors");
   const int32_t* perms = (const int32_t*)(F.p + m * n);
-  CT_TRY(tci_lu_left_right_launch(F.p, perms, perms + m, (int)m, (int)n, (int)K, leftorth ? 1 : 0, L.p, U.p,
-                                  e.stream()));
+  if (ci)
+    CT_TRY(tci_luci_left_right_launch(F.p, perms, perms + m, (int)m, (int)n, (int)K, leftorth ? 1 : 0, L.p, U.p,
+                                      e.stream()));
+  else
+    CT_TRY(tci_lu_left_right_launch(F.p, perms, perms + m, (int)m, (int)n, (int)K, leftorth ? 1 : 0, L.p, U.p,
+                                    e.stream()));
   CT_TRY(cudaStreamSynchronize(e.stream()));  // F goes back to the pool below
   *left = L.take();
   *right = U.take();
@@ -144,7 +152,8 @@ int tt4_contract_naive(Engine& e, const TT4& a, const TT4& b, TT4& out) {
 }
 
 // contract_zipup(A, B; tolerance, method=:LU, maxbonddim) (contraction.jl:442-486).
-int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, int64_t maxbonddim, TT4& out) {
+int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, int64_t maxbonddim, TT4& out,
+                       bool ci) {
   out.cores.clear();
   const size_t L = a.cores.size();
   // R: (link_ab, link_an, link_bn), starts as ones(1, 1, 1)
@@ -183,7 +192,8 @@ int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, 
     int64_t K = 0;
     CT_TRY(cudaStreamSynchronize(e.stream()));
     // _factorize(Cmat, :LU; tolerance, maxbonddim): reltol = tolerance, leftorthogonal = false
-    int rc = device_rrlu_left_right(e, C.p, c_rows, c_cols, maxbonddim, tolerance, 0.0, false, &left, &right, &K);
+    int rc =
+        device_rrlu_left_right(e, C.p, c_rows, c_cols, maxbonddim, tolerance, 0.0, false, &left, &right, &K, ci);
     if (rc) {
       out.release(e);
       return rc;
@@ -200,8 +210,8 @@ int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, 
   return 0;
 }
 
-// compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183).
-int tt4_compress_lu(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bool normalizeerror) {
+// compress!(tt, :LU or :CI; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183).
+int tt4_compress(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bool normalizeerror, bool ci) {
   const size_t L = tt.cores.size();
   auto rest = [](const Tensor4& c) { return c.d[1] * c.d[2]; };
   // left to right, no truncation, left-orthogonal
@@ -211,7 +221,7 @@ int tt4_compress_lu(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bo
     const int64_t m = c.d[0] * rest(c), ncol = c.d[3];
     double *left = nullptr, *right = nullptr;
     int64_t K = 0;
-    int rc = device_rrlu_left_right(e, c.p, m, ncol, 0, 0.0, 0.0, true, &left, &right, &K);
+    int rc = device_rrlu_left_right(e, c.p, m, ncol, 0, 0.0, 0.0, true, &left, &right, &K, ci);
     if (rc) return rc;
     const int64_t nrest = rest(nx) * nx.d[3];
     double* nt = e.alloc_core((size_t)std::max<int64_t>(K * nrest, 1));
@@ -241,7 +251,8 @@ int tt4_compress_lu(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bo
     int64_t K = 0;
     const double reltol = normalizeerror ? tolerance : 1e-14;
     const double abstol = normalizeerror ? 0.0 : tolerance;
-    int rc = device_rrlu_left_right(e, c.p, mrow, ncol, maxbonddim, reltol, abstol, false, &left, &right, &K);
+    int rc =
+        device_rrlu_left_right(e, c.p, mrow, ncol, maxbonddim, reltol, abstol, false, &left, &right, &K, ci);
     if (rc) return rc;
     const int64_t prow = pv.d[0] * rest(pv);
     double* nt = e.alloc_core((size_t)std::max<int64_t>(prow * K, 1));

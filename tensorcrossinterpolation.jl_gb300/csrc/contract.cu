@@ -111,6 +111,67 @@ __global__ void lu_left_right_kernel(const double* __restrict__ F, const int32_t
   }
 }
 
+// MatrixLUCI left/right (matrixluci.jl:40-84) from the factored matrix F as
+// above: one thread per row of left (m threads), then one per column of right
+// (n threads), each in the order of the oracle's loops (separate multiply,
+// add/subtract and divide).
+//   leftorth:  left = colstimespivotinv (rows K.. of L against LowerTriangular(L11),
+//              rows scattered by rowperm), right = rowmatrix = L[1:K, :] * right(lu)
+//   !leftorth: left = colmatrix = left(lu) * U[:, 1:K], right = pivotinvtimesrows
+//              (UpperTriangular(U11) \ U12, columns scattered by colperm)
+__device__ __forceinline__ double f_L(const double* F, int m, int i, int p, int leftorth) {
+  return i < p ? 0.0 : (i == p && leftorth ? 1.0 : F[i + (int64_t)m * p]);
+}
+__device__ __forceinline__ double f_U(const double* F, int m, int p, int j, int leftorth) {
+  return p > j ? 0.0 : (p == j && !leftorth ? 1.0 : F[p + (int64_t)m * j]);
+}
+
+__global__ void luci_left_right_kernel(const double* __restrict__ F, const int32_t* __restrict__ rowperm,
+                                       const int32_t* __restrict__ colperm, int m, int n, int K, int leftorth,
+                                       double* __restrict__ left, double* __restrict__ right) {
+  for (int64_t e = gtid(); e < (int64_t)m + n; e += gstride()) {
+    if (e < m) {
+      const int i = (int)e;
+      double* out = left + rowperm[i];  // out[q * m] = entry (rowperm[i], q)
+      if (leftorth) {
+        if (i < K) {
+          for (int q = 0; q < K; ++q) out[(int64_t)m * q] = i == q ? 1.0 : 0.0;
+        } else {
+          for (int q = K - 1; q >= 0; --q) {
+            double s = f_L(F, m, i, q, 1);
+            for (int p = q + 1; p < K; ++p) s = __dsub_rn(s, __dmul_rn(out[(int64_t)m * p], f_L(F, m, p, q, 1)));
+            out[(int64_t)m * q] = __ddiv_rn(s, f_L(F, m, q, q, 1));
+          }
+        }
+      } else {
+        for (int q = 0; q < K; ++q) {
+          double s = 0.0;
+          for (int p = 0; p <= q; ++p) s = __dadd_rn(s, __dmul_rn(f_L(F, m, i, p, 0), f_U(F, m, p, q, 0)));
+          out[(int64_t)m * q] = s;
+        }
+      }
+    } else {
+      const int j = (int)(e - m);
+      double* out = right + (int64_t)K * colperm[j];  // out[q] = entry (q, colperm[j])
+      if (leftorth) {
+        for (int q = 0; q < K; ++q) {
+          double s = 0.0;
+          for (int p = 0; p <= q; ++p) s = __dadd_rn(s, __dmul_rn(f_L(F, m, q, p, 1), f_U(F, m, p, j, 1)));
+          out[q] = s;
+        }
+      } else if (j < K) {
+        for (int q = 0; q < K; ++q) out[q] = j == q ? 1.0 : 0.0;
+      } else {
+        for (int q = K - 1; q >= 0; --q) {
+          double s = f_U(F, m, q, j, 0);
+          for (int p = q + 1; p < K; ++p) s = __dsub_rn(s, __dmul_rn(f_U(F, m, q, p, 0), out[p]));
+          out[q] = __ddiv_rn(s, f_U(F, m, q, q, 0));
+        }
+      }
+    }
+  }
+}
+
 // C (M x N) = A (M x K) * B (K x N), column-major with leading dimensions.
 __global__ void gemm_kernel(const double* __restrict__ A, int64_t lda, const double* __restrict__ B, int64_t ldb,
                             double* __restrict__ C, int64_t ldc, int M, int N, int K) {
@@ -158,6 +219,14 @@ cudaError_t tci_lu_left_right_launch(const double* F, const int32_t* rowperm, co
   const int64_t total = (left ? (int64_t)m * K : 0) + (right ? (int64_t)K * n : 0);
   if (total == 0) return cudaSuccess;
   lu_left_right_kernel<<<grid_for(total), CT, 0, st>>>(F, rowperm, colperm, m, n, K, leftorth, left, right);
+  return cudaGetLastError();
+}
+
+cudaError_t tci_luci_left_right_launch(const double* F, const int32_t* rowperm, const int32_t* colperm, int m,
+                                       int n, int K, int leftorth, double* left, double* right, cudaStream_t st) {
+  const int64_t total = (int64_t)m + n;
+  if (K == 0 || total == 0) return cudaSuccess;
+  luci_left_right_kernel<<<grid_for(total), CT, 0, st>>>(F, rowperm, colperm, m, n, K, leftorth, left, right);
   return cudaGetLastError();
 }
 

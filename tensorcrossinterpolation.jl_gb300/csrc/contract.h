@@ -26,9 +26,12 @@ int tt4_check_pair(const TT4& a, const TT4& b, bool sites_must_match);
 int tt4_check(const TT4& t);
 
 int tt4_contract_naive(Engine& e, const TT4& a, const TT4& b, TT4& out);
-int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, int64_t maxbonddim, TT4& out);
-int tt4_compress_lu(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bool normalizeerror);
+// ci selects _factorize(:CI) (MatrixLUCI's left/right) over _factorize(:LU).
+int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, int64_t maxbonddim, TT4& out,
+                       bool ci = false);
+int tt4_compress(Engine& e, TT4& tt, double tolerance, int64_t maxbonddim, bool normalizeerror, bool ci = false);
 int device_rrlu_left_right(Engine& e, const double* A, int64_t m, int64_t n, int64_t maxrank, double reltol,
-                           double abstol, bool leftorth, double** left, double** right, int64_t* npivot);
+                           double abstol, bool leftorth, double** left, double** right, int64_t* npivot,
+                           bool ci = false);
 
 }  // namespace tci

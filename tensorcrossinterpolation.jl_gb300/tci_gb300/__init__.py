@@ -27,6 +27,7 @@ BATCH_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctype
 TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
 TCI_CONTRACT_NAIVE, TCI_CONTRACT_ZIPUP = 1, 2
+FACTORIZE = {"LU": 0, "CI": 1}  # _factorize methods on the device (tensortrain.jl:94-137)
 SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
 FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5, "product": 6}
 
@@ -154,10 +155,11 @@ _SIGNATURES = {
                                                 ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]),
     "tci_fp64_peak": (ctypes.c_int, [ctypes.c_size_t, F64P, F64P]),
     "tci_tt4_contract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
-                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_double, ctypes.c_int64,
+                                        ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                        ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_tt4_compress": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, ctypes.c_int32,
+                                        ctypes.c_double, ctypes.c_int64, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_void_p)]),
-    "tci_tt4_compress": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, ctypes.c_double,
-                                        ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]),
     "tci_tt4_length": (ctypes.c_int32, [ctypes.c_void_p]),
     "tci_tt4_dims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
     "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
@@ -665,8 +667,8 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     """contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) of
     tensor trains with 4-leg cores (A's third leg against B's second), or of a
     3-leg train with a 4-leg one.  algorithm "naive" or "zipup"; factorizations
-    use the rank-revealing LU (method "LU") -- the reference's SVD is not on the
-    device.  Returns a TensorTrain."""
+    use the rank-revealing LU (method "LU") or MatrixLUCI over it (method "CI")
+    -- the reference's SVD is not on the device.  Returns a TensorTrain."""
     if f is not None and algorithm != "TCI":
         raise TCIError(TCI_ERR_GENERIC, f"{algorithm.capitalize()} contraction implementation cannot contract "
                        "matrix product with a function. Use algorithm=:TCI instead.")
@@ -675,8 +677,8 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     alg = {"naive": TCI_CONTRACT_NAIVE, "zipup": TCI_CONTRACT_ZIPUP}.get(algorithm)
     if alg is None:
         raise ArgumentError(TCI_ERR_ARG, f"Unknown algorithm {algorithm}.")
-    if method != "LU":
-        raise ArgumentError(TCI_ERR_ARG, "only method=:LU is available on the device")
+    if method not in FACTORIZE:
+        raise TCIError(TCI_ERR_GENERIC, f"method=:{method} is not available on the device (:LU, :CI)")
     ctx = ctx or default_context()
     a, a3 = _as_tt4(A, True)
     b, b3 = _as_tt4(B, False)
@@ -686,7 +688,8 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     b, bd, bp = _tt4_args(b)
     h = ctypes.c_void_p()
     _check(load_library().tci_tt4_contract(ctx.h, len(a), _p(ad, I64P), ap, _p(bd, I64P), bp, alg,
-                                           float(tolerance), int(maxbonddim or 0), ctypes.byref(h)))
+                                           FACTORIZE[method], float(tolerance), int(maxbonddim or 0),
+                                           ctypes.byref(h)))
     cores = _tt4_fetch(h)
     if a3 or b3:  # TensorTrain{3}(tt, prod.(sitedims(tt)))
         cores = [c.reshape((c.shape[0], c.shape[1] * c.shape[2], c.shape[3]), order="F") for c in cores]
@@ -694,16 +697,18 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
 
 
 def compress(tt, method="LU", tolerance=1e-12, maxbonddim=None, normalizeerror=True, ctx=None):
-    """compress!(tt, :LU; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
-    on a train with 4-leg (or 3-leg) cores; returns a new TensorTrain."""
-    if method != "LU":
-        raise ArgumentError(TCI_ERR_ARG, "only method=:LU is available on the device")
+    """compress!(tt, method; tolerance, maxbonddim, normalizeerror) (tensortrain.jl:149-183)
+    with method "LU" or "CI" on a train with 4-leg (or 3-leg) cores; returns a new
+    TensorTrain."""
+    if method not in FACTORIZE:
+        raise TCIError(TCI_ERR_GENERIC, f"method=:{method} is not available on the device (:LU, :CI)")
     ctx = ctx or default_context()
     cores, three = _as_tt4(tt, True)
     cores, d, ptrs = _tt4_args(cores)
     h = ctypes.c_void_p()
-    _check(load_library().tci_tt4_compress(ctx.h, len(cores), _p(d, I64P), ptrs, float(tolerance),
-                                           int(maxbonddim or 0), int(bool(normalizeerror)), ctypes.byref(h)))
+    _check(load_library().tci_tt4_compress(ctx.h, len(cores), _p(d, I64P), ptrs, FACTORIZE[method],
+                                           float(tolerance), int(maxbonddim or 0), int(bool(normalizeerror)),
+                                           ctypes.byref(h)))
     out = _tt4_fetch(h)
     if three:
         out = [c.reshape((c.shape[0], c.shape[2], c.shape[3]), order="F") for c in out]

@@ -1,4 +1,4 @@
-"""GPU tensor-train contraction (contract :naive / :zipup with rrLU, compress!(:LU))
+"""GPU tensor-train contraction (contract :naive / :zipup, compress! with :LU and :CI)
 against the CPU oracle.  Both sum every contracted element in the same fixed
 order with separate multiply and add and factor with the same bit-exact rrLU,
 so the cores must be equal bit for bit; against dense products the results
@@ -101,3 +101,22 @@ def test_contract_errors_like_reference(T):
         T.contract(a, a, algorithm="naive", f=lambda x: 2 * x)
     with pytest.raises(T.ArgumentError, match="Unknown algorithm"):
         T.contract(a, a, algorithm="bogus")
+
+
+def test_ci_factorization_bitwise(T, oracle):
+    """compress!(:CI) and contract(:zipup / :naive, method=:CI): MatrixLUCI's
+    left/right (matrixluci.jl:40-84) on the device equal the oracle's bit for bit."""
+    rng = np.random.default_rng(18)
+    tt = _rand_tt(rng, [1, 6, 9, 9, 6, 1], [2] * 5, [2] * 5)
+    for tol, mb, ne in [(1e-12, None, True), (1e-3, None, True), (1e-12, 4, True), (1e-8, None, False)]:
+        got = T.compress(tt, method="CI", tolerance=tol, maxbonddim=mb, normalizeerror=ne)
+        _same(got, oracle.tt4_compress(tt, "CI", tolerance=tol, maxbonddim=mb, normalizeerror=ne))
+    a = _rand_tt(rng, [1, 4, 6, 6, 4, 1], [2] * 5, [3] * 5)
+    b = _rand_tt(rng, [1, 3, 5, 5, 3, 1], [3] * 5, [2] * 5)
+    for algorithm in ["zipup", "naive"]:
+        ab = T.contract(a, b, algorithm=algorithm, tolerance=1e-10, method="CI")
+        _same(ab, oracle.tt4_contract(a, b, algorithm, tolerance=1e-10, method="CI"))
+        ref = oracle.tt4_full(a) @ oracle.tt4_full(b)
+        assert np.allclose(oracle.tt4_full(ab.sitetensors), ref, rtol=1e-7, atol=1e-9 * np.abs(ref).max())
+    with pytest.raises(T.TCIError, match="not available"):
+        T.compress(tt, method="SVD")

@@ -51,3 +51,20 @@ def test_zipup_truncation_and_compress(oracle):
     comp = oracle.tt4_compress(naive, tolerance=1e-10)
     assert [c.shape[3] for c in comp[:-1]] == [4, 16, 16, 4]  # the exact ranks of the 2-by-2 product
     assert np.allclose(oracle.tt4_full(comp), ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("method", ["LU", "CI"])
+def test_factorization_methods(oracle, method):
+    """compress!(:LU / :CI) and contract_zipup(method) reproduce the dense product
+    (tensortrain.jl:94-110: _factorize with rrlu or MatrixLUCI)."""
+    rng = np.random.default_rng(4)
+    a = _rand_tt(rng, [1, 4, 6, 6, 4, 1], [2] * 5, [2] * 5)
+    b = _rand_tt(rng, [1, 3, 5, 5, 3, 1], [2] * 5, [2] * 5)
+    ref = oracle.tt4_full(a) @ oracle.tt4_full(b)
+    naive = oracle.tt4_contract(a, b, "naive", tolerance=0.0)
+    comp = oracle.tt4_compress(naive, method, tolerance=1e-10)
+    assert [c.shape[3] for c in comp[:-1]] == [4, 16, 16, 4]
+    assert np.allclose(oracle.tt4_full(comp), ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+    zu = oracle.tt4_contract(a, b, "zipup", tolerance=1e-12, method=method)
+    assert np.allclose(oracle.tt4_full(zu), ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
+
