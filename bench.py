@@ -241,6 +241,25 @@ def single_solve_configs(T, ctx, with_cpu=True):
         tc, (ref, rr, _) = _best_of(lambda: O.crossinterpolate2([10] * 8, O.F_LORENTZ, [], None, **kw))
         c.update(cpu_s=tc, cpu_threads=1, same_ranks=list(rr) == list(ranks))
     out["lorentz8"] = c
+    # the same solve with f supplied by the caller (numpy, evaluated on the host
+    # for the points the device cache misses)
+    def lorentz_np(p):
+        return 1.0 / (1.0 + (p.astype(np.int64) ** 2).sum(1))
+
+    counts = []
+
+    def solve_batchfn():
+        bf = T.BatchFunction(lorentz_np)
+        res = T.crossinterpolate2(float, bf, [10] * 8, ctx=ctx, **kw)
+        counts.append((bf.npoints, bf.ncalls))
+        return res
+
+    t, (tci_b, ranks_b, _) = _best_of(solve_batchfn)
+    cb = {"gpu_s": t, "rank": int(tci_b.rank()), "same_ranks_as_device_f": list(ranks_b) == list(ranks),
+          "f_points": counts[-1][0], "f_calls": counts[-1][1]}
+    if O:
+        cb["oracle_f_points"] = int(ref.nfeval)
+    out["lorentz8_caller_f"] = cb
     # quantics 1-D, R = 40, tol 1e-10, maxbonddim 128; 1e6 seeded points
     kw = dict(tolerance=1e-10, maxbonddim=128, maxiter=20)
     f = T.DeviceFunction("qtt1d", [0])
