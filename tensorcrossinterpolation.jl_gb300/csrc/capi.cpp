@@ -72,6 +72,40 @@ std::vector<std::vector<uint8_t>> to_pivots(const int64_t* piv, int64_t np, int 
   return out;
 }
 
+// Points (np x L, row-major, 1-based int64) -> flat 0-based uint8 multi-indices,
+// range-checked; large inputs are split over host threads.
+int pack_points(const int64_t* pts, int64_t np, int L, const std::vector<int>& d, std::vector<uint8_t>& out) {
+  out.resize((size_t)np * (size_t)L);
+  auto run = [&](int64_t p0, int64_t p1) {
+    bool ok = true;
+    for (int64_t p = p0; p < p1; ++p) {
+      const int64_t* x = pts + p * L;
+      uint8_t* o = out.data() + (size_t)p * L;
+      for (int q = 0; q < L; ++q) {
+        ok &= x[q] >= 1 && x[q] <= d[q];
+        o[q] = (uint8_t)(x[q] - 1);
+      }
+    }
+    return ok;
+  };
+  const int64_t work = np * (int64_t)L;
+  int nt = work >= (1 << 22) ? (int)std::min<int64_t>(8, std::max(1u, std::thread::hardware_concurrency())) : 1;
+  bool ok = true;
+  if (nt == 1) {
+    ok = run(0, np);
+  } else {
+    std::vector<std::thread> th;
+    std::vector<char> res(nt, 1);
+    const int64_t per = (np + nt - 1) / nt;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t] { res[t] = run(std::min(np, t * per), std::min(np, (t + 1) * per)); });
+    for (auto& x : th) x.join();
+    for (char r : res) ok &= r != 0;
+  }
+  if (!ok) return fail(TCI_ERR_ARG, "pivot index out of range");
+  return 0;
+}
+
 double now_s() {
   using namespace std::chrono;
   return duration<double>(steady_clock::now().time_since_epoch()).count();
@@ -539,18 +573,14 @@ int tci_get_history(const tci_solve* s, int64_t* ranks, double* errors, int64_t*
 
 int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out) {
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
-  int rc = 0;
-  auto piv = to_pivots(points, np, s->s.L, s->s.d, &rc);
-  if (rc) return rc;
   std::vector<uint8_t> pts;
-  pts.reserve((size_t)np * s->s.L);
-  for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
+  int rc = pack_points(points, np, s->s.L, s->s.d, pts);
+  if (rc) return rc;
   // up to 2^20 points per engine step (split into tasks inside co_evaluate)
   const int64_t chunk = 1 << 20;
   for (int64_t b = 0; b < np; b += chunk) {
     int64_t n = std::min(chunk, np - b);
-    std::vector<uint8_t> sub(pts.begin() + b * s->s.L, pts.begin() + (b + n) * s->s.L);
-    CoTask t = co_evaluate(s->ctx->eng_ref(), s->s, sub, n, nullptr, out + b);
+    CoTask t = co_evaluate(s->ctx->eng_ref(), s->s, pts.data() + b * s->s.L, n, nullptr, out + b);
     rc = run_solve(s->ctx, s->s, t);
     if (rc) return rc;
   }
@@ -966,15 +996,13 @@ int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams,
   Solve s;
   int rc = solve_init(s, L, localdims, fid, fparams, nparams, nullptr, 0);
   if (rc) return rc;
-  auto piv = to_pivots(points, np, L, s.d, &rc);
+  std::vector<uint8_t> pts;
+  rc = pack_points(points, np, L, s.d, pts);
   if (rc) return rc;
   const int64_t chunk = 1 << 20;
   for (int64_t b = 0; b < np; b += chunk) {
     int64_t n = std::min(chunk, np - b);
-    std::vector<uint8_t> pts;
-    pts.reserve((size_t)n * L);
-    for (int64_t i = b; i < b + n; ++i) pts.insert(pts.end(), piv[i].begin(), piv[i].end());
-    CoTask t = co_evaluate(ctx->eng_ref(), s, pts, n, out + b, nullptr);
+    CoTask t = co_evaluate(ctx->eng_ref(), s, pts.data() + b * L, n, out + b, nullptr);
     rc = run_solve(ctx, s, t);
     if (rc) return rc;
   }
@@ -1273,16 +1301,13 @@ int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* 
   Solve s;
   int rc = upload_tt3(e, L, dims, cores, s);
   if (rc) return rc;
-  auto piv = to_pivots(points, np, L, s.d, &rc);
+  std::vector<uint8_t> pts;
+  rc = pack_points(points, np, L, s.d, pts);
   if (!rc) {
-    std::vector<uint8_t> pts;
-    pts.reserve((size_t)np * L);
-    for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
     const int64_t chunk = 1 << 20;
     for (int64_t b = 0; b < np && !rc; b += chunk) {
       const int64_t n = std::min(chunk, np - b);
-      std::vector<uint8_t> sub(pts.begin() + b * L, pts.begin() + (b + n) * L);
-      CoTask t = co_evaluate(e, s, sub, n, nullptr, out + b);
+      CoTask t = co_evaluate(e, s, pts.data() + b * L, n, nullptr, out + b);
       rc = e.run(t);
     }
   }

@@ -1578,7 +1578,7 @@ static void core_table(const Solve& s, std::vector<tci_core_ref>& tab, int& rmax
 }
 
 // f and the train at points (np x L, 0-based bytes).  ttout may be null.
-CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np, double* fout,
+CoTask co_evaluate(Engine& e, Solve& s, const uint8_t* pts, i64 np, double* fout,
                    double* ttout) {
   if (ttout && !s.cores_valid) co_return fail(TCI_ERR_GENERIC, "site tensors are not available");
   std::vector<tci_core_ref> tab;
@@ -1600,7 +1600,7 @@ CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np,
     }
     r.t.m = (int32_t)n;
     r.t.nl = s.L;
-    r.rows = pts.data() + (size_t)p0 * s.L;
+    r.rows = pts + (size_t)p0 * s.L;
     r.rows_bytes = (size_t)n * s.L;
     if (ttout) {
       r.cores = tab.data();

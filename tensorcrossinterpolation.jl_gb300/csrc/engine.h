@@ -365,7 +365,7 @@ CoTask co_sweep2site(Engine& e, Solve& s, int niter, int iter1, double abstol, i
 CoTask co_sweep1site(Engine& e, Solve& s, bool forward, double reltol, double abstol, i64 maxbonddim,
                      bool updatetensors);
 CoTask co_fillsitetensors(Engine& e, Solve& s);
-CoTask co_evaluate(Engine& e, Solve& s, const std::vector<uint8_t>& pts, i64 np, double* fout,
+CoTask co_evaluate(Engine& e, Solve& s, const uint8_t* pts, i64 np, double* fout,
                    double* ttout);
 int addglobalpivots(Solve& s, const std::vector<std::vector<uint8_t>>& pivots);
 i64 solve_rank(const Solve& s);

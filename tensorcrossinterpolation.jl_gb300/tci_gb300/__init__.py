@@ -11,6 +11,7 @@ Indices are 1-based, as in Julia.  Matrices are numpy arrays; site tensors are
 returned as (r_{b-1}, d_b, r_b) arrays.
 """
 import ctypes
+import threading
 import weakref
 import os
 
@@ -209,11 +210,20 @@ def exported_symbols():
     return list(_SIGNATURES)
 
 
+_cb_state = threading.local()  # the exception a BatchFunction's f raised on this thread
+
+
 def _check(rc):
     if rc:
         msg = load_library().tci_last_error()
         msg = msg.decode() if msg else ""
-        raise _EXC.get(rc, TCIError)(rc, msg or f"error code {rc}")
+        err = _EXC.get(rc, TCIError)(rc, msg or f"error code {rc}")
+        pending = getattr(_cb_state, "error", None)
+        _cb_state.error = None
+        if pending is not None and rc == TCI_ERR_GENERIC:
+            raise pending from err  # the caller's own exception, not the library's code
+        raise err
+    _cb_state.error = None
 
 
 def _p(a, t):
@@ -292,7 +302,8 @@ class BatchFunction:
     multi-index.  Each solve keeps the values it has asked for in a device hash
     table (CachedFunction, cachedfunction.jl:8-184) and calls f only for points
     it has not seen, once per device step that needs new values.  An exception
-    raised by f makes the library call fail; it is kept in ``self.error``."""
+    raised by f ends the library call and is re-raised to its caller (and kept
+    in ``self.error``)."""
 
     def __init__(self, f):
         self.f = f
@@ -314,6 +325,7 @@ class BatchFunction:
                 return 0
             except BaseException as e:  # reported through the library's error code
                 self.error = e
+                _cb_state.error = e
                 return 1
 
         self._cb = BATCH_FN(_call)

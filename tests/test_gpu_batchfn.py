@@ -135,8 +135,9 @@ def test_batch_errors(T):
         raise RuntimeError("no values")
 
     bf = T.BatchFunction(boom)
-    with pytest.raises(T.TCIError):
+    with pytest.raises(RuntimeError, match="no values") as ei:
         T.crossinterpolate2(float, bf, [4] * 4, tolerance=1e-8)
+    assert isinstance(ei.value.__cause__, T.TCIError)
     assert isinstance(bf.error, RuntimeError)
 
     def nan_at(p):
