@@ -348,6 +348,22 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
  * with method = :LU or :CI. */
 int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, int32_t method,
                      double tolerance, int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out);
+/* contract(A, B; algorithm = :TCI, tolerance, maxbonddim, f, initialpivots, kwargs...)
+ * (contraction.jl:399-434, 515-545): crossinterpolate2 of the Contraction evaluator
+ * (contraction.jl:5-62, 103-335), which runs on the device with its left/right
+ * environment caches; f values are cached per point.  Local indices of the
+ * interpolated function fuse A's s_in and B's s_out (A's fastest, at most 256).
+ * initialpivots: np x L fused, 1-based; np = 0 draws ninitialpivots random starts
+ * from opts->seed and improves each with optfirstpivot (util.jl:78-108).  f, if
+ * not NULL, maps values in place (values[k] = f(values[k])).  opts carries the
+ * crossinterpolate2 keywords (tolerance, maxbonddim, ...).  Errors as the
+ * reference: different lengths or site dimensions -> TCI_ERR_ARG, no pivot with
+ * a nonzero value -> TCI_ERR_GENERIC. */
+typedef int (*tci_value_fn)(void* user, int64_t n, double* values);
+int tci_tt4_contract_tci(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
+                         const int64_t* b_dims, const double* const* b_cores, const int64_t* initialpivots,
+                         int64_t np, int32_t ninitialpivots, tci_value_fn f, void* user, const tci_opts* opts,
+                         tci_tt4** out);
 int32_t tci_tt4_length(const tci_tt4* t);
 int tci_tt4_dims(const tci_tt4* t, int64_t* dims);
 int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out); /* b is 1-based */

@@ -135,6 +135,10 @@ def lib():
         L.orc_tt4_compress.restype = ctypes.c_void_p
         L.orc_tt4_compress.argtypes = [ctypes.c_int, I64P, F64P, ctypes.c_int, ctypes.c_double, ctypes.c_int64,
                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.orc_tt4_contract_tci.restype = ctypes.c_void_p
+        L.orc_tt4_contract_tci.argtypes = [ctypes.c_int, I64P, F64P, I64P, F64P, I64P, ctypes.c_int64, ctypes.c_int,
+                                           VALUE_FN, ctypes.c_void_p, ctypes.POINTER(Opts),
+                                           ctypes.POINTER(ctypes.c_int)]
         L.orc_tt4_length.argtypes = [ctypes.c_void_p]
         L.orc_tt4_dims.argtypes = [ctypes.c_void_p, I64P]
         L.orc_tt4_core.argtypes = [ctypes.c_void_p, ctypes.c_int, F64P]
@@ -497,6 +501,36 @@ def tt4_compress(cores, method="LU", tolerance=1e-12, maxbonddim=None, normalize
     rc = ctypes.c_int()
     h = lib().orc_tt4_compress(len(cores), _p(d, I64P), _p(v, F64P), METHODS[method], float(tolerance),
                                int(maxbonddim or 0), int(bool(normalizeerror)), ctypes.byref(rc))
+    return _tt4_unpack(h, rc)
+
+
+VALUE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, F64P)
+
+
+def tt4_contract_tci(a, b, initialpivots=10, f=None, **kw):
+    """contract(a, b; algorithm=:TCI, f, initialpivots, kwargs...) (contraction.jl:399-434);
+    returns the list of cores (legs split)."""
+    ad, av = _tt4_pack(a)
+    bd, bv = _tt4_pack(b)
+    L = len(a)
+    if isinstance(initialpivots, (int, np.integer)):
+        piv, ninit = np.zeros((0, L), np.int64), int(initialpivots)
+    else:
+        piv, ninit = np.ascontiguousarray(initialpivots, dtype=np.int64).reshape(-1, L), 0
+    cb = None
+    if f is not None:
+        def _call(user, n, vals):
+            v = np.ctypeslib.as_array(vals, shape=(n,))
+            v[:] = np.asarray(f(v.copy()), dtype=np.float64).reshape(-1)
+            return 0
+        cb = VALUE_FN(_call)
+        _registered.append(cb)
+    o = make_opts(**kw)
+    rc = ctypes.c_int()
+    h = lib().orc_tt4_contract_tci(L, _p(ad, I64P), _p(av, F64P), _p(bd, I64P), _p(bv, F64P),
+                                   _p(piv, I64P) if piv.size else None, piv.shape[0], ninit,
+                                   cb if cb is not None else VALUE_FN(), None,
+                                   ctypes.byref(o), ctypes.byref(rc))
     return _tt4_unpack(h, rc)
 
 

@@ -25,6 +25,8 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <memory>
+#include <unordered_map>
 #include <string>
 #include <thread>
 #include <unordered_set>
@@ -59,11 +61,15 @@ enum { F_LORENTZ = 1, F_SERVED = 2, F_QTT1D = 3, F_QTT2D = 4, F_DENSE = 5, F_PRO
 typedef int (*orc_batch_fn)(void* user, int32_t L, int64_t npoints, const int64_t* points, double* values);
 constexpr int F_USER = 1024;
 
+struct OrcContraction;  // the Contraction evaluator of contract(algorithm = :TCI), below
+double contraction_point(OrcContraction& c, const MultiIndex& v);
+
 struct Func {
   int fid = 0;
   std::vector<double> params;
   orc_batch_fn cb = nullptr;
   void* user = nullptr;
+  std::shared_ptr<OrcContraction> ctr;
   // values at many points through one evaluator call (filltensor on a
   // BatchEvaluator, batcheval.jl:67-83); NaN everywhere if the evaluator fails
   void batch(int L, int64_t np, const int64_t* pts, double* out) const {
@@ -72,6 +78,7 @@ struct Func {
   }
   double operator()(const MultiIndex& v) const {
     const int L = (int)v.size();
+    if (ctr) return contraction_point(*ctr, v);
     if (cb) {
       std::vector<int64_t> p(v.begin(), v.end());
       double out = NaN;
@@ -459,8 +466,16 @@ struct TCI2 {
 
 // filltensor(..., Val(0)) over explicit row/col multi-index lists (tensorci2.jl:290-312,
 // batcheval.jl:32-61).  Column-major |I| x |J|.
+void contraction_fill(OrcContraction& c, const std::vector<MultiIndex>& I, const std::vector<MultiIndex>& J,
+                      std::vector<double>& out);
+
 std::vector<double> fill(TCI2& t, const std::vector<MultiIndex>& I, const std::vector<MultiIndex>& J) {
   std::vector<double> out(I.size() * J.size());
+  if (t.f.ctr) {
+    contraction_fill(*t.f.ctr, I, J, out);
+    t.nfeval += (i64)out.size();
+    return out;
+  }
   if (t.f.cb) {  // one evaluator call for the whole block, column-major
     std::vector<int64_t> pts;
     pts.reserve(out.size() * (size_t)t.L);
@@ -1089,6 +1104,168 @@ TT4 read_tt4(int L, const int64_t* dims, const double* values) {
   return t;
 }
 
+// ---------------------------------------------------------------- Contraction
+// The Contraction batch evaluator (contraction.jl:5-62, 103-335) over two trains
+// of 4-leg cores, for contract(algorithm = :TCI).  Fused local index v (0-based)
+// = i + s_in(A) * j (_unfuse_idx, :95-97).  Environments follow _extend_cache
+// (:103-109): left  tmp[b, t, a'] = sum_a P[a, b] A[a, i, t, a'],
+// E[a', b'] = sum over (b, t), b fastest, of tmp[b, t, a'] B[b, t, j, b'];
+// right the same with the cores' link legs swapped (:165-169).  A Pi element is
+// sum over (a, b), a fastest, of Lenv[a, b] Renv[a, b] (:325-329); a single point
+// is its full left environment.  Values are cached per point, the first request
+// fixing the value (the device evaluator sits behind a value cache).
+typedef int (*orc_value_fn)(void* user, int64_t n, double* values);
+
+struct OrcContraction {
+  TT4 a, b;
+  int L = 0;
+  orc_value_fn vf = nullptr;
+  void* vuser = nullptr;
+  std::unordered_map<std::string, std::vector<double>> left, right;
+  std::unordered_map<std::string, double> values;
+};
+
+std::string key_of(const MultiIndex& v, size_t from, size_t to) {
+  std::string k;
+  for (size_t q = from; q < to; ++q) k.push_back((char)(uint8_t)(v[q] - 1));
+  return k;
+}
+
+const std::vector<double>& env_left(OrcContraction& c, const std::string& k) {
+  auto it = c.left.find(k);
+  if (it != c.left.end()) return it->second;
+  std::vector<double> E;
+  if (k.empty()) {
+    E.assign(1, 1.0);
+  } else {
+    const std::vector<double> P = env_left(c, k.substr(0, k.size() - 1));
+    const int site = (int)k.size() - 1;
+    const Core4 &A = c.a[(size_t)site], &B = c.b[(size_t)site];
+    const i64 ra = A.d[0], s = A.d[1], S = A.d[2], ra2 = A.d[3], rb = B.d[0], s2 = B.d[2], rb2 = B.d[3];
+    const int v = (uint8_t)k.back();
+    const i64 i = v % s, j = v / s;
+    std::vector<double> tmp((size_t)(rb * S * ra2));
+    for (i64 a2 = 0; a2 < ra2; ++a2)
+      for (i64 t = 0; t < S; ++t)
+        for (i64 bb = 0; bb < rb; ++bb) {
+          double acc = 0.0;
+          for (i64 aa = 0; aa < ra; ++aa) acc = acc + P[aa + ra * bb] * A.v[aa + ra * (i + s * (t + S * a2))];
+          tmp[bb + rb * (t + S * a2)] = acc;
+        }
+    E.assign((size_t)(ra2 * rb2), 0.0);
+    for (i64 b2 = 0; b2 < rb2; ++b2)
+      for (i64 a2 = 0; a2 < ra2; ++a2) {
+        double acc = 0.0;
+        for (i64 t = 0; t < S; ++t)
+          for (i64 bb = 0; bb < rb; ++bb)
+            acc = acc + tmp[bb + rb * (t + S * a2)] * B.v[bb + rb * (t + S * (j + s2 * b2))];
+        E[a2 + ra2 * b2] = acc;
+      }
+  }
+  return c.left.emplace(k, std::move(E)).first->second;
+}
+
+const std::vector<double>& env_right(OrcContraction& c, const std::string& k) {
+  auto it = c.right.find(k);
+  if (it != c.right.end()) return it->second;
+  std::vector<double> E;
+  if (k.empty()) {
+    E.assign(1, 1.0);
+  } else {
+    const std::vector<double> P = env_right(c, k.substr(1));
+    const int site = c.L - (int)k.size();
+    const Core4 &A = c.a[(size_t)site], &B = c.b[(size_t)site];
+    const i64 ra = A.d[0], s = A.d[1], S = A.d[2], ra2 = A.d[3], rb = B.d[0], s2 = B.d[2], rb2 = B.d[3];
+    const int v = (uint8_t)k[0];
+    const i64 i = v % s, j = v / s;
+    std::vector<double> tmp((size_t)(rb2 * S * ra));
+    for (i64 aa = 0; aa < ra; ++aa)
+      for (i64 t = 0; t < S; ++t)
+        for (i64 b2 = 0; b2 < rb2; ++b2) {
+          double acc = 0.0;
+          for (i64 a2 = 0; a2 < ra2; ++a2) acc = acc + P[a2 + ra2 * b2] * A.v[aa + ra * (i + s * (t + S * a2))];
+          tmp[b2 + rb2 * (t + S * aa)] = acc;
+        }
+    E.assign((size_t)(ra * rb), 0.0);
+    for (i64 bb = 0; bb < rb; ++bb)
+      for (i64 aa = 0; aa < ra; ++aa) {
+        double acc = 0.0;
+        for (i64 t = 0; t < S; ++t)
+          for (i64 b2 = 0; b2 < rb2; ++b2)
+            acc = acc + tmp[b2 + rb2 * (t + S * aa)] * B.v[bb + rb * (t + S * (j + s2 * b2))];
+        E[aa + ra * bb] = acc;
+      }
+  }
+  return c.right.emplace(k, std::move(E)).first->second;
+}
+
+double contraction_value(OrcContraction& c, const std::string& lk, const std::string& rk) {
+  const std::vector<double>& Lv = env_left(c, lk);
+  const std::vector<double>& Rv = env_right(c, rk);
+  double acc = 0.0;
+  for (size_t q = 0; q < Lv.size(); ++q) acc = acc + Lv[q] * Rv[q];
+  if (c.vf) c.vf(c.vuser, 1, &acc);
+  return acc;
+}
+
+double contraction_point(OrcContraction& c, const MultiIndex& v) {
+  const std::string k = key_of(v, 0, v.size());
+  auto it = c.values.find(k);
+  if (it != c.values.end()) return it->second;
+  const double x = contraction_value(c, k, std::string());
+  c.values.emplace(k, x);
+  return x;
+}
+
+void contraction_fill(OrcContraction& c, const std::vector<MultiIndex>& I, const std::vector<MultiIndex>& J,
+                      std::vector<double>& out) {
+  for (size_t j = 0; j < J.size(); ++j)
+    for (size_t i = 0; i < I.size(); ++i) {
+      const std::string lk = key_of(I[i], 0, I[i].size()), rk = key_of(J[j], 0, J[j].size());
+      const std::string k = lk + rk;
+      auto it = c.values.find(k);
+      if (it != c.values.end()) {
+        out[i + j * I.size()] = it->second;
+        continue;
+      }
+      const double x = contraction_value(c, lk, rk);
+      c.values.emplace(k, x);
+      out[i + j * I.size()] = x;
+    }
+}
+
+// _findinitialpivots + optfirstpivot (contraction.jl:385-397, util.jl:78-108);
+// random starts from tci_rng seeded with `seed`.
+std::vector<MultiIndex> findinitialpivots(const Func& f, const std::vector<int>& d, int nmax, uint64_t seed) {
+  const int L = (int)d.size();
+  tci_rng rng;
+  tci_rng_seed(&rng, seed);
+  std::vector<MultiIndex> starts((size_t)nmax, MultiIndex((size_t)L));
+  for (auto& p : starts)
+    for (int q = 0; q < L; ++q) p[(size_t)q] = (int)tci_rng_uniform1(&rng, (uint64_t)d[(size_t)q]);
+  std::vector<MultiIndex> out;
+  for (auto& pivot : starts) {
+    double valf = std::fabs(f(pivot));
+    for (int sweep = 0; sweep < 1000; ++sweep) {
+      const double prev = valf;
+      for (int q = 0; q < L; ++q)
+        for (int x = 1; x <= d[(size_t)q]; ++x) {
+          const int bak = pivot[(size_t)q];
+          pivot[(size_t)q] = x;
+          const double nv = std::fabs(f(pivot));
+          if (nv > valf)
+            valf = nv;
+          else
+            pivot[(size_t)q] = bak;
+        }
+      if (prev == valf) break;
+    }
+    if (std::fabs(f(pivot)) == 0.0) continue;
+    out.push_back(pivot);
+  }
+  return out;
+}
+
 }  // namespace
 
 // ======================================================================== C ABI
@@ -1422,6 +1599,53 @@ void* orc_tt4_compress(int L, const int64_t* dims, const double* values, int met
                        int64_t maxbonddim, int normalizeerror, int* rc) {
   auto* out = new TT4(read_tt4(L, dims, values));
   *rc = compress_lu(*out, tolerance, maxbonddim > 0 ? maxbonddim : TYPEMAX, normalizeerror != 0, method == 1);
+  return out;
+}
+
+// contract(A, B; algorithm = :TCI, f, initialpivots, kwargs...) (contraction.jl:399-434):
+// pivots np x L fused and 1-based, or np = 0 for ninit random starts.  Returns a
+// TT4 handle with the legs split.
+void* orc_tt4_contract_tci(int L, const int64_t* a_dims, const double* a_values, const int64_t* b_dims,
+                           const double* b_values, const int64_t* pivots, int64_t np, int ninit, orc_value_fn vf,
+                           void* vuser, const orc_opts* o, int* rc) {
+  auto c = std::make_shared<OrcContraction>();
+  c->a = read_tt4(L, a_dims, a_values);
+  c->b = read_tt4(L, b_dims, b_values);
+  c->L = L;
+  c->vf = vf;
+  c->vuser = vuser;
+  auto* out = new TT4();
+  *rc = ORC_OK;
+  std::vector<int> d((size_t)L);
+  for (int n = 0; n < L; ++n) {
+    if (c->a[(size_t)n].d[2] != c->b[(size_t)n].d[1]) {
+      *rc = fail(ORC_ARG, "Cannot contract tensor trains with non-matching site dimensions.");
+      return out;
+    }
+    d[(size_t)n] = (int)(c->a[(size_t)n].d[1] * c->b[(size_t)n].d[2]);
+  }
+  Func f;
+  f.fid = -1;
+  f.ctr = c;
+  std::vector<MultiIndex> piv = np > 0 ? read_pivots(pivots, np, L) : findinitialpivots(f, d, ninit, o->seed);
+  if (piv.empty()) {
+    *rc = fail(ORC_ERR, "No initial pivots found.");
+    return out;
+  }
+  TCI2 t;
+  *rc = tci_new(t, d, f, piv);
+  if (!*rc) *rc = optimize(t, *o);
+  if (*rc) return out;
+  for (int n = 0; n < L; ++n) {
+    const Tensor3& T = t.sitetensors[(size_t)n];
+    Core4 k;
+    k.d[0] = T.d0;
+    k.d[1] = c->a[(size_t)n].d[1];
+    k.d[2] = c->b[(size_t)n].d[2];
+    k.d[3] = T.d2;
+    k.v = T.v;
+    out->push_back(k);
+  }
   return out;
 }
 

@@ -30,8 +30,8 @@ CU_SOURCES = {
     "gather.cu": [],
     "fcache.cu": [],
 }
-CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp"]
-HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "fcache.h", "fc_slot.h"]
+CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp", "contract_tci.cpp"]
+HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h"]
 
 
 def _newer(target, deps):

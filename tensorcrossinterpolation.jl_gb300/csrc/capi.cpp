@@ -16,6 +16,7 @@
 #include <numeric>
 
 #include "contract.h"
+#include "contract_tci.h"
 #include "engine.h"
 
 using namespace tci;
@@ -1213,6 +1214,58 @@ int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double*
   int rc = upload_tt4(e, L, dims, cores, res->tt);
   if (!rc) rc = tt4_check(res->tt);
   if (!rc) rc = tt4_compress(e, res->tt, tolerance, maxbonddim, normalizeerror != 0, method == TCI_FACTORIZE_CI);
+  if (rc) {
+    res->tt.release(e);
+    return rc;
+  }
+  *out = res.release();
+  return 0;
+}
+
+int tci_tt4_contract_tci(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
+                         const int64_t* b_dims, const double* const* b_cores, const int64_t* initialpivots,
+                         int64_t np, int32_t ninitialpivots, tci_value_fn f, void* user, const tci_opts* opts,
+                         tci_tt4** out) {
+  *out = nullptr;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  TT4 a, b;
+  int rc = upload_tt4(e, L, a_dims, a_cores, a);
+  if (!rc) rc = upload_tt4(e, L, b_dims, b_cores, b);
+  if (rc) {
+    a.release(e);
+    b.release(e);
+    return rc;
+  }
+  std::vector<std::vector<uint8_t>> piv;
+  for (int64_t p = 0; p < np; ++p) {
+    std::vector<uint8_t> v((size_t)L);
+    for (int q = 0; q < L; ++q) {
+      const int64_t x = initialpivots[p * L + q];
+      const int64_t dq = a.cores[(size_t)q].d[1] * b.cores[(size_t)q].d[2];
+      if (x < 1 || x > dq || dq > 256) {
+        a.release(e);
+        b.release(e);
+        return fail(TCI_ERR_ARG, "pivot index out of range");
+      }
+      v[(size_t)q] = (uint8_t)(x - 1);
+    }
+    piv.push_back(v);
+  }
+  tci_opts o;
+  if (opts)
+    o = *opts;
+  else
+    tci_opts_default(&o);
+  if (ctx->rq) {  // plain launches: the evaluator's kernels run between steps
+    rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  std::unique_ptr<tci_tt4> res(new tci_tt4());
+  res->ctx = ctx;
+  rc = tt4_contract_tci(e, std::move(a), std::move(b), piv, ninitialpivots > 0 ? ninitialpivots : 10, f, user, o,
+                        res->tt);
   if (rc) {
     res->tt.release(e);
     return rc;

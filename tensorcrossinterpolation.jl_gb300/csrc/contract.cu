@@ -184,6 +184,90 @@ __global__ void gemm_kernel(const double* __restrict__ A, int64_t lda, const dou
   }
 }
 
+// ---- environments of the Contraction evaluator (contraction.jl:103-176) ----
+// One level of new environments: entry e extends parent[e] (ra x rb) by site
+// value (ii[e], jj[e]) of A (ra x s x S x ra2) and B (rb x S x s2 x rb2).
+//   left:  tmp[b, t, a'] = sum_a P[a, b] A[a, i, t, a']
+//          E[a', b']     = sum_(b, t), b fastest, tmp[b, t, a'] B[b, t, j, b']
+//   right: tmp[b2, t, a] = sum_a2 P[a2, b2] A[a, i, t, a2]     (P is ra2 x rb2)
+//          E[a, b]       = sum_(b2, t), b2 fastest, tmp[b2, t, a] B[b, t, j, b2]
+// (_extend_cache, contraction.jl:103-109, with the permuted cores of :165-169).
+struct EnvLevel {
+  const double* A;
+  const double* B;
+  int ra, s, S, ra2, rb, s2, rb2;
+  int right;
+  int n;  // entries
+  const double* const* parent;
+  double* const* out;
+  double* const* tmp;
+  const int32_t* ii;
+  const int32_t* jj;
+};
+
+__global__ void env_tmp_kernel(EnvLevel v) {
+  // left: per entry rb * S * ra2 values; right: rb2 * S * ra values
+  const int64_t per = v.right ? (int64_t)v.rb2 * v.S * v.ra : (int64_t)v.rb * v.S * v.ra2;
+  for (int64_t g = gtid(); g < per * v.n; g += gstride()) {
+    const int e = (int)(g / per);
+    const int64_t x = g % per;
+    const double* P = v.parent[e];
+    const int i = v.ii[e];
+    double acc = 0.0;
+    if (!v.right) {
+      const int b = (int)(x % v.rb), t = (int)((x / v.rb) % v.S), a2 = (int)(x / ((int64_t)v.rb * v.S));
+      const double* Ac = v.A + (int64_t)v.ra * (i + (int64_t)v.s * (t + (int64_t)v.S * a2));
+      for (int a = 0; a < v.ra; ++a) acc = __dadd_rn(acc, __dmul_rn(P[a + (int64_t)v.ra * b], Ac[a]));
+    } else {
+      const int b2 = (int)(x % v.rb2), t = (int)((x / v.rb2) % v.S), a = (int)(x / ((int64_t)v.rb2 * v.S));
+      for (int a2 = 0; a2 < v.ra2; ++a2)
+        acc = __dadd_rn(acc, __dmul_rn(P[a2 + (int64_t)v.ra2 * b2],
+                                       v.A[a + (int64_t)v.ra * (i + (int64_t)v.s * (t + (int64_t)v.S * a2))]));
+    }
+    v.tmp[e][x] = acc;
+  }
+}
+
+__global__ void env_out_kernel(EnvLevel v) {
+  const int64_t per = v.right ? (int64_t)v.ra * v.rb : (int64_t)v.ra2 * v.rb2;
+  for (int64_t g = gtid(); g < per * v.n; g += gstride()) {
+    const int e = (int)(g / per);
+    const int64_t x = g % per;
+    const double* T = v.tmp[e];
+    const int j = v.jj[e];
+    double acc = 0.0;
+    if (!v.right) {
+      const int a2 = (int)(x % v.ra2), b2 = (int)(x / v.ra2);
+      for (int t = 0; t < v.S; ++t) {
+        const double* Tc = T + (int64_t)v.rb * (t + (int64_t)v.S * a2);
+        const double* Bc = v.B + (int64_t)v.rb * (t + (int64_t)v.S * (j + (int64_t)v.s2 * b2));
+        for (int b = 0; b < v.rb; ++b) acc = __dadd_rn(acc, __dmul_rn(Tc[b], Bc[b]));
+      }
+    } else {
+      const int a = (int)(x % v.ra), b = (int)(x / v.ra);
+      for (int t = 0; t < v.S; ++t) {
+        const double* Tc = T + (int64_t)v.rb2 * (t + (int64_t)v.S * a);
+        for (int b2 = 0; b2 < v.rb2; ++b2)
+          acc = __dadd_rn(acc, __dmul_rn(Tc[b2], v.B[b + (int64_t)v.rb * (t + (int64_t)v.S * (j + (int64_t)v.s2 * b2))]));
+      }
+    }
+    v.out[e][x] = acc;
+  }
+}
+
+// out[k] = sum_t L[k][t] R[k][t], t = 0 .. len[k]-1 in order (the (link_a,
+// link_b) contraction of batchevaluate, contraction.jl:325-329, a fastest).
+__global__ void env_dot_kernel(const double* const* L, const double* const* R, const int32_t* len, int n,
+                               double* out) {
+  for (int64_t k = gtid(); k < n; k += gstride()) {
+    const double* l = L[k];
+    const double* r = R[k];
+    double acc = 0.0;
+    for (int t = 0; t < len[k]; ++t) acc = __dadd_rn(acc, __dmul_rn(l[t], r[t]));
+    out[k] = acc;
+  }
+}
+
 int grid_for(int64_t total) {
   int64_t g = (total + CT - 1) / CT;
   if (g < 1) g = 1;
@@ -235,5 +319,24 @@ cudaError_t tci_gemm_launch(const double* A, int64_t lda, const double* B, int64
   const int64_t total = (int64_t)M * N;
   if (total == 0) return cudaSuccess;
   gemm_kernel<<<grid_for(total), CT, 0, st>>>(A, lda, B, ldb, C, ldc, M, N, K);
+  return cudaGetLastError();
+}
+
+cudaError_t tci_env_level_launch(const double* A, const double* B, int ra, int s, int S, int ra2, int rb, int s2,
+                                 int rb2, int right, int n, const double* const* parent, double* const* out,
+                                 double* const* tmp, const int32_t* ii, const int32_t* jj, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  EnvLevel v{A, B, ra, s, S, ra2, rb, s2, rb2, right, n, parent, out, tmp, ii, jj};
+  const int64_t t1 = (right ? (int64_t)rb2 * S * ra : (int64_t)rb * S * ra2) * n;
+  const int64_t t2 = (right ? (int64_t)ra * rb : (int64_t)ra2 * rb2) * n;
+  env_tmp_kernel<<<grid_for(t1), CT, 0, st>>>(v);
+  env_out_kernel<<<grid_for(t2), CT, 0, st>>>(v);
+  return cudaGetLastError();
+}
+
+cudaError_t tci_env_dot_launch(const double* const* L, const double* const* R, const int32_t* len, int n, double* out,
+                               cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  env_dot_kernel<<<grid_for(n), CT, 0, st>>>(L, R, len, n, out);
   return cudaGetLastError();
 }

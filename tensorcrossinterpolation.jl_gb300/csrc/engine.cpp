@@ -1191,6 +1191,37 @@ i64 solve_rank(const Solve& s) {
   return r;
 }
 
+// A solve whose f values come from the device value cache, filled by a
+// caller-supplied fn or by the library's own evaluator.
+static int init_cached(Solve& s, int L, const int64_t* localdims, tci_batch_fn fn, void* user,
+                       std::shared_ptr<FEvaluator> ev) {
+  if (L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
+  s.L = L;
+  s.d.assign(localdims, localdims + L);
+  for (int x : s.d)
+    if (x < 1 || x > 256) return fail(TCI_ERR_ARG, "local dimensions must be in 1..256");
+  s.fid = TCI_FID_CACHE;
+  s.params.assign(4 + (size_t)L, 0.0);
+  s.fcache = std::make_shared<FCache>();
+  int rc = s.fcache->init(L, s.d.data(), fn, user, s.params.data(), std::move(ev));
+  if (rc) return rc;
+  s.Iset.assign(L, IndexSet());
+  s.Jset.assign(L, IndexSet());
+  for (int b = 0; b < L; ++b) {
+    s.Iset[b].len = b;
+    s.Jset[b].len = L - 1 - b;
+  }
+  s.cores.assign(L, Core());
+  s.bonderrors.assign(L - 1, 0.0);
+  s.lutcap0 = s.lutcap1 = 0;
+  s.pivoterrors.clear();
+  return 0;
+}
+
+int solve_init_evaluator(Solve& s, int L, const int64_t* localdims, std::shared_ptr<FEvaluator> ev) {
+  return init_cached(s, L, localdims, nullptr, nullptr, std::move(ev));
+}
+
 int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
                int64_t nparams, const int64_t*, int64_t) {
   if (L < 2) return fail(TCI_ERR_GENERIC, "localdims should have at least 2 elements!");
@@ -1198,26 +1229,7 @@ int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double*
     tci_batch_fn fn = nullptr;
     void* user = nullptr;
     if (!user_fn(fid, &fn, &user)) return fail(TCI_ERR_ARG, "unknown function id");
-    s.L = L;
-    s.d.assign(localdims, localdims + L);
-    for (int x : s.d)
-      if (x < 1 || x > 256) return fail(TCI_ERR_ARG, "local dimensions must be in 1..256");
-    s.fid = TCI_FID_CACHE;
-    s.params.assign(4 + (size_t)L, 0.0);
-    s.fcache = std::make_shared<FCache>();
-    int rc = s.fcache->init(L, s.d.data(), fn, user, s.params.data());
-    if (rc) return rc;
-    s.Iset.assign(L, IndexSet());
-    s.Jset.assign(L, IndexSet());
-    for (int b = 0; b < L; ++b) {
-      s.Iset[b].len = b;
-      s.Jset[b].len = L - 1 - b;
-    }
-    s.cores.assign(L, Core());
-    s.bonderrors.assign(L - 1, 0.0);
-    s.lutcap0 = s.lutcap1 = 0;
-    s.pivoterrors.clear();
-    return 0;
+    return init_cached(s, L, localdims, fn, user, nullptr);
   }
   if (fid < TCI_F_LORENTZ || fid > TCI_F_PRODUCT) return fail(TCI_ERR_ARG, "unknown function id");
   s.L = L;

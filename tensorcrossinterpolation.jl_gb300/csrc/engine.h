@@ -353,6 +353,8 @@ class Engine {
 };
 
 // ------------------------------------------------------------ TCI2 algorithm
+// A solve whose f is the library's own evaluator (values through the device cache).
+int solve_init_evaluator(Solve& s, int L, const int64_t* localdims, std::shared_ptr<FEvaluator> ev);
 int solve_init(Solve& s, int L, const int64_t* localdims, int fid, const double* params,
                int64_t nparams, const int64_t* pivots, int64_t np);
 CoTask co_construct(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> pivots);

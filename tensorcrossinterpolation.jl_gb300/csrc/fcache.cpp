@@ -30,16 +30,10 @@ struct KeyHash {
   size_t operator()(const Key& k) const { return (size_t)tci_fc_hash(k.k0, k.k1); }
 };
 
-// One Pi product of a task: every row multi-index (sites [0, rl)) joined with
-// every column multi-index (sites [rl, rl + cl)); a point list has one empty column.
-struct Prod {
-  const uint8_t* rows;
-  int64_t nr;
-  int rl;
-  const uint8_t* cols;
-  int64_t nc;
-  int cl;
+struct Prod : FcProduct {
   size_t koff = 0, moff = 0;
+  Prod(const uint8_t* r, int64_t nr_, int rl_, const uint8_t* c, int64_t nc_, int cl_)
+      : FcProduct{r, nr_, rl_, c, nc_, cl_} {}
 };
 
 constexpr uint64_t FC_MIN_CAP = 1ull << 16;
@@ -72,10 +66,12 @@ void FCache::release() {
 
 // Mixed-radix weights, v_1 fastest as CachedFunction's coeffs
 // (cachedfunction.jl:16-19), split where a half would reach 2^52.
-int FCache::init(int L_, const int* d_, tci_batch_fn fn_, void* user_, double* params_) {
+int FCache::init(int L_, const int* d_, tci_batch_fn fn_, void* user_, double* params_,
+                 std::shared_ptr<FEvaluator> eval_) {
   L = L_;
   fn = fn_;
   user = user_;
+  eval = std::move(eval_);
   params = params_;
   d.assign(d_, d_ + L);
   w.assign(L, 0);
@@ -246,7 +242,7 @@ int FCache::prefill(Engine& e, const std::vector<Req*>& reqs) {
   std::unordered_set<Key, KeyHash> seen;
   seen.reserve(total * 2);
   std::vector<tci_fc_entry> ent;
-  std::vector<int64_t> pts;
+  std::vector<FcMiss> um;
   size_t at = 0;
   for (size_t q = 0; q < prods.size(); ++q) {
     const Prod& p = prods[q];
@@ -259,21 +255,35 @@ int FCache::prefill(Engine& e, const std::vector<Req*>& reqs) {
       const Key k{(uint64_t)(rk[2 * i] + ck[2 * j]), (uint64_t)(rk[2 * i + 1] + ck[2 * j + 1])};
       if (!seen.insert(k).second) continue;
       ent.push_back(tci_fc_entry{k.k0, k.k1, 0.0, 0});
-      const uint8_t* a = p.rows + (size_t)i * p.rl;
-      for (int c = 0; c < p.rl; ++c) pts.push_back((int64_t)a[c] + 1);
-      const uint8_t* b = p.cols ? p.cols + (size_t)j * p.cl : nullptr;
-      for (int c = 0; c < p.cl; ++c) pts.push_back((int64_t)b[c] + 1);
+      um.push_back(FcMiss{(int32_t)q, i, j});
     }
     at += cnt[q];
   }
   const int64_t u = (int64_t)ent.size();
   std::vector<double> vals((size_t)u);
-  ++cb_depth;
-  const int frc = fn(user, L, u, pts.data(), vals.data());
-  --cb_depth;
+  if (fn) {
+    std::vector<int64_t> pts;
+    pts.reserve((size_t)u * L);
+    for (const FcMiss& x : um) {
+      const Prod& p = prods[(size_t)x.q];
+      const uint8_t* a = p.rows + (size_t)x.i * p.rl;
+      for (int c = 0; c < p.rl; ++c) pts.push_back((int64_t)a[c] + 1);
+      const uint8_t* b = p.cols ? p.cols + (size_t)x.j * p.cl : nullptr;
+      for (int c = 0; c < p.cl; ++c) pts.push_back((int64_t)b[c] + 1);
+    }
+    ++cb_depth;
+    const int frc = fn(user, L, u, pts.data(), vals.data());
+    --cb_depth;
+    if (frc) return fc_fail(TCI_ERR_GENERIC, "caller-supplied f failed (code " + std::to_string(frc) + ")");
+  } else {
+    std::vector<FcProduct> views(prods.begin(), prods.end());
+    ++cb_depth;  // the evaluator may call back into a caller-supplied value map
+    const int erc = eval->values(e, views, um, vals.data());
+    --cb_depth;
+    if (erc) return erc;
+  }
   ++calls;
   evaluated += u;
-  if (frc) return fc_fail(TCI_ERR_GENERIC, "caller-supplied f failed (code " + std::to_string(frc) + ")");
   for (int64_t k = 0; k < u; ++k) ent[(size_t)k].v = vals[(size_t)k];
   rc = grow(count + (uint64_t)u, s);
   if (rc) return rc;

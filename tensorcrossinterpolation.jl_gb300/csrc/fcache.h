@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "../../include/tci_gb300.h"
@@ -24,8 +25,36 @@ namespace tci {
 struct Req;
 class Engine;
 
+// One Pi product of a task: every row multi-index (sites [0, rl)) joined with
+// every column multi-index (sites [rl, rl + cl)); a point list has one empty
+// column.  Multi-indices are 0-based bytes.
+struct FcProduct {
+  const uint8_t* rows;
+  int64_t nr;
+  int rl;
+  const uint8_t* cols;
+  int64_t nc;
+  int cl;
+};
+// A distinct missing point: row i joined with column j of product q.
+struct FcMiss {
+  int32_t q;
+  int64_t i, j;
+};
+
+// An f computed by the library itself for the points the cache misses (the
+// Contraction evaluator of contract(algorithm = :TCI)); it sees the products,
+// so it can exploit their row x column structure.
+class FEvaluator {
+ public:
+  virtual ~FEvaluator() = default;
+  virtual int values(Engine& e, const std::vector<FcProduct>& prods, const std::vector<FcMiss>& miss,
+                     double* out) = 0;
+};
+
 struct FCache {
-  tci_batch_fn fn = nullptr;
+  tci_batch_fn fn = nullptr;   // caller-supplied f, or
+  std::shared_ptr<FEvaluator> eval;  // the library's own evaluator
   void* user = nullptr;
   int L = 0;
   int split = 0;               // sites [0, split) form key word 0, [split, L) word 1
@@ -40,8 +69,10 @@ struct FCache {
   size_t dscr_cap = 0;
 
   ~FCache();
-  // Set up keys for localdims d; params must hold 4 + L doubles.
-  int init(int L, const int* d, tci_batch_fn fn, void* user, double* params);
+  // Set up keys for localdims d; params must hold 4 + L doubles.  Values come
+  // from fn (with user) or, when fn is null, from eval.
+  int init(int L, const int* d, tci_batch_fn fn, void* user, double* params,
+           std::shared_ptr<FEvaluator> eval = nullptr);
   // Values of f at every element the tasks in reqs (those with fcache == this)
   // read, stored in the table; writes the table address into params.
   int prefill(Engine& e, const std::vector<Req*>& reqs);

@@ -24,6 +24,8 @@ I64P = ctypes.POINTER(ctypes.c_int64)
 F64P = ctypes.POINTER(ctypes.c_double)
 # tci_batch_fn: (user, L, npoints, points[npoints x L], values[npoints]) -> status
 BATCH_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, I64P, F64P)
+# tci_value_fn: (user, n, values[n]) -> status, values mapped in place
+VALUE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, F64P)
 
 TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
@@ -161,6 +163,9 @@ _SIGNATURES = {
     "tci_tt4_compress": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, ctypes.c_int32,
                                         ctypes.c_double, ctypes.c_int64, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_tt4_contract_tci": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
+                                            ctypes.c_void_p, I64P, ctypes.c_int64, ctypes.c_int32, VALUE_FN,
+                                            ctypes.c_void_p, ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_void_p)]),
     "tci_tt4_length": (ctypes.c_int32, [ctypes.c_void_p]),
     "tci_tt4_dims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
     "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
@@ -675,17 +680,35 @@ def _as_tt4(t, left_operand):
     return cores, three
 
 
-def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU", ctx=None, f=None):
+def _value_callback(f):
+    """tci_value_fn from an elementwise Python function (values mapped in place)."""
+    def _call(user, n, vals):
+        try:
+            v = np.ctypeslib.as_array(vals, shape=(n,))
+            v[:] = np.asarray(f(v.copy()), dtype=np.float64).reshape(-1)
+            return 0
+        except BaseException as e:  # reported through the library's error code
+            _cb_state.error = e
+            return 1
+    return VALUE_FN(_call)
+
+
+def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU", ctx=None, f=None,
+             initialpivots=10, **kwargs):
     """contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) of
     tensor trains with 4-leg cores (A's third leg against B's second), or of a
-    3-leg train with a 4-leg one.  algorithm "naive" or "zipup"; factorizations
-    use the rank-revealing LU (method "LU") or MatrixLUCI over it (method "CI")
-    -- the reference's SVD is not on the device.  Returns a TensorTrain."""
+    3-leg train with a 4-leg one.  algorithm "TCI" (the default: crossinterpolate2
+    of the Contraction evaluator on the device, with f applied elementwise,
+    `initialpivots` a count of random starts or a list of fused 1-based
+    pivots, and crossinterpolate2 keywords in kwargs), "naive" or "zipup";
+    factorizations use the rank-revealing LU (method "LU") or MatrixLUCI over it
+    (method "CI") -- the reference's SVD is not on the device.  Returns a
+    TensorTrain."""
     if f is not None and algorithm != "TCI":
         raise TCIError(TCI_ERR_GENERIC, f"{algorithm.capitalize()} contraction implementation cannot contract "
                        "matrix product with a function. Use algorithm=:TCI instead.")
     if algorithm == "TCI":
-        raise TCIError(TCI_ERR_GENERIC, "algorithm=:TCI is not available on the device; use 'naive' or 'zipup'")
+        return _contract_tci(A, B, tolerance, maxbonddim, f, initialpivots, ctx, kwargs)
     alg = {"naive": TCI_CONTRACT_NAIVE, "zipup": TCI_CONTRACT_ZIPUP}.get(algorithm)
     if alg is None:
         raise ArgumentError(TCI_ERR_ARG, f"Unknown algorithm {algorithm}.")
@@ -702,6 +725,32 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     _check(load_library().tci_tt4_contract(ctx.h, len(a), _p(ad, I64P), ap, _p(bd, I64P), bp, alg,
                                            FACTORIZE[method], float(tolerance), int(maxbonddim or 0),
                                            ctypes.byref(h)))
+    cores = _tt4_fetch(h)
+    if a3 or b3:  # TensorTrain{3}(tt, prod.(sitedims(tt)))
+        cores = [c.reshape((c.shape[0], c.shape[1] * c.shape[2], c.shape[3]), order="F") for c in cores]
+    return TensorTrain(cores)
+
+
+def _contract_tci(A, B, tolerance, maxbonddim, f, initialpivots, ctx, kwargs):
+    """contract_TCI (contraction.jl:399-434) through tci_tt4_contract_tci."""
+    ctx = ctx or default_context()
+    a, a3 = _as_tt4(A, True)
+    b, b3 = _as_tt4(B, False)
+    if len(a) != len(b):
+        raise ArgumentError(TCI_ERR_ARG, "Cannot contract tensor trains with different length.")
+    a, ad, ap = _tt4_args(a)
+    b, bd, bp = _tt4_args(b)
+    L = len(a)
+    if isinstance(initialpivots, (int, np.integer)):
+        piv, ninit = np.zeros((0, L), np.int64), int(initialpivots)
+    else:
+        piv, ninit = _pivots_array(initialpivots, L), 0
+    o = make_opts(tolerance=tolerance, maxbonddim=maxbonddim, **kwargs)
+    cb = _value_callback(f) if f is not None else VALUE_FN()  # a null pointer without f
+    h = ctypes.c_void_p()
+    _check(load_library().tci_tt4_contract_tci(ctx.h, L, _p(ad, I64P), ap, _p(bd, I64P), bp,
+                                               _p(piv, I64P) if piv.size else None, piv.shape[0], ninit,
+                                               cb, None, ctypes.byref(o), ctypes.byref(h)))
     cores = _tt4_fetch(h)
     if a3 or b3:  # TensorTrain{3}(tt, prod.(sitedims(tt)))
         cores = [c.reshape((c.shape[0], c.shape[1] * c.shape[2], c.shape[3]), order="F") for c in cores]

@@ -68,3 +68,24 @@ def test_factorization_methods(oracle, method):
     zu = oracle.tt4_contract(a, b, "zipup", tolerance=1e-12, method=method)
     assert np.allclose(oracle.tt4_full(zu), ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max())
 
+
+
+@pytest.mark.parametrize("f", [None, lambda x: 2 * x])
+def test_contract_tci(oracle, f):
+    """contract(a, b; algorithm=:TCI, f) (contraction.jl:399-434) reproduces the
+    dense product, as test/test_contraction.jl:68-99, 148-183 check it."""
+    a, b = _testdata(np.random.default_rng(6))
+    ab = oracle.tt4_contract_tci(a, b, tolerance=1e-12, f=f)
+    assert [c.shape[1:3] for c in ab] == [(2, 2)] * 4
+    ref = oracle.tt4_full(a) @ oracle.tt4_full(b)
+    if f is not None:
+        ref = f(ref)
+    assert np.allclose(oracle.tt4_full(ab), ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
+    rng = np.random.default_rng(7)
+    a = _rand_tt(rng, [1, 2, 3, 2, 1], [3] * 4, [3] * 4)
+    v4 = [rng.standard_normal((r0, 3, 1, r1)) for r0, r1 in zip([1, 2, 3, 2], [2, 3, 2, 1])]
+    av = oracle.tt4_contract_tci(a, v4, tolerance=1e-12, f=f)
+    ref = oracle.tt4_full(a) @ oracle.tt4_full(v4)
+    if f is not None:
+        ref = f(ref)
+    assert np.allclose(oracle.tt4_full(av), ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
