@@ -295,6 +295,41 @@ def single_solve_configs(T, ctx, with_cpu=True):
     return out
 
 
+def contract_tci_bench(T, ctx, maxbonddim=128):
+    """contract(operator, mps; algorithm=:TCI) for the 2-D quantics configuration:
+    the 30-site TCI result (tol 1e-9) under the seeded random operator (bond 64,
+    4 x 4 sites, N(0, 1/64) entries), maxbonddim capped; the result checked
+    against the zipup contraction at random points."""
+    import numpy as np
+
+    f = T.DeviceFunction("qtt2d")
+    tci, _, _ = T.crossinterpolate2(float, f, [4] * 30, ctx=ctx, tolerance=1e-9, maxbonddim=512, maxiter=20)
+    mps = T.tensortrains([tci], ctx=ctx)[0]
+    rng = np.random.default_rng(55)
+    bonds = [1] + [64] * 29 + [1]
+    op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 8.0 for i in range(30)]
+    t0 = time.perf_counter()
+    res = T.contract(op, mps, algorithm="TCI", tolerance=1e-9, maxbonddim=maxbonddim, ctx=ctx)
+    t = time.perf_counter() - t0
+    pts = rng.integers(1, 5, size=(20, 30))
+    exact = np.array([_exact_mpo_mps(op, mps.sitetensors, p) for p in pts])
+    got = res.evaluate(pts, ctx=ctx)
+    return {"workload": f"contract(algorithm=:TCI) of the bond-64 operator with the 30-site 2-D quantics train "
+                        f"(rank {int(tci.rank())}), tolerance 1e-9, maxbonddim {maxbonddim}",
+            "gpu_s": t, "rank": int(res.rank()),
+            "max_rel_err_20_points": float(np.abs(got - exact).max() / np.abs(exact).max())}
+
+
+def _exact_mpo_mps(op, mps, p):
+    """(op * mps)[p] by a left-to-right environment sweep on the host (1-based p)."""
+    import numpy as np
+
+    env = np.ones((1, 1))
+    for n, (a, b) in enumerate(zip(op, mps)):
+        env = np.einsum("ab,asc,bsd->cd", env, a[:, p[n] - 1, :, :], b, optimize=True)
+    return float(env[0, 0])
+
+
 def rrlu_batch_bench(T, ctx, peak_sep, with_cpu=True, reps=3):
     """The batched-rrLU configuration: 4096 matrices (2r)x(2r), r in [8, 128], seed 0,
     reltol 1e-10, maxrank 256, one launch.  Device time from CUDA events around the
@@ -370,7 +405,8 @@ def main():
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
     ap.add_argument("--no-sweep", action="store_true", help="skip the latency sweep over arrival rates")
-    ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU")
+    ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU; "
+                    "'contract-tci': only contract(algorithm=:TCI) of the 2-D quantics configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -386,6 +422,9 @@ def main():
         return
     if args.only == "big-rrlu":  # the multi-CTA rrLU alone
         print(json.dumps(large_rrlu_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)))
+        return
+    if args.only == "contract-tci":  # contract(algorithm=:TCI) of the 2-D quantics configuration alone
+        print(json.dumps(contract_tci_bench(T, ctx)))
         return
 
     def specs_for(step):
