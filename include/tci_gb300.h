@@ -201,6 +201,23 @@ int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out);
 /* sum(tt) (abstracttensortrain.jl:191-199), FP64. */
 int tci_sum(tci_solve* s, double* out);
 
+/* optfirstpivot(f, localdims, firstpivot; maxsweep) (util.jl:78-108): coordinate
+ * ascent of |f| from `pivot` (1-based, L entries, updated in place); each sweep
+ * moves every site to the first value that raises |f|; stops when a sweep
+ * changes nothing or after maxsweep sweeps (<= 0: 1000).  f is a registered
+ * device function or a caller-supplied one (tci_f_register). */
+int tci_optfirstpivot(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,
+                      const int64_t* localdims, int64_t* pivot, int32_t maxsweep);
+
+/* estimatetrueerror(TensorTrain(tci), f; nsearch, initialpoints) (globalsearch.jl:1-96):
+ * greedy searches for large |f - tt| with the solve's f and site tensors, from the
+ * np initial points (np x L, 1-based) or, when np = 0, from nsearch random points
+ * drawn from `seed`.  Writes up to cap (pivot, error) pairs, sorted by error
+ * descending with repeats removed: pivots cap x L row-major 1-based; *nout is the
+ * number of pairs found (may exceed cap). */
+int tci_estimatetrueerror(tci_solve* s, int32_t nsearch, const int64_t* initialpoints, int64_t np, uint64_t seed,
+                          int64_t cap, int64_t* pivots, double* errors, int64_t* nout);
+
 /* Batch evaluation of a registered f at np points (np x L, 1-based) on the
  * device: the BatchEvaluator call of batcheval.jl:67-83 with M = L. */
 int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,

@@ -139,6 +139,9 @@ def lib():
         L.orc_tt4_contract_tci.argtypes = [ctypes.c_int, I64P, F64P, I64P, F64P, I64P, ctypes.c_int64, ctypes.c_int,
                                            VALUE_FN, ctypes.c_void_p, ctypes.POINTER(Opts),
                                            ctypes.POINTER(ctypes.c_int)]
+        L.orc_optfirstpivot.argtypes = [ctypes.c_int, F64P, ctypes.c_int64, ctypes.c_int, I64P, I64P, ctypes.c_int]
+        L.orc_estimatetrueerror.argtypes = [ctypes.c_int, F64P, ctypes.c_int64, ctypes.c_int, I64P, I64P, F64P, I64P,
+                                            ctypes.c_int64, I64P, F64P, ctypes.POINTER(ctypes.c_int64)]
         L.orc_tt4_length.argtypes = [ctypes.c_void_p]
         L.orc_tt4_dims.argtypes = [ctypes.c_void_p, I64P]
         L.orc_tt4_core.argtypes = [ctypes.c_void_p, ctypes.c_int, F64P]
@@ -532,6 +535,35 @@ def tt4_contract_tci(a, b, initialpivots=10, f=None, **kw):
                                    cb if cb is not None else VALUE_FN(), None,
                                    ctypes.byref(o), ctypes.byref(rc))
     return _tt4_unpack(h, rc)
+
+
+def optfirstpivot(fid, params, localdims, firstpivot=None, maxsweep=1000):
+    """optfirstpivot (util.jl:78-108) -> the improved pivot (1-based)."""
+    L = len(localdims)
+    d = np.ascontiguousarray(localdims, dtype=np.int64)
+    p = np.ascontiguousarray(firstpivot if firstpivot is not None else np.ones(L), dtype=np.int64)
+    prm = np.ascontiguousarray(params if params is not None else [], dtype=np.float64)
+    lib().orc_optfirstpivot(int(fid), _p(prm, F64P) if prm.size else None, prm.size, L, _p(d, I64P), _p(p, I64P),
+                            int(maxsweep))
+    return p
+
+
+def estimatetrueerror(fid, params, cores, starts):
+    """estimatetrueerror(tt, f; initialpoints) (globalsearch.jl:19-96) for a train of
+    3-leg cores -> list of (pivot, error), error descending."""
+    L = len(cores)
+    links = np.ascontiguousarray([c.shape[0] for c in cores] + [1], dtype=np.int64)
+    dims = np.ascontiguousarray([c.shape[1] for c in cores], dtype=np.int64)
+    vals = np.ascontiguousarray(np.concatenate([np.asarray(c, np.float64).reshape(-1, order="F") for c in cores]))
+    st = np.ascontiguousarray(starts, dtype=np.int64).reshape(-1, L)
+    prm = np.ascontiguousarray(params if params is not None else [], dtype=np.float64)
+    piv = np.zeros((st.shape[0], L), np.int64)
+    err = np.zeros(st.shape[0])
+    n = ctypes.c_int64()
+    lib().orc_estimatetrueerror(int(fid), _p(prm, F64P) if prm.size else None, prm.size, L, _p(links, I64P),
+                                _p(dims, I64P), _p(vals, F64P), _p(st, I64P), st.shape[0], _p(piv, I64P),
+                                _p(err, F64P), ctypes.byref(n))
+    return [(piv[k], float(err[k])) for k in range(n.value)]
 
 
 def tt4_full(cores):

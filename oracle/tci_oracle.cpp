@@ -1510,6 +1510,88 @@ int orc_tt_evaluate(int L, const int64_t* linkdims /*L+1*/, const int64_t* local
   return 0;
 }
 
+// optfirstpivot(f, localdims, firstpivot; maxsweep) (util.jl:78-108), pivot 1-based, in place.
+int orc_optfirstpivot(int fid, const double* params, int64_t nparams, int L, const int64_t* localdims,
+                      int64_t* pivot, int maxsweep) {
+  Func f = make_func(fid, params, nparams);
+  MultiIndex p(L);
+  for (int q = 0; q < L; ++q) p[q] = (int)pivot[q];
+  double valf = std::fabs(f(p));
+  for (int sweep = 0; sweep < maxsweep; ++sweep) {
+    const double prev = valf;
+    for (int i = 0; i < L; ++i)
+      for (int d = 1; d <= localdims[i]; ++d) {
+        const int bak = p[i];
+        p[i] = d;
+        const double nv = std::fabs(f(p));
+        if (nv > valf)
+          valf = nv;
+        else
+          p[i] = bak;
+      }
+    if (prev == valf) break;
+  }
+  for (int q = 0; q < L; ++q) pivot[q] = p[q];
+  return 0;
+}
+
+// estimatetrueerror(tt, f; initialpoints) (globalsearch.jl:19-96) for the train
+// given as in orc_tt_evaluate and np start points (1-based); writes the (pivot,
+// error) pairs sorted by error descending (stable), repeats removed.
+int orc_estimatetrueerror(int fid, const double* params, int64_t nparams, int L, const int64_t* linkdims,
+                          const int64_t* localdims, const double* cores, const int64_t* starts, int64_t np,
+                          int64_t* pivots, double* errors, int64_t* nout) {
+  Func f = make_func(fid, params, nparams);
+  std::vector<Tensor3> tt(L);
+  const double* c = cores;
+  for (int b = 0; b < L; ++b) {
+    tt[b].d0 = linkdims[b];
+    tt[b].d1 = localdims[b];
+    tt[b].d2 = linkdims[b + 1];
+    size_t sz = (size_t)(tt[b].d0 * tt[b].d1 * tt[b].d2);
+    tt[b].v.assign(c, c + sz);
+    c += sz;
+  }
+  std::vector<std::pair<MultiIndex, double>> res;
+  for (int64_t k = 0; k < np; ++k) {  // _floatingzone (:48-96)
+    MultiIndex p(L);
+    for (int q = 0; q < L; ++q) p[q] = (int)starts[k * L + q];
+    double maxerror = std::fabs(f(p) - tt_evaluate(tt, p));
+    for (;;) {
+      const double prev = maxerror;
+      for (int ipos = 0; ipos < L; ++ipos) {
+        double best = -1.0;
+        int arg = 1;
+        for (int v = 1; v <= localdims[ipos]; ++v) {
+          MultiIndex x = p;
+          x[ipos] = v;
+          const double err = std::fabs(f(x) - tt_evaluate(tt, x));
+          if (err > best) {
+            best = err;
+            arg = v;
+          }
+        }
+        p[ipos] = arg;
+        maxerror = std::max(best, maxerror);
+      }
+      if (maxerror == prev) break;
+    }
+    res.emplace_back(p, maxerror);
+  }
+  std::vector<size_t> order(res.size());
+  for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return res[a].second > res[b].second; });
+  std::vector<std::pair<MultiIndex, double>> uniq;
+  for (size_t k : order)
+    if (std::find(uniq.begin(), uniq.end(), res[k]) == uniq.end()) uniq.push_back(res[k]);
+  *nout = (int64_t)uniq.size();
+  for (size_t k = 0; k < uniq.size(); ++k) {
+    for (int q = 0; q < L; ++q) pivots[k * L + q] = uniq[k].first[q];
+    errors[k] = uniq[k].second;
+  }
+  return 0;
+}
+
 double orc_tt_sum(int L, const int64_t* linkdims, const int64_t* localdims, const double* cores) {
   std::vector<Tensor3> tt(L);
   const double* c = cores;

@@ -30,7 +30,7 @@ CU_SOURCES = {
     "gather.cu": [],
     "fcache.cu": [],
 }
-CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp", "contract_tci.cpp"]
+CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp", "contract_tci.cpp", "pivotsearch.cpp"]
 HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h"]
 
 

@@ -1010,6 +1010,51 @@ int tci_feval(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams,
   return 0;
 }
 
+int tci_optfirstpivot(tci_ctx* ctx, int32_t fid, const double* fparams, int64_t nparams, int32_t L,
+                      const int64_t* localdims, int64_t* pivot, int32_t maxsweep) {
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  Solve s;
+  int rc = solve_init(s, L, localdims, fid, fparams, nparams, nullptr, 0);
+  if (rc) return rc;
+  std::vector<std::vector<uint8_t>> piv = to_pivots(pivot, 1, L, s.d, &rc);
+  if (rc) return rc;
+  std::vector<double> valf;
+  CoTask t = co_optfirstpivots(ctx->eng_ref(), s, &piv, &valf, maxsweep > 0 ? maxsweep : 1000);
+  rc = run_solve(ctx, s, t);
+  if (rc) return rc;
+  for (int q = 0; q < L; ++q) pivot[q] = (int64_t)piv[0][(size_t)q] + 1;
+  return 0;
+}
+
+int tci_estimatetrueerror(tci_solve* s, int32_t nsearch, const int64_t* initialpoints, int64_t np, uint64_t seed,
+                          int64_t cap, int64_t* pivots, double* errors, int64_t* nout) {
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  const int L = s->s.L;
+  int rc = 0;
+  std::vector<std::vector<uint8_t>> starts;
+  if (np > 0) {
+    starts = to_pivots(initialpoints, np, L, s->s.d, &rc);
+    if (rc) return rc;
+  } else {
+    if (nsearch <= 0) return fail(TCI_ERR_GENERIC, "No search is performed");
+    tci_rng rng;
+    tci_rng_seed(&rng, seed);
+    starts.assign((size_t)nsearch, std::vector<uint8_t>((size_t)L));
+    for (auto& p : starts)
+      for (int q = 0; q < L; ++q) p[(size_t)q] = (uint8_t)(tci_rng_uniform1(&rng, (uint64_t)s->s.d[(size_t)q]) - 1);
+  }
+  std::vector<std::pair<std::vector<uint8_t>, double>> res;
+  CoTask t = co_estimatetrueerror(s->ctx->eng_ref(), s->s, std::move(starts), &res);
+  rc = run_solve(s->ctx, s->s, t);
+  if (rc) return rc;
+  *nout = (int64_t)res.size();
+  for (int64_t k = 0; k < std::min<int64_t>(cap, (int64_t)res.size()); ++k) {
+    for (int q = 0; q < L; ++q) pivots[k * L + q] = (int64_t)res[(size_t)k].first[(size_t)q] + 1;
+    errors[k] = res[(size_t)k].second;
+  }
+  return 0;
+}
+
 int tci_convergencecriterion(const int64_t* ranks, const double* errors, const int64_t* nglobalpivots,
                              int64_t n, double tolerance, int64_t maxbonddim, int64_t ncheckhistory,
                              int32_t checkconvglobalpivot) {

@@ -232,11 +232,8 @@ class ContractionEval : public FEvaluator {
   std::unordered_map<std::string, double*> left_, right_;
 };
 
-// _findinitialpivots (contraction.jl:385-397) with optfirstpivot (util.jl:78-108):
-// random starts from the solve's RNG seed, then coordinate ascent of |f|; all
-// starts advance together, one site at a time, so each step is one device
-// evaluation.  For one site the greedy scan of the reference keeps the first
-// value that beats the running best, i.e. the first maximum above the current one.
+// _findinitialpivots (contraction.jl:385-397): random starts from the solve's
+// RNG seed, each improved by optfirstpivot; starts whose |f| is zero dropped.
 CoTask co_findinitialpivots(Engine& e, Solve& s, int nmax, uint64_t seed, std::vector<std::vector<uint8_t>>* out) {
   out->clear();
   const int L = s.L;
@@ -245,50 +242,8 @@ CoTask co_findinitialpivots(Engine& e, Solve& s, int nmax, uint64_t seed, std::v
   std::vector<std::vector<uint8_t>> piv((size_t)nmax, std::vector<uint8_t>((size_t)L));
   for (auto& p : piv)
     for (int q = 0; q < L; ++q) p[(size_t)q] = (uint8_t)(tci_rng_uniform1(&rng, (uint64_t)s.d[(size_t)q]) - 1);
-  std::vector<double> valf((size_t)nmax);
-  {
-    std::vector<uint8_t> pts;
-    for (auto& p : piv) pts.insert(pts.end(), p.begin(), p.end());
-    std::vector<double> v((size_t)nmax);
-    CO_TRY(co_evaluate(e, s, pts.data(), nmax, v.data(), nullptr));
-    for (int q = 0; q < nmax; ++q) valf[(size_t)q] = std::fabs(v[(size_t)q]);
-  }
-  std::vector<char> active((size_t)nmax, 1);
-  for (int sweep = 0; sweep < 1000; ++sweep) {
-    std::vector<double> prev = valf;
-    for (int site = 0; site < L; ++site) {
-      const int D = s.d[(size_t)site];
-      std::vector<int> who;
-      std::vector<uint8_t> pts;
-      for (int q = 0; q < nmax; ++q) {
-        if (!active[(size_t)q]) continue;
-        who.push_back(q);
-        for (int v = 0; v < D; ++v) {
-          pts.insert(pts.end(), piv[(size_t)q].begin(), piv[(size_t)q].end());
-          pts[pts.size() - (size_t)L + (size_t)site] = (uint8_t)v;
-        }
-      }
-      if (who.empty()) break;
-      std::vector<double> vals(who.size() * (size_t)D);
-      CO_TRY(co_evaluate(e, s, pts.data(), (i64)vals.size(), vals.data(), nullptr));
-      for (size_t w = 0; w < who.size(); ++w) {
-        const size_t q = (size_t)who[w];
-        for (int v = 0; v < D; ++v) {
-          const double nv = std::fabs(vals[w * (size_t)D + (size_t)v]);
-          if (nv > valf[q]) {
-            valf[q] = nv;
-            piv[q][(size_t)site] = (uint8_t)v;
-          }
-        }
-      }
-    }
-    bool any = false;
-    for (int q = 0; q < nmax; ++q) {
-      if (active[(size_t)q] && prev[(size_t)q] == valf[(size_t)q]) active[(size_t)q] = 0;
-      any |= active[(size_t)q] != 0;
-    }
-    if (!any) break;
-  }
+  std::vector<double> valf;
+  CO_TRY(co_optfirstpivots(e, s, &piv, &valf, 1000));
   for (int q = 0; q < nmax; ++q)
     if (valf[(size_t)q] != 0.0) out->push_back(piv[(size_t)q]);
   co_return 0;

@@ -369,6 +369,13 @@ CoTask co_sweep1site(Engine& e, Solve& s, bool forward, double reltol, double ab
 CoTask co_fillsitetensors(Engine& e, Solve& s);
 CoTask co_evaluate(Engine& e, Solve& s, const uint8_t* pts, i64 np, double* fout,
                    double* ttout);
+// optfirstpivot (util.jl:78-108) for several starts (0-based) in lockstep;
+// valf gets |f| at the final pivots.
+CoTask co_optfirstpivots(Engine& e, Solve& s, std::vector<std::vector<uint8_t>>* piv, std::vector<double>* valf,
+                         int maxsweep);
+// estimatetrueerror (globalsearch.jl:19-96) with the solve's f and site tensors.
+CoTask co_estimatetrueerror(Engine& e, Solve& s, std::vector<std::vector<uint8_t>> starts,
+                            std::vector<std::pair<std::vector<uint8_t>, double>>* out);
 int addglobalpivots(Solve& s, const std::vector<std::vector<uint8_t>>& pivots);
 i64 solve_rank(const Solve& s);
 bool convergencecriterion(const std::vector<i64>& ranks, const std::vector<double>& errors,

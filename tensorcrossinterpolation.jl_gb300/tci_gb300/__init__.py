@@ -166,6 +166,10 @@ _SIGNATURES = {
     "tci_tt4_contract_tci": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
                                             ctypes.c_void_p, I64P, ctypes.c_int64, ctypes.c_int32, VALUE_FN,
                                             ctypes.c_void_p, ctypes.POINTER(Opts), ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_optfirstpivot": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P, ctypes.c_int64, ctypes.c_int32,
+                                         I64P, I64P, ctypes.c_int32]),
+    "tci_estimatetrueerror": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_int64, ctypes.c_uint64,
+                                             ctypes.c_int64, I64P, F64P, ctypes.POINTER(ctypes.c_int64)]),
     "tci_tt4_length": (ctypes.c_int32, [ctypes.c_void_p]),
     "tci_tt4_dims": (ctypes.c_int, [ctypes.c_void_p, I64P]),
     "tci_tt4_get_core": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P]),
@@ -535,6 +539,26 @@ class TensorCI2:
     def pivoterror(self):
         """pivoterror(tci) = maximum(bonderrors) (tensorci2.jl:157-159)."""
         return float(self.bonderrors.max())
+
+    def estimatetrueerror(self, nsearch=100, initialpoints=None, seed=0):
+        """estimatetrueerror(TensorTrain(tci), f; nsearch, initialpoints)
+        (globalsearch.jl:1-96) -> [(pivot, error)], error descending.  Random
+        starts come from `seed`."""
+        L = len(self)
+        if initialpoints is not None:
+            st = _pivots_array(initialpoints, L)
+        else:
+            if nsearch <= 0:
+                raise TCIError(TCI_ERR_GENERIC, "No search is performed")
+            st = np.zeros((0, L), np.int64)
+        cap = max(st.shape[0], int(nsearch), 1)
+        piv = np.zeros((cap, L), np.int64)
+        err = np.zeros(cap)
+        n = ctypes.c_int64()
+        _check(load_library().tci_estimatetrueerror(self.h, int(nsearch), _p(st, I64P) if st.size else None,
+                                                    st.shape[0], int(seed), cap, _p(piv, I64P), _p(err, F64P),
+                                                    ctypes.byref(n)))
+        return [(piv[k].copy(), float(err[k])) for k in range(min(n.value, cap))]
 
     def fcache_stats(self):
         """(distinct points stored, points passed to f, calls of f) of a solve
@@ -983,6 +1007,19 @@ def feval(f, localdims, points, ctx=None):
                                     localdims.size, _p(localdims, I64P), _p(pts, I64P), pts.shape[0],
                                     _p(out, F64P)))
     return out
+
+
+def optfirstpivot(f, localdims, firstpivot=None, maxsweep=1000, ctx=None):
+    """optfirstpivot(f, localdims, firstpivot; maxsweep) (util.jl:78-108) on the
+    device: coordinate ascent of |f| from firstpivot (1-based)."""
+    ctx = ctx or default_context()
+    d = np.ascontiguousarray(localdims, dtype=np.int64)
+    p = np.ascontiguousarray(firstpivot if firstpivot is not None else np.ones(d.size), dtype=np.int64).copy()
+    if p.size != d.size:
+        raise DimensionMismatch(TCI_ERR_DIM, "firstpivot must have one index per leg")
+    _check(load_library().tci_optfirstpivot(ctx.h, f.fid, _p(f.params, F64P) if f.params.size else None,
+                                            f.params.size, d.size, _p(d, I64P), _p(p, I64P), int(maxsweep)))
+    return p
 
 
 def convergencecriterion(ranks, errors, nglobalpivots, tolerance, maxbonddim, ncheckhistory,

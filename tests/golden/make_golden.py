@@ -103,8 +103,17 @@ def main(ref):
     integration = {"source": "test/test_integration.jl:6-28", "coefficients": coeffs, "N": 5,
                    "expect": "integrate(f, a, b) ≈ prod(P(b) - P(a)) for f(x) = prod(p.(x)), P' = p; "
                              "[0,1]^5 and a random box"}
+    util = {"optfirstpivot": {"source": "test/test_util.jl:29-37",
+                              "f": "2^2 (v3 - 1) + 2^1 (v2 - 1) + 2^0 (v1 - 1)", "localdims": [2, 2, 2],
+                              "firstpivot": [1, 1, 1], "expect": [2, 2, 2]}}
+    contraction = {"source": "test/test_contraction.jl:30-47, 68-99, 148-183",
+                   "mpo_mpo": {"bonddims_a": [1, 2, 3, 2, 1], "bonddims_b": [1, 2, 3, 2, 1],
+                               "localdims1": [2, 2, 2, 2], "localdims2": [3, 3, 3, 3], "localdims3": [2, 2, 2, 2]},
+                   "f": [None, "2x"], "algorithms": ["TCI", "naive"],
+                   "expect": "_tomat(contract(a, b)) ≈ _tomat(a) * _tomat(b) (≈ f.(...) with f)"}
     out = {"reference": "TensorCrossInterpolation.jl 0.9.19", "rrlu": cases, "rrlu_lowrank": lowrank,
-           "luci": luci_case, "tci2": tci, "integration": integration}
+           "luci": luci_case, "tci2": tci, "integration": integration, "util": util,
+           "contraction": contraction}
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_known_answers.json")
     with open(dst, "w") as fh:
         json.dump(out, fh, indent=1)
