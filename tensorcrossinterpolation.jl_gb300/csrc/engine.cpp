@@ -323,6 +323,7 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
       return 2 * a16(m * 8) + 2 * a16(n * 8) <= smem;
     case TCI_TASK_EVAL:
       t.smem_mode = 1;
+      if (t.r <= TCI_EVAL_THREAD_RMAX) return (size_t)2 * TCI_EVAL_THREAD_RMAX * TCI_STEP_THREADS * 8 <= smem;
       return (size_t)(TCI_STEP_THREADS / 32) * 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
     case TCI_TASK_SUM:
       t.smem_mode = 1;

@@ -1121,9 +1121,12 @@ __device__ void task_core(const tci_task& T, const char* blob, char* resb, char*
 }
 
 // ---------------------------------------------------------------- EVAL task
-// f and the tensor train at T.m points (rows, L sites each).  One warp per point
-// for the train: out[q] = sum_p v[p] * core[p, i, q], summed in order of p with
-// separate multiply and add, as the oracle's loop.
+constexpr int EVAL_THREAD_RMAX = TCI_EVAL_THREAD_RMAX;  // largest bond of the thread-per-point path
+
+// f and the tensor train at T.m points (rows, L sites each).  The train: one
+// thread per point for bonds up to EVAL_THREAD_RMAX, else one warp per point;
+// out[q] = sum_p v[p] * core[p, i, q], summed in order of p with separate
+// multiply and add, as the oracle's loop.
 __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl) {
   const int np = T.m, L = T.L, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const double* prm = (const double*)at(blob, T.params);
@@ -1136,7 +1139,33 @@ __device__ void task_eval(const tci_task& T, const char* blob, char* resb, char*
     for (int s = 0; s < L; ++s) tci_f_term(T.fid, prm, s, pts[(size_t)p * L + s], &a0, &a1);
     fout[p] = tci_f_finish(T.fid, prm, T.nparams, a0, a1);
   }
-  if (T.cores) {
+  if (T.cores && T.r <= EVAL_THREAD_RMAX) {
+    // bonds up to EVAL_THREAD_RMAX: one thread per point (a warp per point would
+    // leave most lanes idle), the running vector in the thread's own column of
+    // shared memory (2 x EVAL_THREAD_RMAX x NT doubles, within the step's plan)
+    const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
+    double* vs = (double*)smem;
+    double* ws = vs + (size_t)EVAL_THREAD_RMAX * NT;
+    for (int p = tid; p < np; p += NT) {
+      double* v = vs;
+      double* w = ws;
+      v[tid] = 1.0;
+      for (int s = 0; s < L; ++s) {
+        const tci_core_ref c = cr[s];
+        const int i = pts[(size_t)p * L + s];
+        for (int q = 0; q < c.r1; ++q) {
+          const double* col = c.p + (size_t)c.r0 * (i + (size_t)c.d * q);
+          double acc = 0.0;
+          for (int t = 0; t < c.r0; ++t) acc = __dadd_rn(acc, __dmul_rn(v[(size_t)t * NT + tid], col[t]));
+          w[(size_t)q * NT + tid] = acc;
+        }
+        double* tmp = v;
+        v = w;
+        w = tmp;
+      }
+      tout[p] = v[tid];
+    }
+  } else if (T.cores) {
     const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
     const int rmax = T.r;
     double* va = (double*)smem + (size_t)warp * 2 * rmax;

@@ -118,4 +118,7 @@ typedef struct tci_resident_state {
 // Threads of one task CTA, and CTAs resident per SM (the shared-memory budget of
 // a CTA is the SM's divided among them).
 #define TCI_STEP_THREADS 512
+// EVAL tasks whose bonds are at most this run one thread per point, the running
+// vector in 2 x TCI_EVAL_THREAD_RMAX x TCI_STEP_THREADS doubles of shared memory.
+#define TCI_EVAL_THREAD_RMAX 16
 #define TCI_CTAS_PER_SM 1
