@@ -101,9 +101,11 @@ int tci_f_lookup(const char* name, int* fid);
  * the multi-index, so prod(localdims) must stay below 2^104).  The callback runs
  * on the thread that made the library call, between device steps.
  * tci_f_register returns an id >= TCI_F_USER that the solve entry points
- * (tci_solve_create, tci_crossinterpolate2, tci_feval) take in place of a
- * registered function's id; the batched and serving entry points accept only
- * registered device functions. */
+ * (tci_solve_create, tci_crossinterpolate2, tci_feval, tci_optfirstpivot) take
+ * in place of a registered function's id; the batched and serving entry points
+ * accept only registered device functions.  A finalizer run inside the callback
+ * may destroy objects of the same context; entry points that compute fail with
+ * TCI_ERR_GENERIC when called from inside it. */
 typedef int (*tci_batch_fn)(void* user, int32_t L, int64_t npoints, const int64_t* points,
                             double* values);
 #define TCI_F_USER 1024
