@@ -832,7 +832,10 @@ def integrate(ValueType, f, a, b, GKorder=15, ctx=None, **kwargs):
     """integrate(ValueType, f, a, b; GKorder, kwargs...) (integration.jl:20-58):
     Gauss--Kronrod nodes per coordinate, crossinterpolate2 of
     F(i) = prod_n w[n, i_n] * f(x(i)) * GKorder^N with nsearchglobalpivot = 10,
-    then sum(tci) / GKorder^N.  f must be a ProductIntegrand."""
+    then sum(tci) / GKorder^N.  f is a ProductIntegrand (interpolated by the
+    registered device function "product") or any vectorized callable taking an
+    (npoints, N) array of coordinates and returning npoints values (a
+    caller-supplied f behind the device value cache)."""
     from .quadrature import kronrod
 
     if ValueType not in (float, np.float64, "Float64"):
@@ -844,19 +847,33 @@ def integrate(ValueType, f, a, b, GKorder=15, ctx=None, **kwargs):
     if a.size != b.size:
         raise TCIError(TCI_ERR_GENERIC, "Integral bounds must have the same dimensionality, but got "
                        f"{a.size} lower bounds and {b.size} upper bounds.")
-    if not isinstance(f, ProductIntegrand):
-        raise ArgumentError(TCI_ERR_ARG, "integrate on the device needs a ProductIntegrand "
-                            "(f(x) = prod_n g_n(x_n))")
     x1, w1, _ = kronrod(GKorder // 2)
     N = a.size
     nodes = (b - a)[:, None] * (x1[None, :] + 1.0) / 2.0 + a[:, None]
     weights = (b - a)[:, None] * w1[None, :] / 2.0
     norm = float(GKorder) ** N
-    tables = np.array([[weights[n, i] * f.factor(n)(nodes[n, i]) for i in range(x1.size)] for n in range(N)])
     kw = dict(nsearchglobalpivot=10)
     kw.update(kwargs)
-    tci, _, _ = crossinterpolate2(ValueType, product_function(tables, norm), [x1.size] * N, ctx=ctx, **kw)
+    if isinstance(f, ProductIntegrand):
+        tables = np.array([[weights[n, i] * f.factor(n)(nodes[n, i]) for i in range(x1.size)] for n in range(N)])
+        F = product_function(tables, norm)
+    else:
+        F = BatchFunction(quadrature_integrand(f, nodes, weights, norm))
+    tci, _, _ = crossinterpolate2(ValueType, F, [x1.size] * N, ctx=ctx, **kw)
     return tci.sum() / norm
+
+
+def quadrature_integrand(f, nodes, weights, norm):
+    """F(indices) = prod_n weights[n, i_n] * f(x) * norm, x_n = nodes[n, i_n]
+    (integration.jl:41-45), for a batch of 1-based multi-indices."""
+    cols = np.arange(nodes.shape[0])[None, :]
+
+    def F(idx):
+        i0 = idx - 1
+        x = nodes[cols, i0]
+        w = np.prod(weights[cols, i0], axis=1)
+        return w * np.asarray(f(x), dtype=np.float64).reshape(-1) * norm
+    return F
 
 
 def crossinterpolate2(ValueType, f, localdims, initialpivots=None, ctx=None, **kwargs):

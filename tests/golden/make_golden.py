@@ -100,9 +100,13 @@ def main(ref):
     integ_text = open(os.path.join(ref, "test", "test_integration.jl")).read()
     m = re.search(r"coefficients\s*=\s*\[(.*?)\]", integ_text, re.S)
     coeffs = [float(x) for x in m.group(1).replace("\n", " ").split(",") if x.strip()]
+    m10 = re.search(r"Iref\s*=\s*([-0-9.e]+)", integ_text)
     integration = {"source": "test/test_integration.jl:6-28", "coefficients": coeffs, "N": 5,
                    "expect": "integrate(f, a, b) ≈ prod(P(b) - P(a)) for f(x) = prod(p.(x)), P' = p; "
-                             "[0,1]^5 and a random box"}
+                             "[0,1]^5 and a random box",
+                   "tenD": {"source": "test/test_integration.jl:61-70",
+                            "f": "1000 cos(10 sum(x.^2)) exp(-sum(x)^4 / 1000)", "N": 10, "a": -1.0, "b": 1.0,
+                            "GKorder": 15, "tolerance": 1e-8, "Iref": float(m10.group(1)), "abs_tol": 1e-3}}
     util = {"optfirstpivot": {"source": "test/test_util.jl:29-37",
                               "f": "2^2 (v3 - 1) + 2^1 (v2 - 1) + 2^0 (v1 - 1)", "localdims": [2, 2, 2],
                               "firstpivot": [1, 1, 1], "expect": [2, 2, 2]}}

@@ -3,7 +3,9 @@
 reference's 15-coefficient polynomial p over [0,1]^5 and over a random box
 equals prod_n (P(b_n) - P(a_n)), P' = p, to the reference's `≈` (sqrt(eps)).
 The CPU tests run the oracle's crossinterpolate2 on the same device-function
-parameters; the GPU test runs the library's integrate()."""
+parameters; the GPU test runs the library's integrate().  A general integrand
+(a caller-supplied f) is checked on the reference's 10-D integral
+(test/test_integration.jl:61-70), within its 1e-3."""
 import numpy as np
 import pytest
 
@@ -77,3 +79,37 @@ def test_gpu_integrates_reference_polynomials(T, oracle, golden):
     got = T.integrate(float, f, a, b)
     assert got == pytest.approx(np.prod(P(b) - P(a)), rel=1.5e-8)
     assert got == pytest.approx(_oracle_integrate(T, oracle, p, a, b), rel=1e-12)
+
+
+def _tend_f(x):
+    """test/test_integration.jl:64-66, vectorized over rows of x."""
+    return 1000.0 * np.cos(10.0 * (x ** 2).sum(1)) * np.exp(-x.sum(1) ** 4 / 1000.0)
+
+
+def test_oracle_integrates_reference_10d_function(T, oracle, golden):
+    """The reference's 10-D integral (test/test_integration.jl:61-70) through the
+    oracle with the same quadrature integrand the library builds."""
+    from tci_gb300.quadrature import kronrod
+
+    g = golden["integration"]["tenD"]
+    N, GK = g["N"], g["GKorder"]
+    x1, w1, _ = kronrod(GK // 2)
+    a, b = np.full(N, g["a"]), np.full(N, g["b"])
+    nodes = (b - a)[:, None] * (x1[None, :] + 1.0) / 2.0 + a[:, None]
+    weights = (b - a)[:, None] * w1[None, :] / 2.0
+    norm = float(GK) ** N
+    fid = oracle.register_fn(T.quadrature_integrand(_tend_f, nodes, weights, norm))
+    ref, _, _ = oracle.crossinterpolate2([x1.size] * N, fid, (), None, tolerance=g["tolerance"],
+                                         nsearchglobalpivot=10)
+    assert abs(ref.sum() / norm - g["Iref"]) < g["abs_tol"]
+
+
+@pytest.mark.gpu
+def test_gpu_integrates_reference_10d_function(T, golden):
+    """integrate(Float64, f, -ones(10), ones(10); GKorder=15, tolerance=1e-8) of a
+    general integrand (a caller-supplied f) within 1e-3 of the reference's value."""
+    g = golden["integration"]["tenD"]
+    N = g["N"]
+    got = T.integrate(float, _tend_f, np.full(N, g["a"]), np.full(N, g["b"]), GKorder=g["GKorder"],
+                      tolerance=g["tolerance"])
+    assert abs(got - g["Iref"]) < g["abs_tol"]
