@@ -358,3 +358,59 @@ def test_incremental_server(T):
         assert st == 0 and lat > 0
         ta, _, _ = T.crossinterpolate2(float, f, dims, **kw)
         assert ta.rank() == rank
+
+
+def _quantics_index(x, R):
+    """1-based bits of floor(x 2^R), most significant first (a 1-D quantics grid on [0, 1))."""
+    k = int(np.floor(x * 2 ** R))
+    return [((k >> (R - 1 - i)) & 1) + 1 for i in range(R)]
+
+
+@pytest.mark.parametrize("strictlynested,nsearch", [(False, 0), (True, 0), (False, 10)])
+def test_trivial_mps_exp(T, oracle, strictlynested, nsearch):
+    """test/test_tensorci2.jl:55-104: f(x) = exp(-x) on an 8-bit quantics grid,
+    maxbonddim 1, two first pivots: all link dimensions 1 and |tci(x) - f(x)| < 1e-4
+    at x = 0.1, 0.3, 0.6, 0.9; pivots equal the oracle's."""
+    R = 8
+    f = T.DeviceFunction("qtt1d", [1])
+    first = [[1] * R, [1] + [2] * (R - 1)]
+    kw = dict(tolerance=1e-4, maxbonddim=1, maxiter=2, normalizeerror=False, nsearchglobalpivot=nsearch,
+              strictlynested=strictlynested)
+    tci, ranks, _ = T.crossinterpolate2(float, f, [2] * R, first, **kw)
+    assert list(tci.linkdims()) == [1] * (R - 1)
+    ref, rranks, _ = oracle.crossinterpolate2([2] * R, oracle.F_QTT1D, [1], first, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    tt = tci.tensortrain()
+    for x in [0.1, 0.3, 0.6, 0.9]:
+        v = _quantics_index(x, R)
+        fx = np.exp(-np.floor(x * 2 ** R) / 2 ** R)
+        assert abs(tci.evaluate(v) - fx) < 1e-4
+        assert abs(tt.evaluate(v) - fx) < 1e-4
+
+
+def test_trivial_mps_exp_small_maxbonddim(T, oracle):
+    """test/test_tensorci2.jl:168-213: exp(-x) + 1e-4 exp(-2x), tolerance 1e-10 but
+    maxbonddim 1, nsearchglobalpivot 10: link dimensions 1, error below 1e-4."""
+    R = 8
+    f = T.DeviceFunction("qtt1d", [2])
+    first = [[1] * R, [1] + [2] * (R - 1)]
+    kw = dict(tolerance=1e-10, maxbonddim=1, maxiter=10, normalizeerror=False, nsearchglobalpivot=10)
+    tci, ranks, _ = T.crossinterpolate2(float, f, [2] * R, first, **kw)
+    assert list(tci.linkdims()) == [1] * (R - 1)
+    ref, rranks, _ = oracle.crossinterpolate2([2] * R, oracle.F_QTT1D, [2], first, **kw)
+    assert list(ranks) == list(rranks)
+    _same_sets(tci, ref)
+    for x in [0.1, 0.3, 0.6, 0.9]:
+        v = _quantics_index(x, R)
+        t = np.floor(x * 2 ** R) / 2 ** R
+        assert abs(tci.evaluate(v) - (np.exp(-t) + 1e-4 * np.exp(-2 * t))) < 1e-4
+
+
+def test_trivial_mps_one_pivot(T):
+    """test/test_tensorci2.jl:215-232: TensorCI2(f, fill(2, n), [fill(1, n)]) has rank 1."""
+    n = 5
+    tci = T.TensorCI2(T.BatchFunction(lambda p: 0.5 * p.sum(1).astype(float)), [2] * n, [[1] * n])
+    assert len(tci) == n
+    assert tci.rank() == 1
+    assert list(tci.linkdims()) == [1] * (n - 1)
