@@ -738,11 +738,11 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
         raise ArgumentError(TCI_ERR_ARG, f"Unknown algorithm {algorithm}.")
     if method not in FACTORIZE:
         raise TCIError(TCI_ERR_GENERIC, f"method=:{method} is not available on the device (:LU, :CI)")
-    ctx = ctx or default_context()
     a, a3 = _as_tt4(A, True)
     b, b3 = _as_tt4(B, False)
     if len(a) != len(b):
         raise ArgumentError(TCI_ERR_ARG, "Cannot contract tensor trains with different length.")
+    ctx = ctx or default_context()
     a, ad, ap = _tt4_args(a)
     b, bd, bp = _tt4_args(b)
     h = ctypes.c_void_p()
@@ -757,11 +757,11 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
 
 def _contract_tci(A, B, tolerance, maxbonddim, f, initialpivots, ctx, kwargs):
     """contract_TCI (contraction.jl:399-434) through tci_tt4_contract_tci."""
-    ctx = ctx or default_context()
     a, a3 = _as_tt4(A, True)
     b, b3 = _as_tt4(B, False)
     if len(a) != len(b):
         raise ArgumentError(TCI_ERR_ARG, "Cannot contract tensor trains with different length.")
+    ctx = ctx or default_context()
     a, ad, ap = _tt4_args(a)
     b, bd, bp = _tt4_args(b)
     L = len(a)
@@ -787,8 +787,8 @@ def compress(tt, method="LU", tolerance=1e-12, maxbonddim=None, normalizeerror=T
     TensorTrain."""
     if method not in FACTORIZE:
         raise TCIError(TCI_ERR_GENERIC, f"method=:{method} is not available on the device (:LU, :CI)")
-    ctx = ctx or default_context()
     cores, three = _as_tt4(tt, True)
+    ctx = ctx or default_context()
     cores, d, ptrs = _tt4_args(cores)
     h = ctypes.c_void_p()
     _check(load_library().tci_tt4_compress(ctx.h, len(cores), _p(d, I64P), ptrs, FACTORIZE[method],
