@@ -39,3 +39,26 @@ def test_library_registry(T):
         T._check(T.load_library().tci_f_unregister(old + 1000))
     f2.close()
     f3.close()
+
+
+def test_oracle_reconstructs_a_tensor_train(oracle):
+    """test/test_tensorci2.jl:477-502: crossinterpolate2 of a function that is itself
+    a tensor train (bonds 1, 2, 3, 2, 1; local dims 2, 3, 3, 2), tolerance 1e-10,
+    maxbonddim 10, reproduces it at every point."""
+    rng = np.random.default_rng(5)
+    bonds, dims = [1, 2, 3, 2, 1], [2, 3, 3, 2]
+    cores = [rng.random((bonds[n], dims[n], bonds[n + 1])) for n in range(4)]
+
+    def tt(p):
+        out = np.empty(p.shape[0])
+        for k, q in enumerate(p):
+            v = np.ones(1)
+            for n, c in enumerate(cores):
+                v = v @ c[:, q[n] - 1, :]
+            out[k] = v[0]
+        return out
+
+    fid = oracle.register_fn(tt)
+    ref, _, _ = oracle.crossinterpolate2(dims, fid, (), None, tolerance=1e-10, maxbonddim=10)
+    pts = np.array(list(np.ndindex(*dims))) + 1
+    assert np.allclose(ref.evaluate(pts), tt(pts), rtol=1e-9, atol=1e-12)
