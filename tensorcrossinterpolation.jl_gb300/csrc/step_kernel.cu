@@ -9,8 +9,8 @@
 //          _optimizerrlu!/addpivot! (matrixlu.jl:98-181), then optionally
 //          left/right of MatrixLUCI (matrixluci.jl:40-84).
 //   SITE : setsitetensor!(tci, f, b) (tensorci2.jl:367-394): the pivot matrix P
-//          is factored by the same full-pivot LU and T = Pi1 * inv(P) is solved
-//          row by row.
+//          is factored with partial pivoting in LAPACK's order and
+//          T = Pi1 * inv(P) is solved row by row.
 //   CORE : core = Pi1 (tensorci2.jl:379-383, :449-459).
 //   EVAL : f and the tensor train at points (globalpivotfinder.jl:167-177,
 //          abstracttensortrain.jl:124-132).
@@ -598,11 +598,8 @@ __device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C
 
 // Trailing blocks of at most this many elements are finished by warp 0 alone:
 // with one warp no CTA barrier is needed per pivot.  Measured: up to ~6 elements
-// per lane one warp beats the barriers of the whole CTA (192, RRLU tasks); the
-// full-rank factorization of a SITE task's pivot matrix (at most ~32 x 32 on the
-// served stream) is fastest entirely in one warp (1024).
+// per lane one warp beats the barriers of the whole CTA.
 constexpr int WARP_TAIL_RRLU = 192;
-constexpr int WARP_TAIL_SITE = 1024;
 
 // rrlu_loop from pivot K on (decision for K already taken, not stopped), warp 0
 // only; same arithmetic and argmax as the CTA path.  Returns the final K on
@@ -812,14 +809,15 @@ __device__ void post_left(double* A, int lda, int m, int n, int K, bool leftorth
                           double* out) {
   const int tid = threadIdx.x;
   if (leftorth) {
-    // X * L11 = L21, processed right to left; one thread per row of L21.
+    // X * L11 = L21 with unit-lower L11, one thread per row of L21, in the
+    // oracle's order: X[p, q] = L21[p, q] - sum over t = q+1 .. K-1 (ascending)
+    // of X[p, t] * L11[t, q], for q from K-1 down to 0 (the division by the
+    // unit diagonal is exact and omitted).
     for (int p = K + tid; p < m; p += NT) {
       for (int q = K - 1; q >= 0; --q) {
-        double zq = A[p + (size_t)q * lda];
-        for (int s = 0; s < q; ++s) {
-          double l = A[q + (size_t)s * lda];
-          A[p + (size_t)s * lda] = A[p + (size_t)s * lda] - zq * l;
-        }
+        double s = A[p + (size_t)q * lda];
+        for (int t = q + 1; t < K; ++t) s = s - A[p + (size_t)t * lda] * A[t + (size_t)q * lda];
+        A[p + (size_t)q * lda] = s;
       }
     }
     __syncthreads();
@@ -862,12 +860,15 @@ __device__ void post_right(double* A, int lda, int m, int n, int K, bool leftort
         out[q + (size_t)colperm[j] * K] = s;
       }
   } else {
-    // U11 X = U12 with unit-upper U11; one thread per column of U12.
+    // U11 X = U12 with unit-upper U11, one thread per column of U12, in the
+    // oracle's order: X[q, j] = U12[q, j] - sum over p = q+1 .. K-1 (ascending)
+    // of U11[q, p] * X[p, j], for q from K-1 down to 0.
     for (int j = K + tid; j < n; j += NT) {
       double* col = A + (size_t)j * lda;
       for (int q = K - 1; q >= 0; --q) {
-        double xq = col[q];
-        for (int p = 0; p < q; ++p) col[p] = col[p] - A[p + (size_t)q * lda] * xq;
+        double s = col[q];
+        for (int p = q + 1; p < K; ++p) s = s - A[q + (size_t)p * lda] * col[p];
+        col[q] = s;
       }
     }
     __syncthreads();
@@ -978,16 +979,160 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
 }
 
 // ---------------------------------------------------------------- SITE task
-// T.r x T.r pivot matrix P = f(prows x cols); Pi1 = f(rows x cols) (m x r).
+// Warp-wide pivot search of column j of A (lda = r) over rows j .. r-1 with the
+// rule of LAPACK's partial pivoting as the oracle states it: start from |A[j,j]|
+// and take the first row whose |a| is strictly larger than the running best
+// (NaN never wins; a NaN diagonal keeps row j).  Bit patterns of |a| order like
+// the values, so the search runs on the integer pipe.  Every lane gets the row.
+__device__ int site_col_pivot(const double* col, int j, int r) {
+  const int lane = threadIdx.x & 31;
+  uint64_t s = 0;  // |a| bits + 1 of this lane's first maximum, 0 = none
+  int si = INT_MAX;
+  for (int i = j + 1 + lane; i < r; i += 32) {
+    const uint64_t b = abs_bits(col[i]);
+    if (b <= NAN_FLOOR && b + 1 > s) {
+      s = b + 1;
+      si = i;
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t os = __shfl_xor_sync(FULL, s, off);
+    const int oi = __shfl_xor_sync(FULL, si, off);
+    if (os > s || (os == s && oi < si)) {
+      s = os;
+      si = oi;
+    }
+  }
+  const uint64_t d = abs_bits(col[j]);
+  if (d > NAN_FLOOR) return j;
+  return s > d + 1 ? si : j;
+}
+
+// getrf with partial pivoting of the r x r matrix A (lda = r), in the oracle's
+// order: per column j, the pivot row p (site_col_pivot), a whole-row swap of
+// rows j and p, the column below the diagonal times the IEEE reciprocal of the
+// pivot, then the rank-1 update of the trailing block as a separate multiply
+// and subtract.  ipiv[j] = p.  Returns (to every thread) 1 when a pivot is
+// exactly zero -- the reference's SingularException -- else 0.
+// Two block barriers per column: (swap + scale) and (update + next pivot
+// search); warp 0 owns the column being scaled and the next column, whose
+// update it fuses with the search.  Matrices of at most 32 rows run on warp 0
+// alone with warp-level synchronisation.
+__device__ int site_getrf(double* A, int r, int* ipiv, Ctl& ctl) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (r <= 32) {
+    if (warp == 0) {
+      int sing = 0;
+      for (int j = 0; j < r; ++j) {
+        const int p = site_col_pivot(A + (size_t)j * r, j, r);
+        const double piv = A[p + (size_t)j * r];
+        if (piv == 0.0) {
+          sing = 1;
+          break;
+        }
+        if (lane == 0) ipiv[j] = p;
+        __syncwarp();
+        if (p != j && lane < r) {
+          const double a = A[j + (size_t)lane * r], b = A[p + (size_t)lane * r];
+          A[j + (size_t)lane * r] = b;
+          A[p + (size_t)lane * r] = a;
+        }
+        __syncwarp();
+        const double rcp = 1.0 / A[j + (size_t)j * r];
+        if (lane > j && lane < r) A[lane + (size_t)j * r] = A[lane + (size_t)j * r] * rcp;
+        __syncwarp();
+        if (lane > j && lane < r)
+          for (int c = j + 1; c < r; ++c)
+            A[lane + (size_t)c * r] = A[lane + (size_t)c * r] - A[lane + (size_t)j * r] * A[j + (size_t)c * r];
+        __syncwarp();
+      }
+      if (lane == 0) ctl.status = sing;
+    }
+    __syncthreads();
+    const int s = ctl.status;
+    __syncthreads();
+    return s;
+  }
+  if (warp == 0) {
+    const int p = site_col_pivot(A, 0, r);
+    if (lane == 0) {
+      ctl.r = p;
+      ctl.piv = A[p];
+    }
+  }
+  __syncthreads();
+  for (int j = 0; j < r; ++j) {
+    const int p = ctl.r;
+    const double piv = ctl.piv;
+    if (piv == 0.0) {
+      __syncthreads();
+      return 1;
+    }
+    // swap rows j and p (warp 0 takes column j and scales it)
+    if (warp == 0) {
+      double* cj = A + (size_t)j * r;
+      const double djj = cj[j];
+      __syncwarp();
+      const double rcp = 1.0 / piv;
+      for (int i = j + 1 + lane; i < r; i += 32) {
+        const double v = i == p ? djj : cj[i];
+        cj[i] = v * rcp;
+      }
+      if (lane == 0) {
+        cj[j] = piv;
+        ipiv[j] = p;
+      }
+    } else if (p != j) {
+      for (int c = tid - 32; c < r; c += NT - 32) {
+        if (c == j) continue;
+        const double a = A[j + (size_t)c * r], b = A[p + (size_t)c * r];
+        A[j + (size_t)c * r] = b;
+        A[p + (size_t)c * r] = a;
+      }
+    }
+    __syncthreads();
+    // trailing update; warp 0 updates column j+1 and searches its pivot
+    const double* lj = A + (size_t)j * r;
+    if (warp == 0) {
+      if (j + 1 < r) {
+        double* c1 = A + (size_t)(j + 1) * r;
+        const double y = c1[j];
+        for (int i = j + 1 + lane; i < r; i += 32) c1[i] = c1[i] - lj[i] * y;
+        __syncwarp();
+        const int pn = site_col_pivot(c1, j + 1, r);
+        if (lane == 0) {
+          ctl.r = pn;
+          ctl.piv = c1[pn];
+        }
+      }
+    } else {
+      for (int c = j + 2 + (warp - 1); c < r; c += NW - 1) {
+        double* cc = A + (size_t)c * r;
+        const double y = cc[j];
+        for (int i = j + 1 + lane; i < r; i += 32) cc[i] = cc[i] - lj[i] * y;
+      }
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
+// setsitetensor!(tci, f, b) (tensorci2.jl:367-394): P (r x r) = f(prows x cols),
+// Pi1 (m x r) = f(rows x cols), T = Pi1 * inv(P) from transpose(P) \ transpose(Pi1)
+// (:391), i.e. getrf of A = P^T with partial pivoting and, per row of Pi1, the
+// row interchanges, the unit-lower forward substitution and the upper back
+// substitution (division by the diagonal) -- the order of the oracle's LAPACK
+// restatement, so the tensor equals the oracle's bit for bit.
 __device__ void task_site(const tci_task& T, const char* blob, char* resb, char* smem, Ctl& ctl,
                           size_t smem_bytes) {
   const int r = T.r, m = T.m, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   ResPtrs rp = res_ptrs(resb, T);
   const double* prm = (const double*)at(blob, T.params);
   SmemCursor cur{smem};
-  double* P = T.smem_mode ? (double*)cur.take((size_t)r * r * 8) : T.work;
-  int* rowperm = (int*)cur.take((size_t)r * 4);
-  int* colperm = (int*)cur.take((size_t)r * 4);
+  double* A = T.smem_mode ? (double*)cur.take((size_t)r * r * 8) : T.work;
+  int* ipiv = (int*)cur.take((size_t)r * 4);
+  (void)cur.take((size_t)r * 4);  // unused slot (keeps the host's shared-memory plan)
   double* ps0 = (double*)cur.take((size_t)r * 8);
   double* ps1 = (double*)cur.take((size_t)r * 8);
   double* cs0 = (double*)cur.take((size_t)r * 8);
@@ -997,37 +1142,17 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   compute_states(T, prm, (const uint8_t*)at(blob, T.prows), r, T.nl, 0, ps0, ps1);
   compute_states(T, prm, (const uint8_t*)at(blob, T.cols), r, T.nr, T.nl, cs0, cs1);
   compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
-  for (int i = tid; i < r; i += NT) {
-    rowperm[i] = i;
-    colperm[i] = i;
-  }
   __syncthreads();
   double* const rg0[2] = {ps0, rs0};
   double* const rg1[2] = {ps1, rs1};
   const int rc[2] = {r, m};
   const Filler F = make_filler(T, prm, rg0, rg1, rc, 2, cs0, cs1, r, (int64_t)(r + m) * r, ctl);
-  ArgTrack am;
-  am.init();
+  // A[i, j] = P[j, i] = f(prows[j] ++ cols[i])
   for (int j = warp; j < r; j += NW)
-    for (int i = lane; i < r; i += 32) {
-      double v = F.val(ps0, ps1, i, cs0, cs1, j);
-      P[i + (size_t)j * r] = v;
-      am.push(v, pack_key(i, j));
-    }
-  argmax_resolve(am, P, r, 0, r, 0, r, ctl);
-  rrlu_loop(P, r, r, r, r, 0.0, 0.0, true, rowperm, colperm, rp.diag, ctl, nullptr, WARP_TAIL_SITE);
-  int singular = 0;
-  if (tid == 0) {
-    for (int k = 0; k < r; ++k)
-      if (!(P[k + (size_t)k * r] != 0.0)) singular = 1;
-    if (ctl.K < r) singular = 1;
-    ctl.status = singular ? TCI_ST_SINGULAR : 0;
-  }
+    for (int i = lane; i < r; i += 32) A[i + (size_t)j * r] = F.val(ps0, ps1, j, cs0, cs1, i);
   __syncthreads();
-  // T = Pi1 * inv(P): per row, w = Pi1[row, colperm]; z U = w; s L = z; t[rowperm] = s.
-  // The diagonal of U is inverted once; rows multiply by the reciprocals.
-  double* dinv = (double*)cur.take((size_t)r * 8);
-  for (int q = tid; q < r; q += NT) dinv[q] = 1.0 / P[q + (size_t)q * r];
+  const int singular = site_getrf(A, r, ipiv, ctl);
+  (void)cur.take((size_t)r * 8);  // unused slot (keeps the host's shared-memory plan)
   size_t used = (size_t)(cur.p - smem);
   int RB = (int)((smem_bytes > used ? smem_bytes - used : 0) / ((size_t)r * 8 + 8));
   RB = RB > NT ? NT : RB;
@@ -1039,43 +1164,49 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     const int rows_here = min(RB, m - base);
     for (int e = tid; e < rows_here * r; e += NT) {
       int rr = e % rows_here, q = e / rows_here;
-      int row = base + rr, col = colperm[q];
-      double v = F.val(rs0, rs1, row, cs0, cs1, col);
+      double v = F.val(rs0, rs1, base + rr, cs0, cs1, q);
       W[rr + (size_t)q * RB] = v;
       unsigned long long b = abs_bits(v);
       mx = b > mx ? b : mx;
     }
     __syncthreads();
-    if (ctl.status == 0) {
+    if (!singular) {
       for (int rr = tid; rr < rows_here; rr += NT) {
-        // forward: z U = w (U upper, non-unit)
-        for (int q = 0; q < r; ++q) {
-          double zq = W[rr + (size_t)q * RB] * dinv[q];
-          W[rr + (size_t)q * RB] = zq;
-          for (int p = q + 1; p < r; ++p) W[rr + (size_t)p * RB] = W[rr + (size_t)p * RB] - zq * P[q + (size_t)p * r];
+        double* w = W + rr;
+        for (int j = 0; j < r; ++j) {
+          const int p = ipiv[j];
+          if (p != j) {
+            const double a = w[(size_t)j * RB];
+            w[(size_t)j * RB] = w[(size_t)p * RB];
+            w[(size_t)p * RB] = a;
+          }
         }
-        // backward: s L = z (L unit lower)
-        for (int q = r - 1; q >= 0; --q) {
-          double sq = W[rr + (size_t)q * RB];
-          for (int p = 0; p < q; ++p) W[rr + (size_t)p * RB] = W[rr + (size_t)p * RB] - sq * P[q + (size_t)p * r];
+        for (int j = 0; j < r; ++j) {
+          const double bj = w[(size_t)j * RB];
+          for (int i = j + 1; i < r; ++i) w[(size_t)i * RB] = w[(size_t)i * RB] - A[i + (size_t)j * r] * bj;
+        }
+        for (int j = r - 1; j >= 0; --j) {
+          const double bj = w[(size_t)j * RB] / A[j + (size_t)j * r];
+          w[(size_t)j * RB] = bj;
+          for (int i = 0; i < j; ++i) w[(size_t)i * RB] = w[(size_t)i * RB] - A[i + (size_t)j * r] * bj;
         }
       }
     }
     __syncthreads();
     for (int e = tid; e < rows_here * r; e += NT) {
-      int rr = e % rows_here, p = e / rows_here;
-      double v = W[rr + (size_t)p * RB];
+      int rr = e % rows_here, q = e / rows_here;
+      double v = W[rr + (size_t)q * RB];
       if (v != v) nanflag = 1;
-      T.core_out[(base + rr) + (size_t)rowperm[p] * m] = v;
+      T.core_out[(base + rr) + (size_t)q * m] = v;
     }
     __syncthreads();
   }
   unsigned long long mxall = block_max_u64(mx, ctl);
   int nan = block_or(nanflag, ctl);
   if (tid == 0) {
-    rp.head->status = ctl.status | (nan ? TCI_ST_NAN : 0);
-    rp.head->npivot = ctl.K;
-    rp.head->error = ctl.err;
+    rp.head->status = (singular ? TCI_ST_SINGULAR : 0) | (nan ? TCI_ST_NAN : 0);
+    rp.head->npivot = singular ? 0 : r;
+    rp.head->error = 0.0;
     rp.head->maxabs = __longlong_as_double((long long)mxall);
     rp.head->maxabs_nan = mxall > NAN_FLOOR ? 1 : 0;
     rp.head->lut_used = F.lut0 != nullptr;
@@ -2072,6 +2203,7 @@ cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* orde
 // error codes of include/tci_gb300.h (that header's function ids clash with
 // tci_functions.h, so it is not included here)
 #define TCI_ERR_ARG 1
+#define TCI_ERR_NAN 3
 #define TCI_ERR_CUDA 6
 
 namespace tci {
@@ -2096,9 +2228,11 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_noalloc_kernel(const
 }
 
 // Copies the result record and the factors from the scratch array to the
-// caller's buffers.
+// caller's buffers; *status = TCI_ERR_NAN when L or U holds a NaN (the
+// reference's ErrorException "lu.L contains NaNs", matrixlu.jl:164-169), else 0.
 __global__ void rrlu_noalloc_epilogue(const double* fact, const char* resb, int m, int n, int32_t* rowperm,
-                                      int32_t* colperm, int32_t* npivot, double* error, double* factors_out) {
+                                      int32_t* colperm, int32_t* npivot, double* error, int32_t* status,
+                                      double* factors_out) {
   const tci_result_head* h = (const tci_result_head*)resb;
   const int32_t* perms = (const int32_t*)(fact + (size_t)m * n);
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
@@ -2109,6 +2243,7 @@ __global__ void rrlu_noalloc_epilogue(const double* fact, const char* resb, int 
   if (tid == 0) {
     *npivot = h->npivot;
     *error = h->error;
+    *status = (h->status & TCI_ST_NAN) ? TCI_ERR_NAN : 0;
   }
 }
 
@@ -2122,10 +2257,13 @@ struct NoallocDevice {
 // See include/tci_gb300.h.  The first call on a device resolves the device
 // address of the scratch array (cudaGetSymbolAddress) and raises the kernel's
 // shared-memory limit, with that device current; make that first call before
-// any stream capture.  Later calls only launch two kernels on `stream_u`.
+// any stream capture.  Later calls only launch two kernels on `stream_u`.  The
+// address is cached per device for the life of the process, so a device reset
+// (cudaDeviceReset) after the first call is not supported.
 extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank, double reltol,
                                 double abstol, int32_t leftorthogonal, int32_t* rowperm_dev, int32_t* colperm_dev,
-                                int32_t* npivot_dev, double* error_dev, double* factors_dev, uintptr_t stream_u) {
+                                int32_t* npivot_dev, double* error_dev, int32_t* status_dev, double* factors_dev,
+                                uintptr_t stream_u) {
   static std::mutex mu;
   static NoallocDevice devs[64];
   if (m < 1 || n < 1 || m > NOALLOC_MAX_DIM || n > NOALLOC_MAX_DIM || m * n > NOALLOC_MAX_ELEMS) {
@@ -2135,12 +2273,20 @@ extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64
                                             " x " + std::to_string(n) + ")");
     return TCI_ERR_ARG;
   }
-  if (!A_dev || !rowperm_dev || !colperm_dev || !npivot_dev || !error_dev) {
+  if (!A_dev || !rowperm_dev || !colperm_dev || !npivot_dev || !error_dev || !status_dev) {
     tci::set_error(TCI_ERR_ARG, "tci_rrlu_noalloc: null input or output pointer");
     return TCI_ERR_ARG;
   }
+  // A launch error left pending by earlier work on this thread is reported,
+  // not cleared: the caller's own error check still sees it.
+  cudaError_t ce = cudaPeekAtLastError();
+  if (ce != cudaSuccess) {
+    tci::set_error(TCI_ERR_CUDA, std::string("tci_rrlu_noalloc: a CUDA error was pending before the call: ") +
+                                     cudaGetErrorString(ce));
+    return TCI_ERR_CUDA;
+  }
   int dev = 0;
-  cudaError_t ce = cudaGetDevice(&dev);
+  ce = cudaGetDevice(&dev);
   if (ce != cudaSuccess || dev < 0 || dev >= 64) {
     tci::set_error(TCI_ERR_CUDA,std::string("tci_rrlu_noalloc: ") + cudaGetErrorString(ce));
     return TCI_ERR_CUDA;
@@ -2190,7 +2336,7 @@ extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64
   cudaStream_t stream = (cudaStream_t)stream_u;
   rrlu_noalloc_kernel<<<1, NT, smem, stream>>>(T, resb);
   rrlu_noalloc_epilogue<<<64, 256, 0, stream>>>(fact, resb, (int)m, (int)n, rowperm_dev, colperm_dev, npivot_dev,
-                                                error_dev, factors_dev);
+                                                error_dev, status_dev, factors_dev);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) {
     tci::set_error(TCI_ERR_CUDA,std::string("tci_rrlu_noalloc: ") + cudaGetErrorString(ce));

@@ -1,9 +1,12 @@
 """GPU crossinterpolate2 / TensorCI2 against the CPU oracle.
 
 The registered functions evaluate bit-identically on both sides and the rrLU is
-bit-exact, so pivot index sets and ranks must match exactly.  Site tensors come
-from a different (but stable) solve of T = Pi1 * inv(P) than the reference's
-LAPACK call and are compared to a tolerance; so are evaluate() and sum().
+bit-exact, so pivot index sets and ranks must match exactly.  The final site
+tensors (left(MatrixLUCI) of sweep1site!, tensorci2.jl:402-461, and the last
+Pi1) follow the oracle's operation order, so they are compared bit for bit, and
+sum() to 1e-12 relative.  The sampled error on 1e5 seeded lattice points must
+be within the requested tolerance (relative to maxsamplevalue, the reference's
+normalizeerror) and at most 2x the oracle's.
 """
 import itertools
 
@@ -66,7 +69,8 @@ def test_lorentz5_parity(T, oracle, tol):
     pts = np.array(list(itertools.product(*[range(1, 4)] * 5)))
     assert np.allclose(tci.evaluate(pts), 1.0 / (1.0 + (pts ** 2).sum(1)), rtol=max(tol, 1e-12) * 10)
     for b in range(1, 6):
-        assert np.allclose(tci.sitetensor(b), ref.core(b), rtol=1e-9, atol=1e-12)
+        assert np.array_equal(tci.sitetensor(b), ref.core(b)), f"site tensor {b} differs"
+    assert tci.sum() == ref.sum()
 
 
 def test_config1_lorentz8(T, oracle):
@@ -81,12 +85,27 @@ def test_config1_lorentz8(T, oracle):
     _same_sets(tci, ref)
     pts = np.random.default_rng(1234).integers(1, 11, size=(100000, 8))
     fx = 1.0 / (1.0 + (pts ** 2).sum(1))
-    err_gpu = np.max(np.abs(tci.evaluate(pts) - fx))
-    err_ref = np.max(np.abs(ref.evaluate(pts) - fx))
-    assert err_gpu <= 1e-8 * tci.maxsamplevalue * 10
-    assert err_gpu <= 2 * err_ref + 1e-15
+    _check_sampled_error(tci, ref, pts, fx, 1e-8)
+    for b in range(1, 9):
+        assert np.array_equal(tci.sitetensor(b), ref.core(b)), f"site tensor {b} differs"
     s, sr = tci.sum(), ref.sum()
     assert abs(s - sr) <= 1e-12 * abs(sr)
+
+
+def _check_sampled_error(tci, ref, pts, fx, tol, margin=1.0):
+    """Max |f - tt| on the sampled points: at most 2x the oracle's and within
+    margin x the requested tolerance, relative to maxsamplevalue (optimize!
+    normalises its errors, tensorci2.jl:711, :843-845).  margin = 1 where the
+    reference's algorithm itself meets the tolerance on the sample; the quantics
+    configurations use the reference's own guarantee instead: its global pivot
+    search only adds points whose error exceeds tolmarginglobalsearch (10) x
+    tol (globalpivotfinder.jl:179-182), and the oracle's sampled error there is
+    1.5x (R = 40, tol 1e-10) and 1.3x (2-D, tol 1e-9) the tolerance."""
+    err_gpu = float(np.max(np.abs(tci.evaluate(pts) - fx)))
+    err_ref = float(np.max(np.abs(ref.evaluate(pts) - fx)))
+    assert err_gpu <= margin * tol * tci.maxsamplevalue, (err_gpu, tci.maxsamplevalue)
+    assert err_gpu <= 2 * err_ref + 1e-300, (err_gpu, err_ref)
+    return err_gpu, err_ref
 
 
 def _served(rng, L, d):
@@ -122,7 +141,12 @@ def test_quantics_1d(T, oracle):
     ref, rranks, _ = oracle.crossinterpolate2([2] * 40, oracle.F_QTT1D, [0], None, **kw)
     assert list(ranks) == list(rranks)
     _same_sets(tci, ref)
-    assert abs(tci.sum() - ref.sum()) <= 1e-12 * abs(ref.sum()) + 1e-15
+    for b in range(1, 41):
+        assert np.array_equal(tci.sitetensor(b), ref.core(b)), f"site tensor {b} differs"
+    assert abs(tci.sum() - ref.sum()) <= 1e-12 * abs(ref.sum())
+    pts = np.random.default_rng(10).integers(1, 3, size=(100000, 40))
+    fx = oracle.feval(oracle.F_QTT1D, [0], pts)
+    _check_sampled_error(tci, ref, pts, fx, 1e-10, margin=10.0)
 
 
 def test_quantics_2d_config(T, oracle):
@@ -133,12 +157,12 @@ def test_quantics_2d_config(T, oracle):
     ref, rranks, _ = oracle.crossinterpolate2([4] * 30, oracle.F_QTT2D, [], None, **kw)
     assert list(ranks) == list(rranks)
     _same_sets(tci, ref)
-    pts = np.random.default_rng(9).integers(1, 5, size=(10000, 30))
-    assert np.allclose(tci.evaluate(pts), ref.evaluate(pts), rtol=0, atol=1e-12)
-    # the sum over 4^30 points of this oscillating function is ~ -199 out of terms
-    # of size 1: cancellation amplifies the last-bit differences of the site
-    # tensors (LU solve order) to ~1e-5 relative in both implementations
-    assert abs(tci.sum() - ref.sum()) <= 1e-4 * abs(ref.sum())
+    for b in range(1, 31):
+        assert np.array_equal(tci.sitetensor(b), ref.core(b)), f"site tensor {b} differs"
+    assert abs(tci.sum() - ref.sum()) <= 1e-12 * abs(ref.sum())
+    pts = np.random.default_rng(9).integers(1, 5, size=(100000, 30))
+    fx = oracle.feval(oracle.F_QTT2D, [], pts)
+    _check_sampled_error(tci, ref, pts, fx, 1e-9, margin=10.0)
 
 
 def test_batched_equals_alone(T):
