@@ -3,8 +3,8 @@
  * (libtci_gpu.so).
  *
  * Drop-in boundary for TensorCrossInterpolation.jl's TCI2 path: a Julia host
- * binds these entry points with ccall; Python tests bind
- * them with ctypes.  Conventions:
+ * binds these entry points with ccall; Python tests bind them with ctypes.
+ * Conventions:
  *   - multi-indices are 1-based local indices, as in the reference
  *     (MultiIndex = Vector{Int}, abstracttensortrain.jl:6-7), passed as
  *     row-major int64 arrays (one multi-index per row);
@@ -273,26 +273,37 @@ int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t*
                      int64_t* npivots, double* errors);
 
 /* rrlu on caller-owned device buffers, with no allocation by the library.
- * No counterpart in the reference: it serves callers that cannot let a
- * library allocate device memory -- code running while a stream is captured
- * into a CUDA graph, latency-critical loops where cudaMalloc/cudaFree would
- * stall the device, hosts whose every device buffer comes from their own
- * allocator.  Same arithmetic and outputs as tci_rrlu, but all pointers are
- * device pointers: A_dev (m x n column-major, read only); rowperm_dev (m) and
+ * No counterpart in the reference.  It serves callers that cannot let a
+ * library allocate device memory: hosts whose every device buffer comes from
+ * their own allocator (a Julia GPU array pool, a framework's arena), where a
+ * library's cudaMalloc would go around their accounting or fail against their
+ * reservation, and latency-critical loops where a cudaMalloc/cudaFree would
+ * synchronise the device.  Same arithmetic as tci_rrlu (bit-identical
+ * permutations, npivot, error and factors), but all pointers are device
+ * pointers: A_dev (m x n column-major, read only); rowperm_dev (m) and
  * colperm_dev (n) receive the full 0-based permutations, npivot_dev and
- * error_dev one value each, factors_dev (m x n, optional, may be NULL) the
- * factored matrix (L below the diagonal, U on and above, unit diagonal
- * implied on the side leftorthogonal selects).  Work goes to `stream`.
+ * error_dev one value each, status_dev 0 or TCI_ERR_NAN when L or U holds a
+ * NaN (where tci_rrlu returns TCI_ERR_NAN: the reference's ErrorException
+ * "lu.L contains NaNs", matrixlu.jl:164-169), factors_dev (m x n, optional,
+ * may be NULL) the factored matrix (L below the diagonal, U on and above,
+ * unit diagonal implied on the side leftorthogonal selects).  Work goes to
+ * `stream`; the call returns after enqueueing, so the outputs, status_dev
+ * included, are valid once the stream has reached them.
  * Limits: 1 <= m, n <= 16384 and m*n <= 524288 (larger sizes return
  * TCI_ERR_ARG).  The working storage is one fixed device array of the library
  * (about 8.6 MB on every GPU that loads it, kept until the process exits),
  * shared by all calls: calls that overlap on the GPU race on it, calls on one
- * stream are ordered.  The first call on a device looks up that array's
+ * stream are ordered.  Every element a call reads from that array is written
+ * earlier in the same call.  The first call on a device looks up that array's
  * device address and sets the kernel's shared-memory limit with the device
- * current; make it before any stream capture.  Returns after enqueueing. */
+ * current; make it before any stream capture.  The address is kept per device
+ * for the life of the process: a device reset after the first call is not
+ * supported.  A CUDA error already pending on the calling thread makes the
+ * call return TCI_ERR_CUDA without launching and without clearing it. */
 int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank, double reltol,
                      double abstol, int32_t leftorthogonal, int32_t* rowperm_dev, int32_t* colperm_dev,
-                     int32_t* npivot_dev, double* error_dev, double* factors_dev, uintptr_t stream);
+                     int32_t* npivot_dev, double* error_dev, int32_t* status_dev, double* factors_dev,
+                     uintptr_t stream);
 
 /* ---- context utilities --------------------------------------------------- */
 /* cudaStream_t of the context, as an integer. */

@@ -193,7 +193,7 @@ _SIGNATURES = {
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                        ctypes.c_size_t]),
+                                        ctypes.c_void_p, ctypes.c_size_t]),
 }
 
 _lib = None

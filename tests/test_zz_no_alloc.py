@@ -1,13 +1,22 @@
 """tci_rrlu_noalloc: the rrLU entry point that allocates nothing.
 
-It exists for callers that cannot let the library allocate device memory (a
-stream being captured into a CUDA graph, allocation-free serving loops, hosts
-that own every device buffer).  The caller passes device buffers; the library
-works in its own fixed device array.  This test calls it through the C ABI on
-two matrices in a row -- the second larger than shared memory, so the fixed
-array is used as the working matrix -- and checks each result against the
-allocating entry point tci_rrlu on the same matrix.  This file is collected
-last on purpose.
+Some callers cannot let a library allocate device memory: a host whose every
+device buffer comes from its own allocator (a Julia GPU array pool, a
+framework's arena), where an allocation behind its back breaks its accounting
+or fails against its reservation, and latency-critical loops where a
+cudaMalloc/cudaFree would synchronise the device.  This entry point takes
+device buffers from the caller and works in one fixed device array of the
+library.  The tests call it through the C ABI and check it
+
+  - against the allocating entry point tci_rrlu, bit for bit, on two calls in a
+    row (the second larger than shared memory, so the fixed array holds the
+    working matrix) and at the two limit shapes (16384 x 32 and m*n = 2^19);
+  - against the CPU oracle directly on the reference's own rrLU test matrices
+    (test/test_matrixlu.jl), and on a matrix whose L holds a NaN, where the
+    status output must carry TCI_ERR_NAN (the reference's "lu.L contains NaNs",
+    matrixlu.jl:164-169).
+
+This file is collected last on purpose.
 """
 import ctypes
 
@@ -21,38 +30,62 @@ def _noalloc(T, torch, A, **kw):
     m, n = A.shape
     dev = torch.device("cuda:0")
     a = torch.from_numpy(np.asfortranarray(A).reshape(-1, order="F").copy()).to(dev)
-    rowp = torch.empty(m, dtype=torch.int32, device=dev)
-    colp = torch.empty(n, dtype=torch.int32, device=dev)
-    npiv = torch.empty(1, dtype=torch.int32, device=dev)
-    err = torch.empty(1, dtype=torch.float64, device=dev)
+    rowp = torch.full((m,), -1, dtype=torch.int32, device=dev)
+    colp = torch.full((n,), -1, dtype=torch.int32, device=dev)
+    npiv = torch.full((1,), -1, dtype=torch.int32, device=dev)
+    err = torch.full((1,), -1.0, dtype=torch.float64, device=dev)
+    status = torch.full((1,), -1, dtype=torch.int32, device=dev)
     fac = torch.empty(m * n, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
     rc = T.load_library().tci_rrlu_noalloc(
         ctypes.c_void_p(a.data_ptr()), m, n, int(kw.get("maxrank") or 0), kw.get("reltol", 1e-14),
         kw.get("abstol", 0.0), int(kw.get("leftorthogonal", True)), ctypes.c_void_p(rowp.data_ptr()),
         ctypes.c_void_p(colp.data_ptr()), ctypes.c_void_p(npiv.data_ptr()), ctypes.c_void_p(err.data_ptr()),
-        ctypes.c_void_p(fac.data_ptr()), stream)
+        ctypes.c_void_p(status.data_ptr()), ctypes.c_void_p(fac.data_ptr()), stream)
     assert rc == 0, T.load_library().tci_last_error()
     torch.cuda.synchronize(dev)
     F = fac.cpu().numpy().reshape((m, n), order="F")
-    return rowp.cpu().numpy(), colp.cpu().numpy(), int(npiv.item()), float(err.item()), F
+    return dict(rowperm=rowp.cpu().numpy(), colperm=colp.cpu().numpy(), npivot=int(npiv.item()),
+                error=float(err.item()), status=int(status.item()), F=F)
 
 
-def _check_against_allocating(T, torch, A, **kw):
-    rp, cp, K, err, F = _noalloc(T, torch, A, **kw)
-    ref = T.rrlu(A, **kw)
-    assert K == ref.npivot
-    assert np.array_equal(rp + 1, ref.rowpermutation)
-    assert np.array_equal(cp + 1, ref.colpermutation)
-    assert err == ref.error
+def _factors(r, leftorthogonal):
+    K = r["npivot"]
+    F = r["F"]
     L = np.tril(F[:, :K])
     U = np.triu(F[:K, :])
-    if kw.get("leftorthogonal", True):
+    if leftorthogonal:
         np.fill_diagonal(L, 1.0)
     else:
         np.fill_diagonal(U, 1.0)
-    assert np.allclose(L, ref.L, rtol=0, atol=0)
-    assert np.allclose(U, ref.U, rtol=0, atol=0)
+    return L, U
+
+
+def _check_against_allocating(T, torch, A, **kw):
+    r = _noalloc(T, torch, A, **kw)
+    ref = T.rrlu(A, **kw)
+    assert r["status"] == 0
+    assert r["npivot"] == ref.npivot
+    assert np.array_equal(r["rowperm"] + 1, ref.rowpermutation)
+    assert np.array_equal(r["colperm"] + 1, ref.colpermutation)
+    assert r["error"] == ref.error
+    L, U = _factors(r, kw.get("leftorthogonal", True))
+    assert np.array_equal(L, ref.L)
+    assert np.array_equal(U, ref.U)
+
+
+def _check_against_oracle(T, torch, oracle, A, **kw):
+    r = _noalloc(T, torch, A, **kw)
+    ref = oracle.rrlu(A, **kw)
+    assert r["status"] == 0
+    assert r["npivot"] == ref["npivot"]
+    assert np.array_equal(r["rowperm"], ref["rowpermutation"])
+    assert np.array_equal(r["colperm"], ref["colpermutation"])
+    assert r["error"] == ref["error"]
+    L, U = _factors(r, kw.get("leftorthogonal", True))
+    assert np.array_equal(L, ref["L"])
+    assert np.array_equal(U, ref["U"])
+    return r
 
 
 def test_noalloc_matches_allocating_entry_point(T):
@@ -67,8 +100,50 @@ def test_noalloc_matches_allocating_entry_point(T):
     _check_against_allocating(T, torch, A2, reltol=1e-10, maxrank=64, leftorthogonal=False)
 
 
+@pytest.mark.parametrize("shape", [(16384, 32), (512, 1024)])
+def test_noalloc_limit_shapes(T, shape):
+    """The largest accepted shapes: 16384 rows (64 KB of permutations beside the
+    matrix) and m*n = 2^19 exactly."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(shape[0])
+    m, n = shape
+    k = 20
+    A = rng.standard_normal((m, k)) @ rng.standard_normal((k, n)) + 1e-12 * rng.standard_normal((m, n))
+    _check_against_allocating(T, torch, A, reltol=1e-10, maxrank=24)
+
+
+def test_noalloc_reference_matrices_against_oracle(T, oracle, golden):
+    """The reference's own rrLU test matrices (test/test_matrixlu.jl), through the
+    entry point and through the oracle: identical permutations, pivots, errors
+    and factors."""
+    torch = pytest.importorskip("torch")
+    for case in golden["rrlu"]:
+        A = np.array(case["A"], dtype=np.float64)
+        kw = dict(case["kwargs"])
+        _check_against_oracle(T, torch, oracle, A, **kw)
+        _check_against_oracle(T, torch, oracle, A, leftorthogonal=False, **kw)
+
+
+def test_noalloc_reports_nan(T, oracle):
+    """A NaN that reaches L: the oracle raises the reference's "lu.L contains
+    NaNs" and the entry point's status output holds TCI_ERR_NAN."""
+    torch = pytest.importorskip("torch")
+    A = np.ones((3, 3))
+    A[1, 0] = np.nan
+    with pytest.raises(oracle.OracleError):
+        oracle.rrlu(A)
+    r = _noalloc(T, torch, A)
+    assert r["status"] == T.TCI_ERR_NAN
+    with pytest.raises(T.TCIError, match="NaN"):
+        T.rrlu(A)
+    # the next call on a clean matrix reports success again
+    _check_against_allocating(T, torch, np.arange(1.0, 13.0).reshape(3, 4) ** 2)
+
+
 def test_noalloc_rejects_oversize(T):
     L = T.load_library()
-    rc = L.tci_rrlu_noalloc(None, 20000, 10, 0, 1e-14, 0.0, 1, None, None, None, None, None, 0)
+    rc = L.tci_rrlu_noalloc(None, 20000, 10, 0, 1e-14, 0.0, 1, None, None, None, None, None, None, 0)
     assert rc == T.TCI_ERR_ARG
     assert b"16384" in L.tci_last_error()
+    rc = L.tci_rrlu_noalloc(None, 1024, 1024, 0, 1e-14, 0.0, 1, None, None, None, None, None, None, 0)
+    assert rc == T.TCI_ERR_ARG
