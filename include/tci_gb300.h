@@ -53,6 +53,13 @@ enum {
   TCI_F_PRODUCT = 6  /* "product": C prod_n t[n, v_n] (integrate)  params [L, D, C, log|t|, t<0] */
 };
 
+/* Precision of evaluation, site contractions and matrix products: FP64 (the
+ * fixed-order kernels, bitwise equal to the oracle) or TF32x3 -- each FP64
+ * operand split into TF32 hi + lo, hi*hi + hi*lo + lo*hi on the tensor cores
+ * with FP32 accumulation (about 2^-21 relative error per product term;
+ * operands must lie in the FP32 range). */
+enum { TCI_PREC_FP64 = 0, TCI_PREC_TF32X3 = 1 };
+
 /* Sweep strategies (sweepstrategies.jl:1-6). */
 enum { TCI_SWEEP_BACKANDFORTH = 0, TCI_SWEEP_FORWARD = 1, TCI_SWEEP_BACKWARD = 2 };
 
@@ -202,6 +209,14 @@ int64_t tci_solve_nfeval(const tci_solve* s);
 int tci_evaluate(tci_solve* s, const int64_t* points, int64_t np, double* out);
 /* sum(tt) (abstracttensortrain.jl:191-199), FP64. */
 int tci_sum(tci_solve* s, double* out);
+/* evaluate(tt, indexset) in a precision (TCI_PREC_FP64 = tci_evaluate, or
+ * TCI_PREC_TF32X3: the row vectors of 128-point tiles stay on chip as TF32
+ * hi/lo and every site is a split-precision tensor-core product with FP32
+ * accumulation; bonds up to 128).  *err_est (may be NULL): the largest
+ * |split - fp64| / max |fp64| over the first min(np, 256) points, whose FP64
+ * values are computed alongside. */
+int tci_evaluate_prec(tci_solve* s, const int64_t* points, int64_t np, double* out, int32_t precision,
+                      double* err_est);
 
 /* optfirstpivot(f, localdims, firstpivot; maxsweep) (util.jl:78-108): coordinate
  * ascent of |f| from `pivot` (1-based, L entries, updated in place); each sweep
@@ -327,6 +342,10 @@ typedef struct tci_stats {
   /* elements of feval computed from tables of the factored f parts (one FP64
    * operation each) rather than by evaluating f */
   int64_t feval_tabulated;
+  /* split-precision tensor-core work: device milliseconds of its kernels
+   * (CUDA events; operand packing included) and the product FLOPs they did,
+   * counted as 2 M N K per split product (each one is 3 tensor-core products) */
+  double tc_ms, tc_flops;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
 
@@ -336,6 +355,9 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
 int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, const int64_t* points,
                     int64_t np, double* out);
 int tci_tt_sum(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, double* out);
+/* tci_tt_evaluate in a precision, as tci_evaluate_prec. */
+int tci_tt_evaluate_prec(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores,
+                         const int64_t* points, int64_t np, double* out, int32_t precision, double* err_est);
 
 /* ---- incremental server: requests are submitted one at a time while the
  * context serves them with continuous batching (host threads + the resident
@@ -394,6 +416,20 @@ int tci_tt4_contract_tci(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const d
                          const int64_t* b_dims, const double* const* b_cores, const int64_t* initialpivots,
                          int64_t np, int32_t ninitialpivots, tci_value_fn f, void* user, const tci_opts* opts,
                          tci_tt4** out);
+/* tci_tt4_contract with a precision: TCI_PREC_TF32X3 (algorithm = :zipup)
+ * runs both site contractions of contract_zipup (contraction.jl:458-469) as
+ * split-precision tensor-core products; the rank-revealing factorizations stay
+ * FP64.  *err_est (may be NULL) receives the largest relative error of any of
+ * those products against FP64, measured at sampled entries
+ * (max |C - C_fp64| / max |C_fp64|). */
+int tci_tt4_contract_prec(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
+                          const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, int32_t method,
+                          double tolerance, int64_t maxbonddim, int32_t precision, double* err_est, tci_tt4** out);
+/* C = A * B for host column-major A (M x K), B (K x N), C (M x N) -- the
+ * Matrix product of contraction.jl:92 -- in the given precision; *err_est as
+ * above (0 for FP64). */
+int tci_matmul(tci_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+               int32_t precision, double* err_est);
 int32_t tci_tt4_length(const tci_tt4* t);
 int tci_tt4_dims(const tci_tt4* t, int64_t* dims);
 int tci_tt4_get_core(const tci_tt4* t, int32_t b, double* out); /* b is 1-based */

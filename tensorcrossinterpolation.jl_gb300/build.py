@@ -29,9 +29,10 @@ CU_SOURCES = {
     "peak.cu": [],
     "gather.cu": [],
     "fcache.cu": [],
+    "tc_gemm.cu": [],
 }
 CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp", "contract_tci.cpp", "pivotsearch.cpp"]
-HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h"]
+HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h", "tc_gemm.h"]
 
 
 def _newer(target, deps):

@@ -18,6 +18,7 @@
 #include "contract.h"
 #include "contract_tci.h"
 #include "engine.h"
+#include "tc_gemm.h"
 
 using namespace tci;
 
@@ -233,6 +234,8 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.host_resume_ms += s.host_resume_ms;
     t.task_cycles += s.task_cycles;
     t.feval_tabulated += s.feval_tabulated;
+    t.tc_ms += s.tc_ms;
+    t.tc_flops += s.tc_flops;
     if (reset) e->stats = tci_stats{};
   }
   if (ctx->rq) {
@@ -592,6 +595,104 @@ int tci_sum(tci_solve* s, double* out) {
   std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
   CoTask t = co_sum(s->ctx->eng_ref(), s->s, out);
   return run_solve(s->ctx, s->s, t);
+}
+
+namespace {
+
+// evaluate() of the train held in s.cores at np points (packed 0-based local
+// indices) with TF32 hi/lo split products on the tensor cores
+// (tci_tc_evaluate_split); the first min(np, 256) points are also evaluated in
+// FP64 and *err_est = max |split - fp64| / max |fp64| over them.
+int split_evaluate(tci_ctx* ctx, Solve& s, const std::vector<uint8_t>& pts, int64_t np, double* out, double* err_est) {
+  const int L = s.L;
+  std::vector<int64_t> dims((size_t)(3 * L));
+  std::vector<const double*> cores((size_t)L);
+  for (int b = 0; b < L; ++b) {
+    const Core& c = s.cores[(size_t)b];
+    if (!c.p) return fail(TCI_ERR_GENERIC, "site tensors are not available (call fillsitetensors first)");
+    dims[3 * b] = c.d0;
+    dims[3 * b + 1] = c.d1;
+    dims[3 * b + 2] = c.d2;
+    cores[(size_t)b] = c.p;
+  }
+  if (L > 64 || !tci_tc_eval_supported(L, dims.data()))
+    return fail(TCI_ERR_ARG, "split-precision evaluation needs bonds <= 128, at most 64 sites and "
+                             "d * roundup(bond, 16) <= 512 per site");
+  if (ctx->rq) {  // plain launches: the tensor-core kernel needs the SMs
+    int rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  Engine& e = ctx->eng_ref();
+  int dev = 0, nsm = 148;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int ns = (int)std::min<int64_t>(np, 256);
+  const size_t ws = tci_tc_eval_workspace(L, dims.data());
+  double* dpts = e.alloc_core(std::max<size_t>(((size_t)np * L + 7) / 8, 1));
+  double* dout = e.alloc_core(std::max<size_t>((size_t)np + (size_t)ns + 1, 1));
+  double* dws = e.alloc_core(ws / 8 + 1);
+  int rc = 0;
+  if (!dpts || !dout || !dws) rc = fail(TCI_ERR_OOM, "device memory for split-precision evaluation");
+  int* derr = (int*)(dout + np + ns);
+  std::vector<double> samp((size_t)ns);
+  int herr = 0;
+  auto ck = [&](cudaError_t ce) {
+    if (!rc && ce != cudaSuccess) rc = fail(TCI_ERR_CUDA, cudaGetErrorString(ce));
+  };
+  if (!rc && np > 0) ck(cudaMemcpyAsync(dpts, pts.data(), (size_t)np * L, cudaMemcpyHostToDevice, e.stream()));
+  if (!rc) ck(cudaMemsetAsync(derr, 0, sizeof(int), e.stream()));
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  if (!rc) ck(cudaEventCreate(&ev0));
+  if (!rc) ck(cudaEventCreate(&ev1));
+  if (!rc) ck(cudaEventRecord(ev0, e.stream()));
+  if (!rc)
+    ck(tci_tc_evaluate_split(L, dims.data(), cores.data(), (const uint8_t*)dpts, np, dout, ns, dout + np, dws, derr,
+                             nsm, e.stream()));
+  if (!rc) ck(cudaEventRecord(ev1, e.stream()));
+  if (!rc && np > 0) ck(cudaMemcpyAsync(out, dout, (size_t)np * 8, cudaMemcpyDeviceToHost, e.stream()));
+  if (!rc && ns > 0) ck(cudaMemcpyAsync(samp.data(), dout + np, (size_t)ns * 8, cudaMemcpyDeviceToHost, e.stream()));
+  if (!rc) ck(cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, e.stream()));
+  if (!rc) ck(cudaStreamSynchronize(e.stream()));
+  if (!rc && herr) rc = fail(TCI_ERR_TIMEOUT, "tensor-core evaluation: a bounded wait ran out (code " +
+                                                  std::to_string(herr) + ")");
+  if (!rc) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) e.stats.tc_ms += ms;
+    // per point and site b >= 1: d_b products of (1 x r_{b-1}) (r_{b-1} x r_b)
+    double fl = 0.0;
+    for (int b = 1; b < L; ++b) fl += 2.0 * (double)dims[3 * b + 1] * (double)dims[3 * b] * (double)dims[3 * b + 2];
+    e.stats.tc_flops += fl * (double)np;
+  }
+  if (ev0) cudaEventDestroy(ev0);
+  if (ev1) cudaEventDestroy(ev1);
+  if (!rc && err_est) {
+    double dmax = 0, vmax = 0;
+    for (int k = 0; k < ns; ++k) {
+      dmax = std::max(dmax, std::fabs(out[k] - samp[(size_t)k]));
+      vmax = std::max(vmax, std::fabs(samp[(size_t)k]));
+    }
+    *err_est = vmax > 0 ? dmax / vmax : dmax;
+  }
+  if (dpts) e.free_core(dpts);
+  if (dout) e.free_core(dout);
+  if (dws) e.free_core(dws);
+  return rc;
+}
+
+}  // namespace
+
+int tci_evaluate_prec(tci_solve* s, const int64_t* points, int64_t np, double* out, int32_t precision,
+                      double* err_est) {
+  if (precision == TCI_PREC_FP64) {
+    if (err_est) *err_est = 0.0;
+    return tci_evaluate(s, points, np, out);
+  }
+  if (precision != TCI_PREC_TF32X3) return fail(TCI_ERR_ARG, "unknown precision");
+  std::lock_guard<std::recursive_mutex> lk(s->ctx->mu);
+  std::vector<uint8_t> pts;
+  int rc = pack_points(points, np, s->s.L, s->s.d, pts);
+  if (rc) return rc;
+  return split_evaluate(s->ctx, s->s, pts, np, out, err_est);
 }
 
 // ---------------------------------------------------------------- batches / serving
@@ -1247,6 +1348,78 @@ int tci_tt4_contract(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const doubl
   return 0;
 }
 
+int tci_tt4_contract_prec(tci_ctx* ctx, int32_t L, const int64_t* a_dims, const double* const* a_cores,
+                          const int64_t* b_dims, const double* const* b_cores, int32_t algorithm, int32_t method,
+                          double tolerance, int64_t maxbonddim, int32_t precision, double* err_est, tci_tt4** out) {
+  if (precision == TCI_PREC_FP64) {
+    if (err_est) *err_est = 0.0;
+    return tci_tt4_contract(ctx, L, a_dims, a_cores, b_dims, b_cores, algorithm, method, tolerance, maxbonddim, out);
+  }
+  *out = nullptr;
+  if (precision != TCI_PREC_TF32X3) return fail(TCI_ERR_ARG, "unknown precision");
+  if (algorithm != TCI_CONTRACT_ZIPUP) return fail(TCI_ERR_ARG, "split precision is implemented for algorithm = :zipup");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (method != TCI_FACTORIZE_LU && method != TCI_FACTORIZE_CI) return fail(TCI_ERR_GENERIC, "Not implemented yet.");
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  if (ctx->rq) {  // plain launches: the tensor-core kernels need the SMs
+    int rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  Engine& e = ctx->eng_ref();
+  TT4 a, b;
+  int rc = upload_tt4(e, L, a_dims, a_cores, a);
+  if (!rc) rc = upload_tt4(e, L, b_dims, b_cores, b);
+  if (!rc) rc = tt4_check_pair(a, b, true);
+  std::unique_ptr<tci_tt4> res(new tci_tt4());
+  res->ctx = ctx;
+  SplitRun split;
+  if (!rc) rc = tt4_contract_zipup(e, a, b, tolerance, maxbonddim, res->tt, method == TCI_FACTORIZE_CI, &split);
+  a.release(e);
+  b.release(e);
+  if (rc) {
+    res->tt.release(e);
+    return rc;
+  }
+  if (err_est) *err_est = split.max_rel_err;
+  *out = res.release();
+  return 0;
+}
+
+int tci_matmul(tci_ctx* ctx, int64_t M, int64_t N, int64_t K, const double* A, const double* B, double* C,
+               int32_t precision, double* err_est) {
+  if (M < 0 || N < 0 || K < 0) return fail(TCI_ERR_ARG, "negative matrix dimension");
+  if (precision != TCI_PREC_FP64 && precision != TCI_PREC_TF32X3) return fail(TCI_ERR_ARG, "unknown precision");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (err_est) *err_est = 0.0;
+  if (M == 0 || N == 0) return 0;
+  if (ctx->rq) {
+    int rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  Engine& e = ctx->eng_ref();
+  const size_t na = (size_t)(M * K), nb = (size_t)(K * N), nc = (size_t)(M * N);
+  double* dA = e.alloc_core(std::max<size_t>(na, 1));
+  double* dB = e.alloc_core(std::max<size_t>(nb, 1));
+  double* dC = e.alloc_core(nc);
+  int rc = 0;
+  if (!dA || !dB || !dC) rc = fail(TCI_ERR_OOM, "device memory for the matrix product");
+  if (!rc && na && cudaMemcpyAsync(dA, A, na * 8, cudaMemcpyHostToDevice, e.stream()) != cudaSuccess)
+    rc = fail(TCI_ERR_CUDA, "copy of A");
+  if (!rc && nb && cudaMemcpyAsync(dB, B, nb * 8, cudaMemcpyHostToDevice, e.stream()) != cudaSuccess)
+    rc = fail(TCI_ERR_CUDA, "copy of B");
+  if (!rc && K == 0 && cudaMemsetAsync(dC, 0, nc * 8, e.stream()) != cudaSuccess) rc = fail(TCI_ERR_CUDA, "memset");
+  SplitRun split;
+  if (!rc && K > 0) rc = device_matmul(e, dA, dB, dC, M, N, K, precision == TCI_PREC_TF32X3 ? &split : nullptr);
+  if (!rc && cudaMemcpyAsync(C, dC, nc * 8, cudaMemcpyDeviceToHost, e.stream()) != cudaSuccess)
+    rc = fail(TCI_ERR_CUDA, "copy of C");
+  if (!rc && cudaStreamSynchronize(e.stream()) != cudaSuccess) rc = fail(TCI_ERR_CUDA, "synchronize");
+  if (!rc && err_est) *err_est = split.max_rel_err;
+  e.free_core(dA);
+  e.free_core(dB);
+  e.free_core(dC);
+  return rc;
+}
+
 int tci_tt4_compress(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores, int32_t method,
                      double tolerance, int64_t maxbonddim, int32_t normalizeerror, tci_tt4** out) {
   *out = nullptr;
@@ -1409,6 +1582,26 @@ int tci_tt_evaluate(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* 
       rc = e.run(t);
     }
   }
+  e.release_cores(s);
+  return rc;
+}
+
+int tci_tt_evaluate_prec(tci_ctx* ctx, int32_t L, const int64_t* dims, const double* const* cores,
+                         const int64_t* points, int64_t np, double* out, int32_t precision, double* err_est) {
+  if (precision == TCI_PREC_FP64) {
+    if (err_est) *err_est = 0.0;
+    return tci_tt_evaluate(ctx, L, dims, cores, points, np, out);
+  }
+  if (precision != TCI_PREC_TF32X3) return fail(TCI_ERR_ARG, "unknown precision");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (L < 1) return fail(TCI_ERR_ARG, "empty tensor train");
+  Engine& e = ctx->eng_ref();
+  Solve s;
+  int rc = upload_tt3(e, L, dims, cores, s);
+  if (rc) return rc;
+  std::vector<uint8_t> pts;
+  rc = pack_points(points, np, L, s.d, pts);
+  if (!rc) rc = split_evaluate(ctx, s, pts, np, out, err_est);
   e.release_cores(s);
   return rc;
 }

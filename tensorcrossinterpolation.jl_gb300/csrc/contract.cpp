@@ -8,7 +8,10 @@
 
 #include <algorithm>
 #include <climits>
+#include <cstring>
 #include <string>
+
+#include "tc_gemm.h"
 
 cudaError_t tci_naive_site_launch(const double* a, const double* b, double* out, int ra, int s1, int s2, int ra2,
                                   int rb, int s3, int rb2, cudaStream_t st);
@@ -55,7 +58,64 @@ struct Buf {
   }
 };
 
+// One split-precision product on the engine stream, then its FP64 error at
+// split->samples hashed entries (waits for the stream).
+int split_product(Engine& e, SplitRun* split, int64_t M, int64_t N, int64_t K, const double* A, tci_map3 a_row,
+                  tci_map3 a_k, int a_kfast, const double* B, tci_map3 b_row, tci_map3 b_k, int b_kfast, double* C,
+                  tci_map3 c_row, tci_map3 c_col) {
+  if (M == 0 || N == 0) return 0;
+  const size_t ws = tci_tc_gemm_workspace(M, N, K);
+  Buf W(e, ws / sizeof(double) + 1), S(e, 4);
+  if (!W.p || !S.p) return fail(TCI_ERR_OOM, "device memory for the split-precision product");
+  CT_TRY(cudaMemsetAsync(S.p, 0, 4 * sizeof(double), e.stream()));
+  int* err = (int*)(S.p + 2);
+  cudaEvent_t ev[2];
+  CT_TRY(cudaEventCreate(&ev[0]));
+  CT_TRY(cudaEventCreate(&ev[1]));
+  struct EvGuard {
+    cudaEvent_t* ev;
+    ~EvGuard() {
+      cudaEventDestroy(ev[0]);
+      cudaEventDestroy(ev[1]);
+    }
+  } evg{ev};
+  CT_TRY(cudaEventRecord(ev[0], e.stream()));
+  CT_TRY(tci_tc_gemm_split(M, N, K, A, a_row, a_k, a_kfast, B, b_row, b_k, b_kfast, C, c_row, c_col, W.p, err,
+                           e.stream()));
+  CT_TRY(cudaEventRecord(ev[1], e.stream()));
+  CT_TRY(tci_tc_gemm_sample_error(M, N, K, A, a_row, a_k, B, b_row, b_k, C, c_row, c_col, split->samples,
+                                  0x5eedULL + (uint64_t)split->products, (unsigned long long*)S.p, e.stream()));
+  double h[4];
+  CT_TRY(cudaMemcpyAsync(h, S.p, sizeof(h), cudaMemcpyDeviceToHost, e.stream()));
+  CT_TRY(cudaStreamSynchronize(e.stream()));
+  int code;
+  std::memcpy(&code, &h[2], sizeof(int));
+  if (code) return fail(TCI_ERR_TIMEOUT, "tensor-core product: a bounded wait ran out (code " + std::to_string(code) + ")");
+  const double rel = h[1] > 0 ? h[0] / h[1] : h[0];
+  split->max_rel_err = std::max(split->max_rel_err, rel);
+  split->products += 1;
+  split->flops += 2.0 * (double)M * (double)N * (double)K;
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, ev[0], ev[1]) == cudaSuccess) e.stats.tc_ms += ms;
+  e.stats.tc_flops += 2.0 * (double)M * (double)N * (double)K;
+  return 0;
+}
+
 }  // namespace
+
+int device_matmul(Engine& e, const double* A, const double* B, double* C, int64_t M, int64_t N, int64_t K,
+                  SplitRun* split) {
+  if (M == 0 || N == 0) return 0;
+  if (!split) {
+    if (!fits_int(M) || !fits_int(N) || !fits_int(K)) return fail(TCI_ERR_TOO_LARGE, "matrix too large");
+    CT_TRY(tci_gemm_launch(A, M, B, K, C, M, (int)M, (int)N, (int)K, e.stream()));
+    CT_TRY(cudaStreamSynchronize(e.stream()));
+    return 0;
+  }
+  // C[m, n] = sum_k A[m + M k] * B[k + K n]: A rows unit stride, B "rows" (n) stride K
+  return split_product(e, split, M, N, K, A, tci_map_stride(1), tci_map_stride(M), M == 1, B, tci_map_stride(K),
+                       tci_map_stride(1), 1, C, tci_map_stride(1), tci_map_stride(M));
+}
 
 void TT4::release(Engine& e) {
   for (auto& c : cores) {
@@ -153,7 +213,7 @@ int tt4_contract_naive(Engine& e, const TT4& a, const TT4& b, TT4& out) {
 
 // contract_zipup(A, B; tolerance, method=:LU, maxbonddim) (contraction.jl:442-486).
 int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, int64_t maxbonddim, TT4& out,
-                       bool ci) {
+                       bool ci, SplitRun* split) {
   out.cores.clear();
   const size_t L = a.cores.size();
   // R: (link_ab, link_an, link_bn), starts as ones(1, 1, 1)
@@ -174,9 +234,27 @@ int tt4_contract_zipup(Engine& e, const TT4& a, const TT4& b, double tolerance, 
       out.release(e);
       return fail(TCI_ERR_OOM, "device memory for the zipup blocks");
     }
-    CT_TRY(tci_zip_ra_launch(R.p, A.p, RA.p, (int)nab, (int)rna, (int)rnb, (int)s, (int)sp, (int)an2, e.stream()));
-    CT_TRY(tci_zip_c_launch(RA.p, B.p, C.p, (int)nab, (int)rnb, (int)s, (int)sp, (int)an2, (int)spp, (int)bn2,
-                            e.stream()));
+    if (!split) {
+      CT_TRY(tci_zip_ra_launch(R.p, A.p, RA.p, (int)nab, (int)rna, (int)rnb, (int)s, (int)sp, (int)an2, e.stream()));
+      CT_TRY(tci_zip_c_launch(RA.p, B.p, C.p, (int)nab, (int)rnb, (int)s, (int)sp, (int)an2, (int)spp, (int)bn2,
+                              e.stream()));
+    } else {
+      // RA[ab, bn, (s, s', an')] = sum_an R[ab, an, bn] A[an, (s, s', an')]: rows (ab, bn)
+      int rc = split_product(e, split, nab * rnb, s * sp * an2, rna, R.p, tci_map_2(nab, 1, nab * rna),
+                             tci_map_stride(nab), nab == 1, A.p, tci_map_stride(rna), tci_map_stride(1), 1, RA.p,
+                             tci_map_stride(1), tci_map_stride(nab * rnb));
+      // C[ab, s, s'', an', bn'] = sum_(bn, s') RA[ab, bn, s, s', an'] B[bn, s', s'', bn']:
+      // rows (ab, s, an'), contracted (bn, s'), columns (s'', bn')
+      if (!rc)
+        rc = split_product(e, split, nab * s * an2, spp * bn2, rnb * sp, RA.p,
+                           tci_map_3(nab, s, 1, nab * rnb, nab * rnb * s * sp), tci_map_2(rnb, nab, nab * rnb * s),
+                           nab == 1, B.p, tci_map_stride(rnb * sp), tci_map_stride(1), 1, C.p,
+                           tci_map_3(nab, s, 1, nab, nab * s * spp), tci_map_2(spp, nab * s, nab * s * spp * an2));
+      if (rc) {
+        out.release(e);
+        return rc;
+      }
+    }
     Tensor4 core;
     core.d[0] = nab;
     core.d[1] = s;

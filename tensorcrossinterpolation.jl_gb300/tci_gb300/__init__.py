@@ -30,6 +30,8 @@ VALUE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int64, F64P)
 TCI_OK, TCI_ERR_ARG, TCI_ERR_DIM, TCI_ERR_NAN, TCI_ERR_SINGULAR, TCI_ERR_GENERIC = 0, 1, 2, 3, 4, 5
 TCI_ERR_CUDA, TCI_ERR_OOM, TCI_ERR_TIMEOUT, TCI_ERR_TOO_LARGE = 6, 7, 8, 9
 TCI_CONTRACT_NAIVE, TCI_CONTRACT_ZIPUP = 1, 2
+# precision of contractions and matrix products: FP64, or TF32 hi/lo split products on the tensor cores
+PRECISION = {"fp64": 0, "tf32x3": 1}
 FACTORIZE = {"LU": 0, "CI": 1}  # _factorize methods on the device (tensortrain.jl:94-137)
 SWEEP = {"backandforth": 0, "forward": 1, "backward": 2}
 FUNCTIONS = {"lorentz": 1, "served": 2, "qtt1d": 3, "qtt2d": 4, "dense": 5, "product": 6}
@@ -99,6 +101,8 @@ class Stats(ctypes.Structure):
         ("host_resume_ms", ctypes.c_double),
         ("task_cycles", ctypes.c_int64),
         ("feval_tabulated", ctypes.c_int64),
+        ("tc_ms", ctypes.c_double),
+        ("tc_flops", ctypes.c_double),
     ]
 
 
@@ -138,6 +142,7 @@ _SIGNATURES = {
     "tci_get_history": (ctypes.c_int, [ctypes.c_void_p, I64P, F64P, I64P, I64P]),
     "tci_solve_nfeval": (ctypes.c_int64, [ctypes.c_void_p]),
     "tci_evaluate": (ctypes.c_int, [ctypes.c_void_p, I64P, ctypes.c_int64, F64P]),
+    "tci_evaluate_prec": (ctypes.c_int, [ctypes.c_void_p, I64P, ctypes.c_int64, F64P, ctypes.c_int32, F64P]),
     "tci_sum": (ctypes.c_int, [ctypes.c_void_p, F64P]),
     "tci_crossinterpolate2_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(Request),
                                                      ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
@@ -160,6 +165,11 @@ _SIGNATURES = {
     "tci_tt4_contract": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
                                         ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
                                         ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_tt4_contract_prec": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
+                                             ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                             ctypes.c_int64, ctypes.c_int32, F64P, ctypes.POINTER(ctypes.c_void_p)]),
+    "tci_matmul": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, F64P, F64P, F64P,
+                                  ctypes.c_int32, F64P]),
     "tci_tt4_compress": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, ctypes.c_int32,
                                         ctypes.c_double, ctypes.c_int64, ctypes.c_int32,
                                         ctypes.POINTER(ctypes.c_void_p)]),
@@ -188,6 +198,8 @@ _SIGNATURES = {
     "tci_tt_evaluate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P, ctypes.c_int64,
                                        F64P]),
     "tci_tt_sum": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, F64P]),
+    "tci_tt_evaluate_prec": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, I64P, ctypes.c_void_p, I64P,
+                                            ctypes.c_int64, F64P, ctypes.c_int32, F64P]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -579,13 +591,20 @@ class TensorCI2:
         return r, e, g
 
     # ---- tensor train
-    def evaluate(self, points):
-        """evaluate(tci, indexset) for one point or an array of points (1-based)."""
+    def evaluate(self, points, precision="fp64"):
+        """evaluate(tci, indexset) for one point or an array of points (1-based).
+        precision "tf32x3": split-precision tensor-core evaluation; its error
+        against FP64 (sampled) is left in self.eval_err_est."""
+        if precision not in PRECISION:
+            raise ArgumentError(TCI_ERR_ARG, f"Unknown precision {precision}.")
         pts = np.asarray(points, dtype=np.int64)
         single = pts.ndim == 1
         pts = np.ascontiguousarray(pts.reshape(-1, len(self)))
         out = np.zeros(pts.shape[0])
-        _check(load_library().tci_evaluate(self.h, _p(pts, I64P), pts.shape[0], _p(out, F64P)))
+        err = np.zeros(1)
+        _check(load_library().tci_evaluate_prec(self.h, _p(pts, I64P), pts.shape[0], _p(out, F64P),
+                                                PRECISION[precision], _p(err, F64P)))
+        self.eval_err_est = float(err[0])
         return float(out[0]) if single else out
 
     __call__ = evaluate
@@ -644,16 +663,23 @@ class TensorTrain:
         dims = np.ascontiguousarray([list(c.shape) for c in cores], dtype=np.int64).reshape(-1)
         return cores, dims, (ctypes.c_void_p * len(cores))(*[c.ctypes.data for c in cores])
 
-    def evaluate(self, points, ctx=None):
-        """evaluate(tt, indexset) (abstracttensortrain.jl:124-162) on the device, 1-based."""
+    def evaluate(self, points, ctx=None, precision="fp64"):
+        """evaluate(tt, indexset) (abstracttensortrain.jl:124-162) on the device, 1-based.
+        precision "tf32x3": split-precision tensor-core evaluation; its error
+        against FP64 (sampled) is left in self.eval_err_est."""
+        if precision not in PRECISION:
+            raise ArgumentError(TCI_ERR_ARG, f"Unknown precision {precision}.")
         ctx = ctx or default_context()
         cores, dims, ptrs = self._args()
         pts = np.asarray(points, dtype=np.int64)
         single = pts.ndim == 1
         pts = np.ascontiguousarray(pts.reshape(-1, len(cores)))
         out = np.zeros(pts.shape[0])
-        _check(load_library().tci_tt_evaluate(ctx.h, len(cores), _p(dims, I64P), ptrs, _p(pts, I64P), pts.shape[0],
-                                              _p(out, F64P)))
+        err = np.zeros(1)
+        _check(load_library().tci_tt_evaluate_prec(ctx.h, len(cores), _p(dims, I64P), ptrs, _p(pts, I64P),
+                                                   pts.shape[0], _p(out, F64P), PRECISION[precision],
+                                                   _p(err, F64P)))
+        self.eval_err_est = float(err[0])
         return float(out[0]) if single else out
 
     def sum(self, ctx=None):
@@ -718,7 +744,7 @@ def _value_callback(f):
 
 
 def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU", ctx=None, f=None,
-             initialpivots=10, **kwargs):
+             initialpivots=10, precision="fp64", **kwargs):
     """contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) of
     tensor trains with 4-leg cores (A's third leg against B's second), or of a
     3-leg train with a 4-leg one.  algorithm "TCI" (the default: crossinterpolate2
@@ -726,8 +752,12 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     `initialpivots` a count of random starts or a list of fused 1-based
     pivots, and crossinterpolate2 keywords in kwargs), "naive" or "zipup";
     factorizations use the rank-revealing LU (method "LU") or MatrixLUCI over it
-    (method "CI") -- the reference's SVD is not on the device.  Returns a
-    TensorTrain."""
+    (method "CI") -- the reference's SVD is not on the device.  precision
+    "tf32x3" (zipup) runs the site contractions as TF32 hi/lo split products on
+    the tensor cores; the result's `err_est` is the largest relative error of
+    those products against FP64 at sampled entries.  Returns a TensorTrain."""
+    if precision not in PRECISION:
+        raise ArgumentError(TCI_ERR_ARG, f"Unknown precision {precision}.")
     if f is not None and algorithm != "TCI":
         raise TCIError(TCI_ERR_GENERIC, f"{algorithm.capitalize()} contraction implementation cannot contract "
                        "matrix product with a function. Use algorithm=:TCI instead.")
@@ -746,13 +776,40 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     a, ad, ap = _tt4_args(a)
     b, bd, bp = _tt4_args(b)
     h = ctypes.c_void_p()
-    _check(load_library().tci_tt4_contract(ctx.h, len(a), _p(ad, I64P), ap, _p(bd, I64P), bp, alg,
-                                           FACTORIZE[method], float(tolerance), int(maxbonddim or 0),
-                                           ctypes.byref(h)))
+    err = np.zeros(1)
+    _check(load_library().tci_tt4_contract_prec(ctx.h, len(a), _p(ad, I64P), ap, _p(bd, I64P), bp, alg,
+                                                FACTORIZE[method], float(tolerance), int(maxbonddim or 0),
+                                                PRECISION[precision], _p(err, F64P), ctypes.byref(h)))
     cores = _tt4_fetch(h)
     if a3 or b3:  # TensorTrain{3}(tt, prod.(sitedims(tt)))
         cores = [c.reshape((c.shape[0], c.shape[1] * c.shape[2], c.shape[3]), order="F") for c in cores]
-    return TensorTrain(cores)
+    tt = TensorTrain(cores)
+    tt.err_est = float(err[0])
+    return tt
+
+
+def matmul(A, B, precision="fp64", ctx=None):
+    """A * B of FP64 matrices on the device (the product of contraction.jl:92):
+    "fp64" is the fixed-order FP64 kernel, "tf32x3" the TF32 hi/lo split product
+    on the tensor cores.  Returns (C, err_est): err_est is the relative error of
+    the split product against FP64 at sampled entries (0 for "fp64")."""
+    if precision not in PRECISION:
+        raise ArgumentError(TCI_ERR_ARG, f"Unknown precision {precision}.")
+    A = np.asfortranarray(A, dtype=np.float64)
+    B = np.asfortranarray(B, dtype=np.float64)
+    if A.ndim != 2 or B.ndim != 2 or A.shape[1] != B.shape[0]:
+        raise DimensionMismatch(TCI_ERR_DIM, f"matrix A has dimensions {A.shape}, matrix B has dimensions {B.shape}")
+    ctx = ctx or default_context()
+    M, K = A.shape
+    N = B.shape[1]
+    a = np.ascontiguousarray(A.reshape(-1, order="F"))
+    b = np.ascontiguousarray(B.reshape(-1, order="F"))
+    c = np.zeros(max(M * N, 1))
+    err = np.zeros(1)
+    _check(load_library().tci_matmul(ctx.h, M, N, K, _p(a, F64P) if a.size else None,
+                                     _p(b, F64P) if b.size else None, _p(c, F64P), PRECISION[precision],
+                                     _p(err, F64P)))
+    return c[: M * N].reshape((M, N), order="F"), float(err[0])
 
 
 def _contract_tci(A, B, tolerance, maxbonddim, f, initialpivots, ctx, kwargs):
