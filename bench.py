@@ -42,11 +42,52 @@ METRIC = "TCI solves/sec and p50/p99 latency, served+batched vs plain GPU at err
 UNIT = "solves/s"
 
 
-def make_requests(n, seed):
+def make_requests(n, seed, tol_range=(-10.0, -6.0)):
     """Served-stream family requests (L, d, params, tol, maxbonddim)."""
     from tci_gb300 import workloads
 
-    return workloads.served_requests(n, seed)
+    return workloads.served_requests(n, seed, tol_range=tol_range)
+
+
+def step_seed(step, rank):
+    """Seed of the request list of bench step `step` on replica `rank`; both arms
+    draw their requests from it."""
+    return 1000 * step + rank
+
+
+def oracle_solve(reqs, cores):
+    """crossinterpolate2 of every request (initial pivot all ones) by the oracle
+    on `cores` host threads; returns (wall seconds, ranks)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ctypes
+
+    import oracle as O
+
+    lib = O.lib()
+    n = len(reqs)
+    Ls = np.array([r[0] for r in reqs], np.int32)
+    dims = np.concatenate([[r[1]] * r[0] for r in reqs]).astype(np.int64)
+    doff = np.concatenate([[0], np.cumsum(Ls)[:-1]]).astype(np.int64)
+    fids = np.full(n, O.F_SERVED, np.int32)
+    prm = np.concatenate([r[2] for r in reqs]).astype(np.float64)
+    np_ = np.array([len(r[2]) for r in reqs], np.int64)
+    poff = np.concatenate([[0], np.cumsum(np_)[:-1]]).astype(np.int64)
+    tol = np.array([r[3] for r in reqs])
+    mbd = np.array([r[4] for r in reqs], np.int64)
+    o = O.make_opts()
+    rank = np.zeros(n, np.int64)
+    secs = np.zeros(n)
+    I32P = ctypes.POINTER(ctypes.c_int32)
+    t0 = time.perf_counter()
+    rc = lib.orc_solve_batch(n, Ls.ctypes.data_as(I32P), dims.ctypes.data_as(O.I64P),
+                             doff.ctypes.data_as(O.I64P), fids.ctypes.data_as(I32P), prm.ctypes.data_as(O.F64P),
+                             poff.ctypes.data_as(O.I64P), np_.ctypes.data_as(O.I64P), tol.ctypes.data_as(O.F64P),
+                             mbd.ctypes.data_as(O.I64P), ctypes.byref(o), rank.ctypes.data_as(O.I64P),
+                             secs.ctypes.data_as(O.F64P), int(cores))
+    dt = time.perf_counter() - t0
+    if rc:
+        raise RuntimeError(f"oracle solve failed with code {rc}")
+    return dt, rank
 
 
 # FP64 operations per registered-function evaluation of the served family,
@@ -106,45 +147,76 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(reqs, seconds=20.0):
-    """The oracle solving requests on all host cores until ~`seconds` of work."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import ctypes
+def cpu_baseline(reqs, n=6000, what="the bench stream"):
+    """The oracle solving the first n requests in one batch on all host cores
+    (threads take the next request as they finish, so no thread idles on a
+    chunk's slowest solve)."""
+    cores = os.cpu_count() or 1
+    sub = reqs[:n]
+    dt, _ = oracle_solve(sub, cores)
+    return {"value": len(sub) / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the first {len(sub)} requests of {what}, crossinterpolate2 by the C++ "
+                      f"oracle on {cores} threads in one batch, {dt:.1f} s"}
 
+
+def parity_sample(T, res, reqs, nsample=200, npts=10000, seed=123):
+    """Checks a sample of the timed solves against the oracle: `nsample` requests
+    spread over the whole size range (every k-th by the HBM estimate
+    L d^2 maxbonddim^2), each solved again by the oracle on the host threads.
+    Per solve: pivot index sets identical, site tensors identical, and the max
+    error |f - tt| on `npts` seeded lattice points against the request's
+    tolerance (relative to maxsamplevalue)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
-    lib = O.lib()
-    cores = os.cpu_count() or 1
-    done = 0
+    order = sorted(range(len(reqs)), key=lambda i: reqs[i][0] * reqs[i][1] ** 2 * reqs[i][4] ** 2)
+    pick = sorted({order[int(k)] for k in np.linspace(0, len(order) - 1, nsample)})
+
+    def solve(i):
+        L, d, prm, tol, mbd = reqs[i]
+        ref, _, _ = O.crossinterpolate2([d] * L, O.F_SERVED, prm, None, tolerance=tol, maxbonddim=mbd)
+        return ref
+
     t0 = time.perf_counter()
-    chunk = max(cores * 2, 8)
-    i = 0
-    while time.perf_counter() - t0 < seconds and i < len(reqs):
-        sub = reqs[i:i + chunk]
-        i += len(sub)
-        n = len(sub)
-        Ls = np.array([r[0] for r in sub], np.int32)
-        dims = np.concatenate([[r[1]] * r[0] for r in sub]).astype(np.int64)
-        doff = np.concatenate([[0], np.cumsum(Ls)[:-1]]).astype(np.int64)
-        fids = np.full(n, O.F_SERVED, np.int32)
-        prm = np.concatenate([r[2] for r in sub]).astype(np.float64)
-        np_ = np.array([len(r[2]) for r in sub], np.int64)
-        poff = np.concatenate([[0], np.cumsum(np_)[:-1]]).astype(np.int64)
-        tol = np.array([r[3] for r in sub])
-        mbd = np.array([r[4] for r in sub], np.int64)
-        o = O.make_opts()
-        rank = np.zeros(n, np.int64)
-        secs = np.zeros(n)
-        I32P = ctypes.POINTER(ctypes.c_int32)
-        lib.orc_solve_batch(n, Ls.ctypes.data_as(I32P), dims.ctypes.data_as(O.I64P), doff.ctypes.data_as(O.I64P),
-                            fids.ctypes.data_as(I32P), prm.ctypes.data_as(O.F64P), poff.ctypes.data_as(O.I64P),
-                            np_.ctypes.data_as(O.I64P), tol.ctypes.data_as(O.F64P), mbd.ctypes.data_as(O.I64P),
-                            ctypes.byref(o), rank.ctypes.data_as(O.I64P), secs.ctypes.data_as(O.F64P), cores)
-        done += n
-    dt = time.perf_counter() - t0
-    return {"value": done / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done} served-family requests from the bench stream, crossinterpolate2 by the C++ "
-                      f"oracle on {cores} threads, {dt:.1f} s"}
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        refs = list(ex.map(solve, pick))
+    rng = np.random.default_rng(seed)
+    same_piv = same_cores = within_tol = within_10tol = within_2x_oracle = 0
+    uncapped = unc_tol = unc_10tol = 0
+    worst = worst_unc = 0.0
+    for i, ref in zip(pick, refs):
+        L, d, prm, tol, mbd = reqs[i]
+        tci = res[i]
+        sp = all(np.array_equal(tci.sets(b)[0], ref.sets(b)[0]) and np.array_equal(tci.sets(b)[1], ref.sets(b)[1])
+                 for b in range(1, L + 1))
+        sc = sp and all(np.array_equal(tci.sitetensor(b), ref.core(b)) for b in range(1, L + 1))
+        same_piv += sp
+        same_cores += sc
+        pts = rng.integers(1, d + 1, size=(npts, L))
+        fx = O.feval(O.F_SERVED, prm, pts)
+        err = float(np.max(np.abs(tci.evaluate(pts) - fx)))
+        err_ref = err if sc else float(np.max(np.abs(ref.evaluate(pts) - fx)))
+        ratio = err / (tol * tci.maxsamplevalue)
+        worst = max(worst, ratio)
+        within_tol += ratio <= 1.0
+        within_10tol += ratio <= 10.0
+        within_2x_oracle += err <= 2 * err_ref + 1e-300
+        if tci.rank() < mbd:  # the rank cap did not bind: the tolerance decides the error
+            uncapped += 1
+            unc_tol += ratio <= 1.0
+            unc_10tol += ratio <= 10.0
+            worst_unc = max(worst_unc, ratio)
+    return {"solves_checked": len(pick), "of_timed": len(reqs), "points_per_solve": npts,
+            "pivots_identical": int(same_piv), "site_tensors_identical": int(same_cores),
+            "mismatches": int(len(pick) - same_piv),
+            "sampled_err_within_tol": int(within_tol), "sampled_err_within_10tol": int(within_10tol),
+            "sampled_err_within_2x_oracle": int(within_2x_oracle), "max_err_over_tol": worst,
+            "below_rank_cap": int(uncapped), "below_rank_cap_within_tol": int(unc_tol),
+            "below_rank_cap_within_10tol": int(unc_10tol), "below_rank_cap_max_err_over_tol": worst_unc,
+            "oracle_s": time.perf_counter() - t0,
+            "selection": "every k-th of the last timed step's requests ordered by L d^2 maxbonddim^2"}
 
 
 def dist_setup(world):
@@ -267,8 +339,15 @@ def single_solve_configs(T, ctx, with_cpu=True):
     pts = np.random.default_rng(2024).integers(1, 3, size=(1000000, 40))
     te, vals = _best_of(lambda: tci.evaluate(pts), reps=2)
     ts, sm = _best_of(lambda: tci.sum(), reps=2)
+    ctx.stats(reset=True)
+    tse, vs = _best_of(lambda: tci.evaluate(pts, precision="tf32x3"), reps=2)
+    st = ctx.stats(reset=True)
     c = {"gpu_s": t, "rank": int(tci.rank()), "eval_points": 1000000, "gpu_eval_s": te,
-         "gpu_eval_points_per_s": 1e6 / te, "gpu_sum_s": ts}
+         "gpu_eval_points_per_s": 1e6 / te, "gpu_sum_s": ts,
+         "split_eval": {"precision": "tf32x3 (TF32 hi/lo, 3 tensor-core products, FP32 accumulation)",
+                        "e2e_s": tse, "points_per_s": 1e6 / tse, "kernel_ms": st["tc_ms"] / 2,
+                        "max_rel_err_vs_fp64": float(np.abs(vs - vals).max() / np.abs(vals).max()),
+                        "err_est_reported": tci.eval_err_est}}
     if O:
         tc, (ref, rr, _) = _best_of(lambda: O.crossinterpolate2([2] * 40, O.F_QTT1D, [0], None, **kw))
         sample = pts[:100000]
@@ -290,7 +369,23 @@ def single_solve_configs(T, ctx, with_cpu=True):
     op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 8.0 for i in range(30)]
     tz, res = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, ctx=ctx),
                        reps=1)
-    c.update(zipup_gpu_s=tz, zipup_rank=int(res.rank()))
+    ctx.stats(reset=True)
+    tzs, res_s = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, ctx=ctx,
+                                              precision="tf32x3"), reps=1)
+    st = ctx.stats(reset=True)
+    pts = rng.integers(1, 5, size=(20, 30))
+    exact = np.array([_exact_mpo_mps(op, mps.sitetensors, p) for p in pts])
+    scale = np.abs(exact).max()
+    tc_tflops = st["tc_flops"] / (st["tc_ms"] * 1e-3) / 1e12 if st["tc_ms"] > 0 else None
+    c.update(zipup_gpu_s=tz, zipup_rank=int(res.rank()),
+             zipup_rel_err_20pts=float(np.abs(res.evaluate(pts, ctx=ctx) - exact).max() / scale),
+             zipup_split={"precision": "tf32x3: both site contractions per site on the tensor cores, "
+                                       "rrLU factorizations in FP64",
+                          "gpu_s": tzs, "rank": int(res_s.rank()),
+                          "rel_err_20pts": float(np.abs(res_s.evaluate(pts, ctx=ctx) - exact).max() / scale),
+                          "products_err_est": res_s.err_est,
+                          "tensor_kernel_ms": st["tc_ms"], "product_tflops": tc_tflops,
+                          "tensor_pipe_tflops": 3 * tc_tflops if tc_tflops else None})
     out["quantics2d_30"] = c
     return out
 
@@ -371,24 +466,42 @@ def rrlu_batch_bench(T, ctx, peak_sep, with_cpu=True, reps=3):
     return out
 
 
+def bench_config(args):
+    """The `config` object of both arms' JSON lines."""
+    return {"workload": f"served-stream family: {args.batch} crossinterpolate2 requests per step "
+                        "(L 4..16, d 2..16, tol 1e-10..1e-6, maxbonddim 32..256), continuous batching "
+                        f"with up to {args.live} live solves",
+            "max_live": args.live, "global_batch": args.batch, "parallelism": f"replicas{args.gpus}",
+            "requests": "step s draws its list from seed 1000*s + rank",
+            "l2": "inputs are per-step index lists; Pi matrices stay on chip"}
+
+
 def run_reference(args):
+    """The reference's CPU path (the oracle port: Julia is absent) on the same
+    seeded request lists as the GPU arm's steps: each step solves the first
+    --ref-sample requests of that step's list on all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    reqs = make_requests(4096, seed=7)
-    per_step = []
+    cores = os.cpu_count() or 1
+    sample = min(args.ref_sample, args.batch)
+    step_s = []
     for s in range(args.warmup + args.steps):
-        r = cpu_baseline(reqs[(s * 64) % 2048:], seconds=max(2.0, 30.0 / max(args.steps, 1)))
+        reqs = make_requests(args.batch, seed=step_seed(s, 0))
+        n = 64 if s < args.warmup else sample  # warm-up steps: a short prefix
+        dt, _ = oracle_solve(reqs[:n], cores)
         if s >= args.warmup:
-            per_step.append(r["value"])
-    v = float(np.mean(per_step))
+            step_s.append(dt)
+    total = sum(step_s)
+    v = sample * args.steps / total
+    desc = (f"the first {sample} of each timed step's {args.batch} requests (the GPU arm's seeded lists), "
+            f"crossinterpolate2 by the C++ restatement of the reference on {cores} host threads")
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "served-stream family batch (L 4..16, d 2..16, tol 1e-10..1e-6, "
-                                   "maxbonddim 32..256)", "solver": "C++ restatement of the reference, all host cores"},
+            "warmup": args.warmup, "ms_per_step": total * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": bench_config(args),
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": r["cores"], "kind": "port", "sample": r["sample"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -401,12 +514,16 @@ def main():
     ap.add_argument("--batch", type=int, default=10000)
     ap.add_argument("--live", type=int, default=1024)
     ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--ref-sample", type=int, default=2000,
+                    help="requests of each step's list that the reference arm solves")
+    ap.add_argument("--no-parity", action="store_true", help="skip the parity sample of the timed solves")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
     ap.add_argument("--no-sweep", action="store_true", help="skip the latency sweep over arrival rates")
     ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU; "
-                    "'contract-tci': only contract(algorithm=:TCI) of the 2-D quantics configuration")
+                    "'contract-tci': only contract(algorithm=:TCI) of the 2-D quantics configuration; "
+                    "'single': only the single-solve configurations")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -426,9 +543,12 @@ def main():
     if args.only == "contract-tci":  # contract(algorithm=:TCI) of the 2-D quantics configuration alone
         print(json.dumps(contract_tci_bench(T, ctx)))
         return
+    if args.only == "single":  # the single-solve configurations alone
+        print(json.dumps(single_solve_configs(T, ctx, with_cpu=not args.no_cpu)))
+        return
 
-    def specs_for(step):
-        reqs = make_requests(args.batch, seed=1000 * step + rank)
+    def specs_for(step, tol_range=(-10.0, -6.0)):
+        reqs = make_requests(args.batch, seed=step_seed(step, rank), tol_range=tol_range)
         return reqs, [(T.DeviceFunction("served", r[2]), [r[1]] * r[0],
                        dict(tolerance=r[3], maxbonddim=r[4])) for r in reqs]
 
@@ -480,6 +600,7 @@ def main():
         ranks = [tt.rank() for tt in tts]
         e2e_s.append(time.perf_counter() - t0)
         nsolves += len(res)
+        last_reqs, last_res = reqs, res
         del res
     if tstream is not None:
         torch.cuda.synchronize()
@@ -500,6 +621,29 @@ def main():
     kern_s = kernel_ms / 1e3 if kernel_ms > 0 else total_dev_s
     achieved = ops / kern_s / 1e12 if kern_s > 0 else 0.0
     peak = peak_sep / 1e12
+
+    # a seeded sample of the last timed step's solves against the oracle
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = parity_sample(T, last_res, last_reqs)
+    del last_res
+
+    # the same family at tolerances 1e-10 .. 1e-8 only (the metric's error bar)
+    _, specs_t = specs_for(7777, tol_range=(-10.0, -8.0))
+    if tstream is not None:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(tstream)
+    t0 = time.perf_counter()
+    T.crossinterpolate2_batched(specs_t, max_live=args.live, ctx=ctx)
+    tight_s = time.perf_counter() - t0
+    if tstream is not None:
+        e1.record(tstream)
+        e1.synchronize()
+        tight_s = e0.elapsed_time(e1) / 1e3
+    tight = {"workload": f"{len(specs_t)} requests of the served family with tolerance log-uniform in "
+                         "[1e-10, 1e-8]", "solves_per_s_device": len(specs_t) / tight_s}
+    ctx.stats(reset=True)
 
     # plain one-at-a-time GPU path on a subset
     reqs, specs = specs_for(9999)
@@ -532,7 +676,8 @@ def main():
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(make_requests(4096, seed=31), seconds=20.0)
+        cpu = cpu_baseline(make_requests(args.batch, seed=step_seed(args.warmup, 0)),
+                           what="the first timed step's list")
     rrlu_line = None if args.no_rrlu else rrlu_batch_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
     single = None if args.no_single else single_solve_configs(T, ctx, with_cpu=not args.no_cpu)
     large = None if args.no_rrlu else large_rrlu_bench(T, ctx, peak_sep, with_cpu=not args.no_cpu)
@@ -541,12 +686,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": (total_dev_s * 1e3) / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"served-stream family: {args.batch} crossinterpolate2 requests per step "
-                               "(L 4..16, d 2..16, tol 1e-10..1e-6, maxbonddim 32..256), continuous batching "
-                               f"with up to {args.live} live solves",
-                   "max_live": args.live,
-                   "global_batch": args.batch, "parallelism": f"replicas{args.gpus}",
-                   "l2": "inputs are per-step index lists; Pi matrices stay on chip"},
+        "config": bench_config(args),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": st["h2d_bytes"] // max(args.steps, 1),
                 "d2h_bytes_per_step": st["d2h_bytes"] // max(args.steps, 1)},
         "gpu_launches": st["launches"],
@@ -555,6 +695,8 @@ def main():
         "serve_p50_ms": float(np.percentile(lat, 50) * 1e3), "serve_p99_ms": float(np.percentile(lat, 99) * 1e3),
         "serve_rate_per_s": lam,
         "serve_sweep": sweep,
+        "tight_tolerance": tight,
+        "parity_sample": parity,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": None,
                      "peak_source": "measured FP64 mul+sub throughput (tci_fp64_peak), this run",

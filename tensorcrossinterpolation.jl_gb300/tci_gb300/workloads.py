@@ -5,11 +5,12 @@ No dataset is involved anywhere: every input is generated here from a seed.
 import numpy as np
 
 
-def served_requests(n, seed):
+def served_requests(n, seed, tol_range=(-10.0, -6.0)):
     """Requests of the served-stream family: f(v) = 1/(1 + a v.v) + b exp(-g |v - c|^2)
     with a, b, g log-uniform in [1e-2, 1e1], c uniform on the lattice; L uniform in
-    4..16, d uniform in 2..16, tolerance log-uniform in [1e-10, 1e-6], maxbonddim
-    uniform in {32, 64, 128, 256}.  Returns (L, d, params, tolerance, maxbonddim)."""
+    4..16, d uniform in 2..16, tolerance log-uniform in [1e-10, 1e-6] (log10 bounds
+    `tol_range`), maxbonddim uniform in {32, 64, 128, 256}.  Returns (L, d, params,
+    tolerance, maxbonddim)."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(n):
@@ -17,7 +18,7 @@ def served_requests(n, seed):
         d = int(rng.integers(2, 17))
         a, b, g = 10 ** rng.uniform(-2, 1, size=3)
         c = rng.integers(1, d + 1, size=L)
-        tol = float(10 ** rng.uniform(-10, -6))
+        tol = float(10 ** rng.uniform(*tol_range))
         mbd = int(rng.choice([32, 64, 128, 256]))
         out.append((L, d, [a, b, g] + [float(x) for x in c], tol, mbd))
     return out
