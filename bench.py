@@ -415,6 +415,41 @@ def contract_tci_bench(T, ctx, maxbonddim=128):
             "max_rel_err_20_points": float(np.abs(got - exact).max() / np.abs(exact).max())}
 
 
+def tc_gemm_bench(T, ctx, M=16384, N=2048, K=1024, reps=3):
+    """The split-precision tensor-core product alone on a large shape: C = A B
+    with A (M x K), B (K x N) N(0, 1) (seed 5).  Device time of operand packing
+    + tcgen05 GEMM from CUDA events (stats tc_ms), host copies excluded."""
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((K, N))
+    T.matmul(A[:256], B, precision="tf32x3", ctx=ctx)  # warm-up
+    ctx.stats(reset=True)
+    C = None
+    for _ in range(reps):
+        C, err = T.matmul(A, B, precision="tf32x3", ctx=ctx)
+    st = ctx.stats(reset=True)
+    ms = st["tc_ms"] / reps
+    useful = 2.0 * M * N * K
+    sub = slice(0, 512)
+    rel = float((np.abs(C[sub] - A[sub] @ B) / (np.abs(A[sub]) @ np.abs(B))).max())
+    meas = _measured_peaks()
+    tf32_peak = meas.get("bf16_tflops", 1900.0) / 2 if meas else 950.0
+    tensor = 3 * useful / (ms * 1e-3) / 1e12
+    return {"workload": f"C = A B, A {M}x{K}, B {K}x{N}, FP64 in/out, TF32 hi/lo split (3 tensor-core products)",
+            "kernel_ms": ms, "product_tflops": useful / (ms * 1e-3) / 1e12, "tensor_pipe_tflops": tensor,
+            "tf32_peak_tflops": tf32_peak, "tensor_frac": tensor / tf32_peak,
+            "tf32_peak_source": "half the measured bf16 dense peak (TF32 runs at half the BF16 rate)",
+            "max_err_over_sum_abs": rel, "err_est": err}
+
+
+def _measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
 def _exact_mpo_mps(op, mps, p):
     """(op * mps)[p] by a left-to-right environment sweep on the host (1-based p)."""
     import numpy as np
@@ -523,7 +558,7 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the latency sweep over arrival rates")
     ap.add_argument("--only", default="", help="'rrlu': only the batched-rrLU configuration; 'big-rrlu': only the multi-CTA rrLU; "
                     "'contract-tci': only contract(algorithm=:TCI) of the 2-D quantics configuration; "
-                    "'single': only the single-solve configurations")
+                    "'single': only the single-solve configurations; 'tc-gemm': only the tensor-core product")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -542,6 +577,9 @@ def main():
         return
     if args.only == "contract-tci":  # contract(algorithm=:TCI) of the 2-D quantics configuration alone
         print(json.dumps(contract_tci_bench(T, ctx)))
+        return
+    if args.only == "tc-gemm":  # the split-precision tensor-core product alone
+        print(json.dumps(tc_gemm_bench(T, ctx)))
         return
     if args.only == "single":  # the single-solve configurations alone
         print(json.dumps(single_solve_configs(T, ctx, with_cpu=not args.no_cpu)))

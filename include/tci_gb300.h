@@ -346,8 +346,19 @@ typedef struct tci_stats {
    * (CUDA events; operand packing included) and the product FLOPs they did,
    * counted as 2 M N K per split product (each one is 3 tensor-core products) */
   double tc_ms, tc_flops;
+  /* most solves live at once in a batched or serving run (admission by the
+   * live cap and the HBM budget) */
+  int64_t peak_live;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
+/* Bounds of the resident kernel's waits (no reference counterpart): it leaves
+ * after idle_us with nothing published (default 20000; the host relaunches it
+ * on demand), and a worker CTA waits at most wait_us for its task ticket
+ * (default 60 s); a wait that runs out stops the kernel and the call in
+ * progress returns TCI_ERR_TIMEOUT.  Tasks of that call that were published
+ * but not run are abandoned: after TCI_ERR_TIMEOUT destroy the context.  Takes
+ * effect at the next launch of the kernel. */
+int tci_ctx_set_resident_limits(tci_ctx* ctx, int32_t idle_us, int64_t wait_us);
 
 /* evaluate / sum (abstracttensortrain.jl:124-199) of a tensor train the caller
  * gives: cores[b] is r0 x d x r1 column-major, dims[3*b + 0..2] its sizes;

@@ -40,6 +40,7 @@ struct tci_ctx {
   // destroy objects of the same context from inside it.  Entry points that
   // compute refuse to run there (Engine::run / run_tasks).
   std::recursive_mutex mu;
+  int64_t peak_live = 0;  // most solves live at once in a batched / serving drive (stats)
   Engine& eng_ref() { return *engp; }
 };
 
@@ -217,6 +218,16 @@ int tci_ctx_synchronize(tci_ctx* ctx) {
   return 0;
 }
 
+int tci_ctx_set_resident_limits(tci_ctx* ctx, int32_t idle_us, int64_t wait_us) {
+  if (idle_us < 100 || wait_us < 1) return fail(TCI_ERR_ARG, "idle_us must be >= 100 and wait_us >= 1");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (!ctx->rq) return 0;  // batched launches only: nothing waits
+  int rc = ctx->rq->stop();  // the next launch takes the new limits
+  ctx->rq->qc->idle_us = idle_us;
+  ctx->rq->wait_ns = (unsigned long long)wait_us * 1000ull;
+  return rc;
+}
+
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
   tci_stats t{};
   for (auto& e : ctx->pool) {
@@ -238,6 +249,8 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.tc_flops += s.tc_flops;
     if (reset) e->stats = tci_stats{};
   }
+  t.peak_live = ctx->peak_live;
+  if (reset) ctx->peak_live = 0;
   if (ctx->rq) {
     t.kernel_ms += ctx->rq->kernel_ms;
     t.launches += ctx->rq->launches;
@@ -809,6 +822,7 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
             jp = &jobs[order[sh.next++]];
             ++sh.live;
             sh.live_bytes += jp->est;
+            ctx->peak_live = std::max(ctx->peak_live, sh.live);
           }
         }
         if (!jp) break;

@@ -28,7 +28,7 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
                                 int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
                                 cudaStream_t stream);
 cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
-                                int grid, cudaStream_t stream);
+                                int grid, unsigned long long wait_ns, cudaStream_t stream);
 
 namespace tci {
 
@@ -716,7 +716,7 @@ int ResidentQueue::start() {
   if (running) return 0;
   std::atomic_ref<int32_t>(qc->stop).store(0, std::memory_order_release);
   CUDA_TRY(cudaEventRecord(ev0, stream));
-  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, stream));
+  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
   CUDA_TRY(cudaEventRecord(ev1, stream));
   running = true;
   ++launches;
@@ -729,12 +729,19 @@ int ResidentQueue::ensure_alive() {
   cudaError_t q = cudaEventQuery(ev1);
   if (q == cudaErrorNotReady) return 0;
   if (q != cudaSuccess) return fail(TCI_ERR_CUDA, cudaGetErrorString(q));
-  // every CTA has left on its idle limit: account the launch and start again
+  // every CTA has left: account the launch; if a wait ran out, report it
+  // instead of starting again, else (the idle limit) start again
   float ms = 0;
   cudaEventElapsedTime(&ms, ev0, ev1);
   kernel_ms += ms;
+  int32_t err = 0;
+  CUDA_TRY(cudaMemcpy(&err, &st_dev->error, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err) {
+    running = false;
+    return fail(TCI_ERR_TIMEOUT, "resident kernel: a wait for a task hit its limit");
+  }
   CUDA_TRY(cudaEventRecord(ev0, stream));
-  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, stream));
+  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
   CUDA_TRY(cudaEventRecord(ev1, stream));
   ++launches;
   return 0;

@@ -177,6 +177,7 @@ struct ResidentQueue {
   bool running = false;
   double kernel_ms = 0;
   int64_t launches = 0;
+  unsigned long long wait_ns = 60ull * 1000000000ull;  // a worker's longest wait for its ticket
   int init(int device, int num_sms, int idle_us);
   ~ResidentQueue();
   int start();        // launch the kernel unless it is running

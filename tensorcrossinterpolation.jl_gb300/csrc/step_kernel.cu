@@ -1552,18 +1552,18 @@ __device__ __forceinline__ void st_release_gpu_s32(int32_t* p, int v) {
 }
 
 constexpr int RES_MAX_PARAMS = 64;                          // params copied to shared memory
-constexpr uint64_t RES_WAIT_LIMIT_NS = 60ull * 1000000000ull;  // a worker's longest wait for a ticket
-constexpr long long RES_MAX_POLLS = 1LL << 31;              // and its poll count
+constexpr long long RES_MAX_POLLS = 1LL << 31;  // a worker's most polls of one ticket
 constexpr int TASK_WORDS = (int)(sizeof(tci_task) / 8);
 static_assert(sizeof(tci_task) % 8 == 0, "task record is a whole number of words");
 
 // Warp 0 of CTA 0: move published host-ring descriptors, 32 at a time, into
 // the device ring (in ticket order, while the device ring has room), mark the
 // host slots free, publish the device tickets.  Leaves -- and tells the
-// workers -- when the host asks to stop and nothing published is left, or
-// after qc->idle_us with nothing published.
+// workers -- when the host asks to stop and nothing published is left, after
+// qc->idle_us with nothing published, when a worker has reported a failed
+// wait, or after wait_ns without room in the device ring.
 __device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmask, tci_resident_state* st,
-                                  tci_queue_ctl* qc) {
+                                  tci_queue_ctl* qc, uint64_t wait_ns) {
   const int lane = threadIdx.x;
   unsigned long long pos = *(volatile unsigned long long*)&st->host_pos;
   unsigned long long k = 0;
@@ -1602,10 +1602,10 @@ __device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmas
     int leave = 0;
     if (lane == 0) {
       const uint64_t waited = global_ns() - t_idle;
-      if (!pub)  // nothing published: the host is done, or quiet for too long
-        leave = (*(volatile int32_t*)&qc->stop != 0) || waited > idle_ns;
+      if (!pub)  // nothing published: the host is done, quiet for too long, or a worker failed
+        leave = (*(volatile int32_t*)&qc->stop != 0) || waited > idle_ns || (*(volatile int32_t*)&st->error != 0);
       else       // published but no room: the workers must free slots; they may have failed
-        leave = (*(volatile int32_t*)&st->error != 0) || waited > RES_WAIT_LIMIT_NS;
+        leave = (*(volatile int32_t*)&st->error != 0) || waited > wait_ns;
     }
     if (__shfl_sync(FULL, leave, 0)) break;
     __nanosleep(sleep_ns);
@@ -1622,12 +1622,13 @@ __device__ void resident_dispatch(tci_queue_slot* __restrict__ hs, uint32_t hmas
 // CTA 0 hosts the dispatcher; every other CTA claims the next device ticket
 // with one atomic, waits until it is dispatched (or the dispatcher has left:
 // tickets past the last dispatched one are never used), runs the task and
-// publishes the result record to the host.
+// publishes the result record to the host.  A worker waits at most wait_ns for
+// its ticket; then it sets st->error and every CTA leaves.
 __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     tci_resident_kernel(tci_queue_slot* __restrict__ hslots, uint32_t hmask, tci_resident_state* st,
-                        tci_queue_ctl* qc, size_t smem_bytes) {
+                        tci_queue_ctl* qc, size_t smem_bytes, unsigned long long wait_ns) {
   if (blockIdx.x == 0) {
-    if (threadIdx.x < 32) resident_dispatch(hslots, hmask, st, qc);
+    if (threadIdx.x < 32) resident_dispatch(hslots, hmask, st, qc, wait_ns);
     return;
   }
   extern __shared__ __align__(16) char smem[];
@@ -1652,7 +1653,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
           if (ld_acquire_gpu(&d->seq) == t + 1) got = (long long)t;
           break;
         }
-        if (it >= RES_MAX_POLLS || global_ns() - t_begin > RES_WAIT_LIMIT_NS) {
+        if (it >= RES_MAX_POLLS || global_ns() - t_begin > wait_ns) {
           atomicExch(&st->error, 1);
           break;
         }
@@ -2163,12 +2164,12 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
 // (cooperative launch), after clearing the per-launch part of its state.
 // slots/qc are mapped pinned host memory, st device memory.
 cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
-                                int grid, cudaStream_t stream) {
+                                int grid, unsigned long long wait_ns, cudaStream_t stream) {
   const size_t off = offsetof(tci_resident_state, count);
   cudaError_t e = cudaMemsetAsync((char*)st + off, 0, sizeof(tci_resident_state) - off, stream);
   if (e != cudaSuccess) return e;
   size_t smem = tci_resident_smem_bytes();
-  void* args[] = {(void*)&slots, (void*)&mask, (void*)&st, (void*)&qc, (void*)&smem};
+  void* args[] = {(void*)&slots, (void*)&mask, (void*)&st, (void*)&qc, (void*)&smem, (void*)&wait_ns};
   return cudaLaunchCooperativeKernel((const void*)tci_resident_kernel, dim3(grid), dim3(NT), args, smem, stream);
 }
 

@@ -219,7 +219,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   uint64_t* bars = (uint64_t*)(base + STAGES * S::STAGE_BYTES);  // full[STAGES], empty[STAGES], done
   uint32_t* tmem_slot = (uint32_t*)(bars + 2 * STAGES + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  // N tiles run fastest: the CTAs that share an A tile run together and read it from L2
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * BM;
   constexpr int TMEM_COLS = BN <= 32 ? 32 : (BN <= 64 ? 64 : (BN <= 128 ? 128 : 256));
 
   if (threadIdx.x == 0) {
@@ -361,7 +362,8 @@ cudaError_t launch_bn(const CUtensorMap& ta, const CUtensorMap& tb, int M, int N
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  dim3 grid((unsigned)(Mp / BM), (unsigned)(Np / BN));
+  if (Mp / BM > 65535) return cudaErrorInvalidValue;
+  dim3 grid((unsigned)(Np / BN), (unsigned)(Mp / BM));
   tc_gemm_kernel<BN, STAGES><<<grid, TC_THREADS, S::TOTAL, st>>>(ta, tb, M, N, Mp, Np, kiters, C, crow, ccol, err);
   return cudaGetLastError();
 }

@@ -103,6 +103,7 @@ class Stats(ctypes.Structure):
         ("feval_tabulated", ctypes.c_int64),
         ("tc_ms", ctypes.c_double),
         ("tc_flops", ctypes.c_double),
+        ("peak_live", ctypes.c_int64),
     ]
 
 
@@ -202,6 +203,7 @@ _SIGNATURES = {
                                             ctypes.c_int64, F64P, ctypes.c_int32, F64P]),
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
+    "tci_ctx_set_resident_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -277,6 +279,11 @@ class Context:
 
     def synchronize(self):
         _check(load_library().tci_ctx_synchronize(self.h))
+
+    def set_resident_limits(self, idle_us=20000, wait_us=60_000_000):
+        """Bounds of the resident kernel's waits: it leaves after idle_us with
+        nothing to do, and a worker waits at most wait_us for its task."""
+        _check(load_library().tci_ctx_set_resident_limits(self.h, int(idle_us), int(wait_us)))
 
     def stats(self, reset=False):
         s = Stats()
