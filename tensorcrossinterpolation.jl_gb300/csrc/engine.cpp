@@ -21,9 +21,9 @@ cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* orde
                             int* counter_dev, int grid, cudaStream_t stream);
 cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
 size_t tci_resident_smem_bytes();
-size_t tci_rrlu_big_smem(int64_t m, int64_t n);
-bool tci_rrlu_big_fits(int64_t m, int64_t n);
-size_t tci_rrlu_big_scratch_bytes(int grid);
+size_t tci_rrlu_big_smem(int64_t m, int64_t n, int G);
+bool tci_rrlu_big_fits(int64_t m, int64_t n, int G);
+size_t tci_rrlu_big_scratch_bytes(int grid, int kmax);
 cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, char* res, void* scratch, int m,
                                 int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
                                 cudaStream_t stream);
@@ -1033,11 +1033,11 @@ static CoTask co_tasks(Engine& e, std::vector<Req*> reqs) {
 
 // A rank-revealing LU of a given matrix large enough to spread over every SM:
 // the multi-CTA kernel instead of one CTA working out of global memory.
-static bool big_eligible(const Req& r, bool resident) {
+static bool big_eligible(const Req& r, bool resident, int grid) {
   const tci_task& t = r.t;
   return !resident && t.kind == TCI_TASK_RRLU && (t.ain || r.ain_host) &&
          (t.post == TCI_POST_FACTORS || t.post == TCI_POST_NONE) && (int64_t)t.m * t.n >= ((int64_t)1 << 18) &&
-         tci_rrlu_big_fits(t.m, t.n);
+         tci_rrlu_big_fits(t.m, t.n, grid);
 }
 
 int Engine::run_big(Req& r) {
@@ -1045,7 +1045,7 @@ int Engine::run_big(Req& r) {
   const int64_t m = t.m, n = t.n;
   const int grid = num_sms * TCI_CTAS_PER_SM;
   const size_t rb = result_bytes(t);
-  const size_t scratch = tci_rrlu_big_scratch_bytes(grid);
+  const size_t scratch = tci_rrlu_big_scratch_bytes(grid, t.maxrank);
   // one device block: result record, scratch, input copy (if host), working matrix
   const size_t in_elems = r.ain_host ? (size_t)(m * n) : 0;
   const size_t fact_elems = t.post == TCI_POST_FACTORS ? 0 : (size_t)(m * n) + ((size_t)(m + n) * 4 + 7) / 8;
@@ -1093,7 +1093,7 @@ int Engine::run_big(Req& r) {
 
 int Engine::run_tasks(std::vector<Req*>& reqs) {
   if (fc_callback_depth()) return reentry();
-  if (reqs.size() == 1 && big_eligible(*reqs[0], resident())) return run_big(*reqs[0]);
+  if (reqs.size() == 1 && big_eligible(*reqs[0], resident(), num_sms * TCI_CTAS_PER_SM)) return run_big(*reqs[0]);
   CoTask t = co_tasks(*this, reqs);
   return run(t, false);
 }

@@ -23,6 +23,8 @@
 // (matrixlu.jl:16-31).  The comparison of v*v is skipped for elements whose |v|
 // is more than 16 ulps below the running maximum, where v*v is provably smaller.
 #include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
 #include <limits.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -53,6 +55,7 @@ struct Ctl {
   int red_k[NW + 1];
   unsigned long long red_u[NW + 1];
   unsigned long long red_b[NW + 1];
+  unsigned red_p[NW + 1];
   long long red4[4][NW + 1];
 };
 
@@ -1690,17 +1693,22 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
 }
 
 // ------------------------------------------------------------ multi-CTA rrLU
-// One rank-revealing LU spread over every SM (cooperative launch, one CTA per
-// SM) for matrices far larger than shared memory: CTA b owns the columns
-// j = b, b + G, ...  Columns are never moved: the column swaps of swapcol!
-// (matrixlu.jl:106-112) are tracked as a permutation (pos: column -> physical
-// position, stor: position -> column), and the argmax key of an element is
-// (physical column << 16) | row, so ties break exactly as in the physically
-// permuted matrix.  Rows are swapped physically inside each CTA's own columns.
-// Per pivot: decision (every CTA, identically), row swap + scaling in own
-// columns, grid barrier, rank-1 update of own trailing columns with the pivot
-// column read from L2, partial argmax, grid barrier, reduction of the partials
-// (every CTA, in the same order).  The arithmetic per element is the same
+// One rank-revealing LU spread over every SM (cooperative launch) for matrices
+// far larger than shared memory.  The CTAs form a Pr x Pc grid; CTA (p, q) owns
+// the row block p x column block q of the working matrix.  Nothing moves: the
+// row and column swaps of swaprow!/swapcol! (matrixlu.jl:98-112) are tracked as
+// permutations (pos: physical -> logical position, stor: logical -> physical),
+// and the argmax key of an element is (logical column << 16) | logical row, so
+// ties break exactly as in the physically permuted matrix.  The scaling of
+// addpivot! (matrixlu.jl:114-124) is applied where it is needed with the same
+// operands: the update of step k uses x_i = A[i, C] / piv (leftorthogonal) or
+// y_j = A[R, j] / piv, each CTA dividing the entries of its own rows / columns
+// (the pivot row R and column C are stable after the barrier: they leave the
+// trailing block), and the stored factors are divided the same way when they
+// are written out.  Per pivot: every CTA reduces the G partial argmaxes (same
+// result everywhere), takes the decision, forms its x and y slices, updates its
+// block of the trailing matrix fused with its partial argmax, and meets the
+// others at ONE grid barrier.  The arithmetic per element is the same
 // __dmul_rn/__dsub_rn/__ddiv_rn sequence as rrlu_loop, so the factors are
 // bit-identical.
 
@@ -1710,21 +1718,24 @@ struct BigBar {
 };
 struct BigPartial {
   unsigned long long A, B;
-  unsigned int k, nan;
-  double v;  // the element at key k (the next pivot's value)
+  unsigned int k, ph;  // key and physical position (row | column << 16) of the maximum
+  double v;            // the element at key k (the next pivot's value)
+  unsigned int nan, pad;
 };
 
-// ArgTrack that also carries the value at its key (push in any key order).
+// Running argmax of |v| with the value and physical position at its key (push
+// in any key order).
 struct BigTrack {
   uint64_t A, B;
-  uint32_t k;
+  uint32_t k, ph;
   double v;
   __device__ __forceinline__ void init() {
     A = B = 0;
     k = 0xffffffffu;
+    ph = 0;
     v = 0.0;
   }
-  __device__ __forceinline__ void push(double x, uint32_t key) {
+  __device__ __forceinline__ void push(double x, uint32_t key, uint32_t phys) {
     uint64_t b = abs_bits(x);
     if (b > NAN_FLOOR) return;
     b += 1;
@@ -1732,10 +1743,12 @@ struct BigTrack {
       B = A;
       A = b;
       k = key;
+      ph = phys;
       v = x;
     } else if (b == A) {
       if (key < k) {
         k = key;
+        ph = phys;
         v = x;
       }
     } else if (b > B) {
@@ -1743,17 +1756,19 @@ struct BigTrack {
     }
   }
 };
-__device__ __forceinline__ void big_combine(uint64_t& A, uint32_t& k, uint64_t& B, double& v, uint64_t A2,
-                                            uint32_t k2, uint64_t B2, double v2) {
+__device__ __forceinline__ void big_combine(uint64_t& A, uint32_t& k, uint32_t& ph, uint64_t& B, double& v,
+                                            uint64_t A2, uint32_t k2, uint32_t ph2, uint64_t B2, double v2) {
   if (A2 > A) {
     B = B2 > A ? B2 : A;
     A = A2;
     k = k2;
+    ph = ph2;
     v = v2;
   } else if (A2 == A) {
     B = B2 > B ? B2 : B;
     if (k2 < k) {
       k = k2;
+      ph = ph2;
       v = v2;
     }
   } else if (A2 > B) {
@@ -1788,7 +1803,7 @@ __device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, Ctl& c
           break;
         }
         __nanosleep(sleep_ns);
-        sleep_ns = sleep_ns < 256 ? sleep_ns * 2 : 256;
+        sleep_ns = sleep_ns < 128 ? sleep_ns * 2 : 128;
       }
     }
     gen = g + 1;
@@ -1798,24 +1813,27 @@ __device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, Ctl& c
   return ctl.bar_err == 0;
 }
 
-// The CTA's (A, k, B, v) of a BigTrack; lane 0 of warp 0 gets the result.
-__device__ void block_track(const BigTrack& t, Ctl& ctl, BigPartial* out) {
+// Block reduction of every thread's BigTrack; every thread gets the result.
+// Ends with a barrier.
+__device__ void block_track(BigTrack& t, Ctl& ctl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t a = t.A, b = t.B;
-  uint32_t kk = t.k;
+  uint32_t kk = t.k, ph = t.ph;
   double v = t.v;
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
     const uint64_t a2 = __shfl_down_sync(FULL, a, off);
     const uint64_t b2 = __shfl_down_sync(FULL, b, off);
     const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
     const double v2 = __shfl_down_sync(FULL, v, off);
-    big_combine(a, kk, b, v, a2, k2, b2, v2);
+    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
   }
   if (lane == 0) {
     ctl.red_u[warp] = a;
     ctl.red_b[warp] = b;
     ctl.red_k[warp] = (int)kk;
+    ctl.red_p[warp] = ph;
     ctl.red_s[warp] = v;
   }
   __syncthreads();
@@ -1823,64 +1841,44 @@ __device__ void block_track(const BigTrack& t, Ctl& ctl, BigPartial* out) {
     a = lane < NW ? ctl.red_u[lane] : 0ULL;
     b = lane < NW ? ctl.red_b[lane] : 0ULL;
     kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+    ph = lane < NW ? ctl.red_p[lane] : 0u;
     v = lane < NW ? ctl.red_s[lane] : 0.0;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const uint64_t a2 = __shfl_down_sync(FULL, a, off);
       const uint64_t b2 = __shfl_down_sync(FULL, b, off);
       const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+      const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
       const double v2 = __shfl_down_sync(FULL, v, off);
-      big_combine(a, kk, b, v, a2, k2, b2, v2);
+      big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
     }
     if (lane == 0) {
-      out->A = a;
-      out->B = b;
-      out->k = kk;
-      out->v = v;
+      ctl.red_u[NW] = a;
+      ctl.red_b[NW] = b;
+      ctl.red_k[NW] = (int)kk;
+      ctl.red_p[NW] = ph;
+      ctl.red_s[NW] = v;
     }
   }
   __syncthreads();
-}
-
-// Warp 0 reduces the G partials (same order in every CTA); lane 0 gets it.
-__device__ void big_reduce(const BigPartial* parts, int G, uint64_t& A, uint32_t& k, uint64_t& B, double& v,
-                           unsigned& nan) {
-  const int lane = threadIdx.x & 31;
-  uint64_t a = 0, b = 0;
-  uint32_t kk = 0xffffffffu;
-  double vv = 0.0;
-  unsigned nn = 0;
-  for (int g = lane; g < G; g += 32) {
-    const uint64_t a2 = __ldcg(&parts[g].A), b2 = __ldcg(&parts[g].B);
-    const uint32_t k2 = __ldcg(&parts[g].k);
-    const double v2 = __ldcg(&parts[g].v);
-    nn |= __ldcg(&parts[g].nan);
-    big_combine(a, kk, b, vv, a2, k2, b2, v2);
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-    const double v2 = __shfl_down_sync(FULL, vv, off);
-    nn |= __shfl_down_sync(FULL, nn, off);
-    big_combine(a, kk, b, vv, a2, k2, b2, v2);
-  }
-  A = a;
-  k = kk;
-  B = b;
-  v = vv;
-  nan = nn;
+  t.A = ctl.red_u[NW];
+  t.B = ctl.red_b[NW];
+  t.k = (uint32_t)ctl.red_k[NW];
+  t.ph = ctl.red_p[NW];
+  t.v = ctl.red_s[NW];
+  __syncthreads();
 }
 
 struct BigArgs {
   const double* ain;      // m x n input (column-major)
-  double* A;              // m x n working copy
-  double* fact;           // m x n factors in physical order, then int32 rowperm[m], colperm[n]
+  double* A;              // m x n working copy (physical positions never change)
+  double* fact;           // m x n factors in logical order, then int32 rowperm[m], colperm[n]
   char* res;              // result record (tci_result_head, rowp[kcap], colp[kcap], diag[kcap])
-  BigPartial* parts;      // gridDim.x partials
+  BigPartial* parts;      // 2 x gridDim.x partials (double-buffered by pivot parity)
+  double* pivs;           // signed pivot of every step (kmax)
   BigBar* bar;
   int m, n, kmax, kcap, leftorth;
+  int pr, pc, mb, nb;     // CTA grid and block sizes
   double reltol, abstol;
 };
 
@@ -1889,32 +1887,52 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   __shared__ Ctl ctl;
   const int tid = threadIdx.x, G = gridDim.x, b = blockIdx.x, m = P.m, n = P.n;
   const bool leftorth = P.leftorth != 0;
-  double* x = (double*)smem;  // pivot column, m
-  int* stor = (int*)(x + m);  // physical position -> column, n
-  int* pos = stor + n;        // column -> physical position, n
-  int* rowperm = pos + n;     // m
+  const int r0 = (b / P.pc) * P.mb, c0 = (b % P.pc) * P.nb;
+  const int r1 = min(m, r0 + P.mb), c1 = min(n, c0 + P.nb);
+  const int nrb = max(0, r1 - r0), ncb = max(0, c1 - c0);  // block extent
+  double* xs = (double*)smem;          // x of the active rows (mb)
+  double* ys = xs + P.mb;              // y of the active columns (nb)
+  int* pos_r = (int*)(ys + P.nb);      // physical row -> logical (m)
+  int* stor_r = pos_r + m;             // logical row -> physical (m)
+  int* pos_c = stor_r + m;             // (n)
+  int* stor_c = pos_c + n;             // (n)
+  int* act_r = stor_c + n;             // active rows of the block, and the slot of each (mb each)
+  int* slot_r = act_r + P.mb;
+  int* act_c = slot_r + P.mb;          // (nb each)
+  int* slot_c = act_c + P.nb;
   unsigned gen = 0;
-  for (int j = tid; j < n; j += NT) {
-    stor[j] = j;
-    pos[j] = j;
-  }
-  for (int i = tid; i < m; i += NT) rowperm[i] = i;
+  for (int i = tid; i < m; i += NT) pos_r[i] = stor_r[i] = i;
+  for (int j = tid; j < n; j += NT) pos_c[j] = stor_c[j] = j;
+  for (int t = tid; t < nrb; t += NT) act_r[t] = slot_r[t] = t;  // local indices
+  for (int u = tid; u < ncb; u += NT) act_c[u] = slot_c[u] = u;
   if (tid == 0) {
     ctl.maxerror = 0.0;
     ctl.err = __longlong_as_double(0x7ff8000000000000LL);
     ctl.stop = 0;
-    P.parts[b].nan = 0;
+    ctl.r = nrb;  // active row / column counts
+    ctl.c = ncb;
   }
-  // copy own columns, first argmax
+  // copy own block, first argmax
   BigTrack bt;
   bt.init();
-  for (int j = b; j < n; j += G)
-    for (int i = tid; i < m; i += NT) {
+  {
+    const long long tot = (long long)nrb * ncb;
+    for (long long e = tid; e < tot; e += NT) {
+      const int i = r0 + (int)(e % nrb), j = c0 + (int)(e / nrb);
       const double v = P.ain[i + (size_t)j * m];
       P.A[i + (size_t)j * m] = v;
-      bt.push(v, pack_key(i, j));
+      bt.push(v, pack_key(i, j), pack_key(i, j));
     }
-  block_track(bt, ctl, &P.parts[b]);
+  }
+  block_track(bt, ctl);
+  if (tid == 0) {
+    BigPartial& o = P.parts[b];  // buffer 0: read at pivot 0
+    o.A = bt.A;
+    o.B = bt.B;
+    o.k = bt.k;
+    o.ph = bt.ph;
+    o.v = bt.v;
+  }
   bool ok = big_barrier(P.bar, G, gen, ctl);
   int K = 0;
   tci_result_head* head = (tci_result_head*)P.res;
@@ -1923,69 +1941,95 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   int* colp = (int*)(P.res + sizeof(tci_result_head) + align_up((size_t)kcap * 4, 8));
   double* diag = (double*)(P.res + sizeof(tci_result_head) + 2 * align_up((size_t)kcap * 4, 8));
   while (ok) {
-    // ---- the pivot: argmax of abs2 over the trailing block, from the partials
-    if (tid < 32) {
-      uint64_t A, B;
-      uint32_t k;
-      double v;
-      unsigned nn;
-      big_reduce(P.parts, G, A, k, B, v, nn);
+    // the partials of pivot K are in buffer K & 1: a CTA writes the next set to
+    // the other buffer, so a fast CTA never overwrites what a slow one reads
+    BigPartial* const cur = P.parts + (size_t)(K & 1) * G;
+    // ---- the pivot: argmax of abs2 over the trailing block, from the G partials
+    {
+      BigTrack g;
+      g.init();
+      for (int t = tid; t < G; t += NT) {
+        const BigPartial* q = cur + t;
+        big_combine(g.A, g.k, g.ph, g.B, g.v, __ldcg(&q->A), __ldcg(&q->k), __ldcg(&q->ph), __ldcg(&q->B),
+                    __ldcg(&q->v));
+      }
+      block_track(g, ctl);
       if (tid == 0) {
-        const uint64_t Mstar = A ? A - 1 : 0;
+        const uint64_t Mstar = g.A ? g.A - 1 : 0;
         const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
-        const bool close = B != 0 && (B - 1) + 16 >= Mstar;
+        const bool close = g.B != 0 && (g.B - 1) + 16 >= Mstar;
         ctl.red_u[NW] = Mstar;
-        ctl.need_exact = (A != 0 && !(safe && !close)) ? 1 : 0;
-        if (A == 0) {  // every element NaN: the scan keeps its start
-          ctl.r = K;
-          ctl.c = K;
-          ctl.piv = __ldcg(&P.A[K + (size_t)stor[K] * m]);
+        ctl.need_exact = (g.A != 0 && !(safe && !close)) ? 1 : 0;
+        if (g.A == 0) {  // every element NaN: the scan keeps its start
+          ctl.kmax = (int)(((unsigned)stor_c[K] << 16) | (unsigned)stor_r[K]);
+          ctl.K = (K << 16) | K;
+          ctl.piv = __ldcg(&P.A[stor_r[K] + (size_t)stor_c[K] * m]);
         } else {
-          ctl.r = (int)(k & 0xffffu);
-          ctl.c = (int)(k >> 16);
-          ctl.piv = v;
+          ctl.kmax = (int)g.ph;
+          ctl.K = (int)g.k;
+          ctl.piv = g.v;
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
     if (ctl.need_exact) {  // squares of the elements near the maximum (rare)
       const uint64_t Mstar = ctl.red_u[NW];
+      const int nr = ctl.r, nc = ctl.c;
       ArgBest ab;
       ab.init();
-      for (int j = b; j < n; j += G) {
-        const int pj = pos[j];
-        if (pj < K) continue;
-        for (int i = K + tid; i < m; i += NT) {
-          const double v = P.A[i + (size_t)j * m];
-          if (near_max(abs_bits(v), Mstar)) ab.consider(v, pack_key(i, pj));
+      uint32_t abph = 0;
+      for (long long e = tid; e < (long long)nr * nc; e += NT) {
+        const int i = r0 + act_r[(int)(e % nr)], j = c0 + act_c[(int)(e / nr)];
+        const double v = P.A[i + (size_t)j * m];
+        if (near_max(abs_bits(v), Mstar)) {
+          const uint32_t key = pack_key(pos_r[i], pos_c[j]);
+          const uint64_t q = (uint64_t)__double_as_longlong(__dmul_rn(v, v)) + 1;
+          if (q > ab.s || (q == ab.s && key < ab.key)) {
+            ab.s = q;
+            ab.key = key;
+            ab.val = v;
+            abph = pack_key(i, j);
+          }
         }
       }
       BigTrack et;
       et.A = ab.s;
       et.B = 0;
       et.k = ab.key;
+      et.ph = abph;
       et.v = ab.val;
       ok = big_barrier(P.bar, G, gen, ctl);  // everyone has read the partials
       if (!ok) break;
-      block_track(et, ctl, &P.parts[b]);
+      block_track(et, ctl);
+      if (tid == 0) {
+        BigPartial& o = cur[b];
+        o.A = et.A;
+        o.B = 0;
+        o.k = et.k;
+        o.ph = et.ph;
+        o.v = et.v;
+      }
       ok = big_barrier(P.bar, G, gen, ctl);
       if (!ok) break;
-      if (tid < 32) {
-        uint64_t A, B;
-        uint32_t k;
-        double v;
-        unsigned nn;
-        big_reduce(P.parts, G, A, k, B, v, nn);
-        if (tid == 0 && A) {
-          ctl.r = (int)(k & 0xffffu);
-          ctl.c = (int)(k >> 16);
-          ctl.piv = v;
-        }
+      BigTrack g;
+      g.init();
+      for (int t = tid; t < G; t += NT) {
+        const BigPartial* q = cur + t;
+        big_combine(g.A, g.k, g.ph, g.B, g.v, __ldcg(&q->A), __ldcg(&q->k), __ldcg(&q->ph), __ldcg(&q->B),
+                    __ldcg(&q->v));
+      }
+      block_track(g, ctl);
+      if (tid == 0 && g.A) {
+        ctl.kmax = (int)g.ph;
+        ctl.K = (int)g.k;
+        ctl.piv = g.v;
       }
       __syncthreads();
     }
-    // ---- decision (every CTA computes the same)
-    const int r = ctl.r, cp = ctl.c, cs = stor[cp];
+    // ---- decision (every CTA computes the same); thread 0 updates the maps
+    const unsigned key = (unsigned)ctl.K, ph = (unsigned)ctl.kmax;
+    const int rl = (int)(key & 0xffffu), cl = (int)(key >> 16);
+    const int R = (int)(ph & 0xffffu), Cc = (int)(ph >> 16);
     const double piv = ctl.piv;
     if (tid == 0) {
       const double e = fabs(piv);
@@ -1993,77 +2037,102 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
       ctl.stop = ((e < P.reltol * ctl.maxerror || e < P.abstol) && K > 0) ? 1 : 0;
       if (!ctl.stop) {
         ctl.maxerror = jmax(ctl.maxerror, e);
-        if (b == 0) diag[K] = e;
-        int t = rowperm[K];
-        rowperm[K] = rowperm[r];
-        rowperm[r] = t;
-        const int sk = stor[K];
-        stor[K] = cs;
-        stor[cp] = sk;
-        pos[cs] = K;
-        pos[sk] = cp;
+        if (b == 0) {
+          diag[K] = e;
+          P.pivs[K] = piv;
+        }
+        // swaprow!(K, rl), swapcol!(K, cl) on the maps
+        const int sr = stor_r[K];
+        stor_r[K] = R;
+        stor_r[rl] = sr;
+        pos_r[R] = K;
+        pos_r[sr] = rl;
+        const int sc = stor_c[K];
+        stor_c[K] = Cc;
+        stor_c[cl] = sc;
+        pos_c[Cc] = K;
+        pos_c[sc] = cl;
+        // the pivot row and column leave this block's active sets
+        if (R >= r0 && R < r1) {
+          const int s = slot_r[R - r0], last = act_r[ctl.r - 1];
+          act_r[s] = last;
+          slot_r[last] = s;
+          ctl.r -= 1;
+        }
+        if (Cc >= c0 && Cc < c1) {
+          const int s = slot_c[Cc - c0], last = act_c[ctl.c - 1];
+          act_c[s] = last;
+          slot_c[last] = s;
+          ctl.c -= 1;
+        }
       }
     }
     __syncthreads();
     if (ctl.stop) break;
-    // ---- swaprow! in own columns, then the scaling (matrixlu.jl:98-104, 114-124)
-    if (r != K)
-      for (int j = b + tid * G; j < n; j += NT * G) {
-        double* col = P.A + (size_t)j * m;
-        const double a = col[K];
-        col[K] = col[r];
-        col[r] = a;
-      }
-    __syncthreads();
-    if (leftorth) {
-      if (cs % G == b) {
-        double* col = P.A + (size_t)cs * m;
-        for (int i = K + 1 + tid; i < m; i += NT) col[i] = __ddiv_rn(col[i], piv);
-      }
-    } else {
-      for (int j = b + tid * G; j < n; j += NT * G)
-        if (pos[j] > K) P.A[K + (size_t)j * m] = __ddiv_rn(P.A[K + (size_t)j * m], piv);
-    }
     ++K;
     if (K == P.kmax) break;  // the trailing update after the last pivot is not observable
-    ok = big_barrier(P.bar, G, gen, ctl);
-    if (!ok) break;
-    // ---- rank-1 update of own trailing columns, fused with the argmax
-    const double* xs = P.A + (size_t)cs * m;
-    for (int i = K + tid; i < m; i += NT) x[i] = __ldcg(&xs[i]);
+    // ---- x (pivot column) for the active rows, y (pivot row) for the active columns
+    const int nr = ctl.r, nc = ctl.c;
+    for (int t = tid; t < nr; t += NT) {
+      const double v = __ldcg(&P.A[r0 + act_r[t] + (size_t)Cc * m]);
+      xs[t] = leftorth ? __ddiv_rn(v, piv) : v;
+    }
+    for (int u = tid; u < nc; u += NT) {
+      const double v = __ldcg(&P.A[R + (size_t)(c0 + act_c[u]) * m]);
+      ys[u] = leftorth ? v : __ddiv_rn(v, piv);
+    }
     __syncthreads();
+    // ---- rank-1 update of the block's active part, fused with its argmax
     bt.init();
-    for (int j = b; j < n; j += G) {
-      const int pj = pos[j];
-      if (pj < K) continue;
-      double* col = P.A + (size_t)j * m;
-      const double y = col[K - 1];
-      for (int i = K + tid; i < m; i += NT) {
-        const double v = __dsub_rn(col[i], __dmul_rn(x[i], y));
-        col[i] = v;
-        bt.push(v, pack_key(i, pj));
+    if (nr > 0 && nc > 0) {
+      const long long tot = (long long)nr * nc;
+      const int sq = NT / nr, sr = NT % nr;
+      int tt = tid % nr, uu = tid / nr;
+      for (long long e = tid; e < tot; e += NT) {
+        const int i = r0 + act_r[tt], j = c0 + act_c[uu];
+        double* a = P.A + i + (size_t)j * m;
+        const double v = __dsub_rn(*a, __dmul_rn(xs[tt], ys[uu]));
+        *a = v;
+        bt.push(v, pack_key(pos_r[i], pos_c[j]), pack_key(i, j));
+        tt += sr;
+        uu += sq;
+        if (tt >= nr) {
+          tt -= nr;
+          uu += 1;
+        }
       }
     }
-    block_track(bt, ctl, &P.parts[b]);
+    block_track(bt, ctl);
+    if (tid == 0) {
+      BigPartial& o = P.parts[(size_t)(K & 1) * G + b];  // read at pivot K (already incremented)
+      o.A = bt.A;
+      o.B = bt.B;
+      o.k = bt.k;
+      o.ph = bt.ph;
+      o.v = bt.v;
+    }
     ok = big_barrier(P.bar, G, gen, ctl);
   }
+  if (ok) ok = big_barrier(P.bar, G, gen, ctl);  // every pivot value is recorded
   if (!ok) {
     if (b == 0 && tid == 0) head->status = TCI_ST_TOO_LARGE;
     return;
   }
-  __syncthreads();  // the last pivot's scaling (other threads' columns / rows) is in place
-  // ---- NaN scan of L and U (matrixlu.jl:162-169), the factors in physical order
+  // ---- the factors in logical order, with the deferred scaling of addpivot!,
+  // and the NaN scan of L and U (matrixlu.jl:162-169)
   int bad = 0;
-  for (int j = b; j < n; j += G) {
-    const int pj = pos[j];
-    const double* col = P.A + (size_t)j * m;
-    double* dst = P.fact + (size_t)pj * m;
-    for (int i = tid; i < m; i += NT) {
-      const double v = col[i];
-      const bool inL = pj < K && i >= pj;
-      const bool inU = i < K && i <= pj;
+  {
+    const long long tot = (long long)nrb * ncb;
+    for (long long e = tid; e < tot; e += NT) {
+      const int i = r0 + (int)(e % nrb), j = c0 + (int)(e / nrb);
+      const int lr = pos_r[i], lc = pos_c[j];
+      double v = P.A[i + (size_t)j * m];
+      if (leftorth && lc < K && lr > lc) v = __ddiv_rn(v, __ldcg(&P.pivs[lc]));
+      if (!leftorth && lr < K && lc > lr) v = __ddiv_rn(v, __ldcg(&P.pivs[lr]));
+      const bool inL = lc < K && lr >= lc;
+      const bool inU = lr < K && lr <= lc;
       if ((inL || inU) && v != v) bad = 1;
-      dst[i] = v;
+      P.fact[lr + (size_t)lc * m] = v;
     }
   }
   bad = __syncthreads_or(bad);
@@ -2074,24 +2143,18 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
     return;
   }
   if (b == 0) {
-    if (tid < 32) {
-      uint64_t A, B;
-      uint32_t k;
-      double v;
-      unsigned nn;
-      big_reduce(P.parts, G, A, k, B, v, nn);
-      if (tid == 0) ctl.status = nn ? 1 : 0;
-    }
-    __syncthreads();
+    int nan = 0;
+    for (int t = tid; t < G; t += NT) nan |= (int)__ldcg(&P.parts[t].nan);
+    nan = __syncthreads_or(nan);
     int* fr = (int*)(P.fact + (size_t)m * n);
-    for (int i = tid; i < m; i += NT) fr[i] = rowperm[i];
-    for (int j = tid; j < n; j += NT) fr[m + j] = stor[j];
+    for (int i = tid; i < m; i += NT) fr[i] = stor_r[i];
+    for (int j = tid; j < n; j += NT) fr[m + j] = stor_c[j];
     for (int q = tid; q < K; q += NT) {
-      rowp[q] = rowperm[q];
-      colp[q] = stor[q];
+      rowp[q] = stor_r[q];
+      colp[q] = stor_c[q];
     }
     if (tid == 0) {
-      head->status = ctl.status ? TCI_ST_NAN : 0;
+      head->status = nan ? TCI_ST_NAN : 0;
       head->npivot = K;
       head->error = K >= min(m, n) ? 0.0 : ctl.err;
       head->maxabs = 0.0;
@@ -2124,23 +2187,52 @@ cudaError_t tci_step_configure() {
                               (int)tci_step_smem_bytes());
 }
 
-// Multi-CTA rrLU (rrlu_big_kernel): shared memory per CTA, and whether a matrix
-// qualifies (keys pack 16-bit rows and columns; the CTA keeps the pivot column,
-// both column maps and the row permutation on chip).
-size_t tci_rrlu_big_smem(int64_t m, int64_t n) { return (size_t)(12 * m + 8 * n + 64); }
-bool tci_rrlu_big_fits(int64_t m, int64_t n) {
-  return m >= 1 && n >= 1 && m <= 65535 && n <= 65535 && tci_rrlu_big_smem(m, n) <= tci_step_smem_bytes();
+// Multi-CTA rrLU (rrlu_big_kernel).  The CTA grid: pr x pc <= G CTAs with the
+// largest count, then the most square blocks.  Shared memory per CTA: both
+// permutation maps (8 (m + n) bytes) and, per block row / column, x or y, the
+// active list and the slot map (16 bytes each).
+namespace {
+struct BigGrid {
+  int pr, pc, mb, nb;
+};
+BigGrid big_grid(int64_t m, int64_t n, int G) {
+  BigGrid best{1, 1, (int)m, (int)n};
+  double best_score = -1.0;
+  for (int pr = 1; pr <= G; ++pr) {
+    const int pc = G / pr;
+    if (pr > m || pc > n || pc < 1) continue;
+    const int mb = (int)((m + pr - 1) / pr), nb = (int)((n + pc - 1) / pc);
+    const double aspect = (double)mb / nb;
+    const double score = (double)pr * pc - 1e-3 * std::fabs(std::log(aspect));
+    if (score > best_score) {
+      best_score = score;
+      best = BigGrid{pr, pc, mb, nb};
+    }
+  }
+  return best;
 }
-size_t tci_rrlu_big_scratch_bytes(int grid) { return 64 + (size_t)grid * sizeof(BigPartial); }
+}  // namespace
+size_t tci_rrlu_big_smem(int64_t m, int64_t n, int G) {
+  const BigGrid g = big_grid(m, n, G);
+  return (size_t)(8 * (m + n) + 16 * ((int64_t)g.mb + g.nb) + 64);
+}
+bool tci_rrlu_big_fits(int64_t m, int64_t n, int G) {
+  return m >= 1 && n >= 1 && m <= 65535 && n <= 65535 && tci_rrlu_big_smem(m, n, G) <= tci_step_smem_bytes();
+}
+size_t tci_rrlu_big_scratch_bytes(int grid, int kmax) {
+  return 64 + 2 * (size_t)grid * sizeof(BigPartial) + (size_t)std::max(kmax, 1) * sizeof(double);
+}
 
-// Launch on `grid` CTAs (all co-resident: cooperative launch).  scratch holds
-// the grid barrier and the partials (tci_rrlu_big_scratch_bytes); it is
-// cleared here.  res is a device result record with room for kcap pivots.
+// Launch on up to `grid` CTAs (all co-resident: cooperative launch).  scratch
+// holds the grid barrier, the partials and the pivot values
+// (tci_rrlu_big_scratch_bytes); it is cleared here.  res is a device result
+// record with room for kcap pivots.
 cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, char* res, void* scratch, int m,
                                 int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
                                 cudaStream_t stream) {
-  cudaError_t e = cudaMemsetAsync(scratch, 0, tci_rrlu_big_scratch_bytes(grid), stream);
+  cudaError_t e = cudaMemsetAsync(scratch, 0, tci_rrlu_big_scratch_bytes(grid, kmax), stream);
   if (e != cudaSuccess) return e;
+  const BigGrid g = big_grid(m, n, grid);
   BigArgs a;
   a.ain = ain;
   a.A = work;
@@ -2148,16 +2240,21 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
   a.res = res;
   a.bar = (BigBar*)scratch;
   a.parts = (BigPartial*)((char*)scratch + 64);
+  a.pivs = (double*)((char*)scratch + 64 + 2 * (size_t)grid * sizeof(BigPartial));
   a.m = m;
   a.n = n;
   a.kmax = kmax;
   a.kcap = kcap;
   a.leftorth = leftorth;
+  a.pr = g.pr;
+  a.pc = g.pc;
+  a.mb = g.mb;
+  a.nb = g.nb;
   a.reltol = reltol;
   a.abstol = abstol;
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(grid), dim3(NT), args,
-                                     tci_rrlu_big_smem(m, n), stream);
+  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(NT), args,
+                                     tci_rrlu_big_smem(m, n, grid), stream);
 }
 
 // Launch the resident kernel: one CTA per SM, all resident at once
