@@ -2082,16 +2082,48 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
       ys[u] = leftorth ? v : __ddiv_rn(v, piv);
     }
     __syncthreads();
-    // ---- rank-1 update of the block's active part, fused with its argmax
+    // ---- rank-1 update of the block's active part, fused with its argmax.
+    // Four elements per step with their loads issued first (four L2 reads in
+    // flight per thread); the columns are walked in reverse on odd pivots, so
+    // the part of the block the last pass touched last is still in L1.
     bt.init();
     if (nr > 0 && nc > 0) {
       const long long tot = (long long)nr * nc;
       const int sq = NT / nr, sr = NT % nr;
+      const bool rev = (K & 1) != 0;
       int tt = tid % nr, uu = tid / nr;
-      for (long long e = tid; e < tot; e += NT) {
-        const int i = r0 + act_r[tt], j = c0 + act_c[uu];
+      long long e = tid;
+      for (; e + 3LL * NT < tot; e += 4LL * NT) {
+        int ti[4], ui[4];
+        double* ap[4];
+        double av[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          ti[q] = tt;
+          ui[q] = rev ? nc - 1 - uu : uu;
+          ap[q] = P.A + (r0 + act_r[ti[q]]) + (size_t)(c0 + act_c[ui[q]]) * m;
+          tt += sr;
+          uu += sq;
+          if (tt >= nr) {
+            tt -= nr;
+            uu += 1;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) av[q] = *ap[q];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double v = __dsub_rn(av[q], __dmul_rn(xs[ti[q]], ys[ui[q]]));
+          *ap[q] = v;
+          const int i = r0 + act_r[ti[q]], j = c0 + act_c[ui[q]];
+          bt.push(v, pack_key(pos_r[i], pos_c[j]), pack_key(i, j));
+        }
+      }
+      for (; e < tot; e += NT) {
+        const int u = rev ? nc - 1 - uu : uu;
+        const int i = r0 + act_r[tt], j = c0 + act_c[u];
         double* a = P.A + i + (size_t)j * m;
-        const double v = __dsub_rn(*a, __dmul_rn(xs[tt], ys[uu]));
+        const double v = __dsub_rn(*a, __dmul_rn(xs[tt], ys[u]));
         *a = v;
         bt.push(v, pack_key(pos_r[i], pos_c[j]), pack_key(i, j));
         tt += sr;
@@ -2252,6 +2284,15 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
   a.nb = g.nb;
   a.reltol = reltol;
   a.abstol = abstol;
+  // most of the SM's on-chip memory as L1: the CTA's block of the working
+  // matrix is re-read every pivot (the attribute is a hint; the shared memory
+  // the launch asks for is always granted)
+  static bool carve = false;
+  if (!carve) {
+    e = cudaFuncSetAttribute((const void*)rrlu_big_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+    if (e != cudaSuccess) return e;
+    carve = true;
+  }
   void* args[] = {(void*)&a};
   return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(NT), args,
                                      tci_rrlu_big_smem(m, n, grid), stream);
