@@ -469,25 +469,36 @@ def rrlu_batch_bench(T, ctx, peak_sep, with_cpu=True, reps=3):
     mats = workloads.rrlu_batch(4096, seed=0)
     nbytes = sum(a.size for a in mats) * 8
     T.rrlu_batched(mats[:64], maxrank=256, reltol=1e-10, ctx=ctx)  # warm-up
-    e2e = []
-    kern = []
-    ops = 0.0
-    for _ in range(reps):
-        ctx.stats(reset=True)
-        t0 = time.perf_counter()
-        res = T.rrlu_batched(mats, maxrank=256, reltol=1e-10, ctx=ctx)
-        e2e.append(time.perf_counter() - t0)
-        st = ctx.stats(reset=True)
-        kern.append(st["kernel_ms"] * 1e-3)
-        ops = 2.0 * st["lu_updates"]
-    kt = float(np.median(kern))
+
+    def run():
+        e2e, kern, ops, res = [], [], 0.0, None
+        for _ in range(reps):
+            ctx.stats(reset=True)
+            t0 = time.perf_counter()
+            res = T.rrlu_batched(mats, maxrank=256, reltol=1e-10, ctx=ctx)
+            e2e.append(time.perf_counter() - t0)
+            st = ctx.stats(reset=True)
+            kern.append(st["kernel_ms"] * 1e-3)
+            ops = 2.0 * st["lu_updates"]
+        return res, float(np.median(kern)), e2e, ops
+
+    tuned = ctx.tune_table()
+    res, kt, e2e, ops = run()
+    # the same launch with the kernel's fixed default for every bucket
+    ctx.tune_table([0] * len(tuned))
+    res_f, kt_f, _, _ = run()
+    ctx.tune_table(tuned)
+    same = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[3] == b[3]
+               for a, b in zip(res, res_f))
     out = {"workload": "4096 matrices (2r)x(2r), r uniform in [8,128] (seed 0), U diag(10^(-k/4)) V^T + 1e-12 "
                        "noise, reltol 1e-10, maxrank 256",
            "matrices_per_s_device": len(mats) / kt, "kernel_ms": kt * 1e3,
            "e2e_matrices_per_s": len(mats) / float(np.median(e2e)),
            "mean_npivot": float(np.mean([r[2] for r in res])),
            "fp64_tflops": ops / kt / 1e12, "fp64_frac_of_measured": ops / kt / peak_sep,
-           "input_gb": nbytes / 1e9, "input_read_gbs": nbytes / kt / 1e9}
+           "input_gb": nbytes / 1e9, "input_read_gbs": nbytes / kt / 1e9,
+           "autotune": {"tuned_table": tuned, "fixed_kernel_ms": kt_f * 1e3, "tuned_over_fixed": kt_f / kt,
+                        "same_pivots_and_errors": bool(same)}}
     if with_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle as O
@@ -552,6 +563,7 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=2000,
                     help="requests of each step's list that the reference arm solves")
     ap.add_argument("--no-parity", action="store_true", help="skip the parity sample of the timed solves")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the kernel's fixed rrLU tail size")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-rrlu", action="store_true", help="skip the batched-rrLU sub-measurement")
     ap.add_argument("--no-single", action="store_true", help="skip the single-solve configurations")
@@ -570,6 +582,8 @@ def main():
     ctx = T.Context(int(os.environ.get("LOCAL_RANK", "0")))
     peak_sep, peak_fma = T.fp64_peak(ctx)
     if args.only == "rrlu":  # the batched-rrLU configuration alone (one warm-up launch, then --steps)
+        if not args.no_autotune:
+            ctx.autotune_rrlu()
         print(json.dumps(rrlu_batch_bench(T, ctx, peak_sep, with_cpu=False, reps=max(1, args.steps))))
         return
     if args.only == "big-rrlu":  # the multi-CTA rrLU alone
@@ -601,6 +615,17 @@ def main():
         tstream = torch.cuda.ExternalStream(ctx.stream)
     except Exception:
         tstream = None
+
+    # the autotuner: rrLU tail size per (rows, cols) bucket, calibrated on seeded
+    # matrices before anything is timed; every later task of the context uses it
+    tune = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        sp, md, mt = ctx.autotune_rrlu()
+        tune = {"calibration_speedup": sp, "calibration_ms_default": md, "calibration_ms_tuned": mt,
+                "table": ctx.tune_table(), "calibration_s": time.perf_counter() - t0,
+                "knob": "trailing-block size (elements) below which a factorization continues on one warp, "
+                        "per (rows, cols) bucket"}
 
     # warm-up
     for s in range(args.warmup):
@@ -665,6 +690,25 @@ def main():
     if rank == 0 and not args.no_parity:
         parity = parity_sample(T, last_res, last_reqs)
     del last_res
+
+    # tuned over fixed on the served stream: one step's device time each
+    if tune is not None and tstream is not None:
+        def step_ms(table):
+            ctx.tune_table(table)
+            _, sp_ = specs_for(8888)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(tstream)
+            T.crossinterpolate2_batched(sp_, max_live=args.live, ctx=ctx)
+            e1.record(tstream)
+            e1.synchronize()
+            return e0.elapsed_time(e1)
+        fixed_ms = step_ms([0] * len(tune["table"]))
+        tuned_ms = step_ms(tune["table"])
+        tune["served_step_ms_fixed"] = fixed_ms
+        tune["served_step_ms_tuned"] = tuned_ms
+        tune["served_tuned_over_fixed"] = fixed_ms / tuned_ms
+        ctx.stats(reset=True)
 
     # the same family at tolerances 1e-10 .. 1e-8 only (the metric's error bar)
     _, specs_t = specs_for(7777, tol_range=(-10.0, -8.0))
@@ -734,6 +778,7 @@ def main():
         "serve_rate_per_s": lam,
         "serve_sweep": sweep,
         "tight_tolerance": tight,
+        "autotune": tune,
         "parity_sample": parity,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak if peak else None, "traffic": None,

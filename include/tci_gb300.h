@@ -320,6 +320,23 @@ int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank,
                      int32_t* npivot_dev, double* error_dev, int32_t* status_dev, double* factors_dev,
                      uintptr_t stream);
 
+/* ---- autotuner (no reference counterpart) -------------------------------
+ * The rank-revealing LU of a step-kernel task runs on the whole CTA until its
+ * trailing block has at most T elements and finishes on one warp (no CTA
+ * barriers per pivot).  tci_autotune_rrlu picks T per (rows, cols) bucket
+ * (12 buckets: the smaller dimension in <= 24, <= 48, <= 96, <= 160, <= 256,
+ * > 256, times square-ish or more than 2:1) by timing the candidates
+ * {1, 96, 192, 320, 512, 768, 1024, 1536} on seeded matrices of each bucket
+ * (U diag(10^(-k/4)) V^T + 1e-12 noise, one per SM, reltol 1e-10), reps timed
+ * runs each after one warm-up, with CUDA events around the step kernel; every
+ * later rrLU and TCI task of the context uses the table.  *speedup = the sum of
+ * the default's (T = 192) times over the sum of the best times; ms_default /
+ * ms_tuned those sums (any may be NULL).  Pivots do not depend on T. */
+int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_default, double* ms_tuned);
+/* Read (set = 0) or write (set = 1) the tuned table: nbuckets entries (0 = the
+ * kernel's default); *nbuckets receives the count (pass table = NULL to query). */
+int tci_autotune_table(tci_ctx* ctx, int32_t* table, int32_t* nbuckets, int32_t set);
+
 /* ---- context utilities --------------------------------------------------- */
 /* cudaStream_t of the context, as an integer. */
 uintptr_t tci_ctx_stream(tci_ctx* ctx);

@@ -1280,6 +1280,142 @@ int tci_rrlu_batched(tci_ctx* ctx, int64_t nmat, const double* A, const int64_t*
   return 0;
 }
 
+// ---------------------------------------------------------------- autotuner
+namespace {
+
+// Seeded calibration matrices of one tuning bucket: A = G1 diag(10^(-k/4)) G2^T
+// + 1e-12 noise (the decay of the batched-rrLU workload), Gaussian G1, G2; the
+// terms beyond k = 48 (below 1e-12) are left to the noise.
+struct TuneRng {
+  uint64_t s;
+  uint64_t next() {
+    uint64_t z = (s += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  }
+  double uniform() { return ((double)(next() >> 11) + 0.5) * (1.0 / 9007199254740992.0); }
+  double normal() {
+    const double u = uniform(), v = uniform();
+    return std::sqrt(-2.0 * std::log(u)) * std::cos(6.283185307179586 * v);
+  }
+};
+
+void tune_matrix(TuneRng& g, int64_t m, int64_t n, std::vector<double>& A) {
+  const int64_t r = std::min<int64_t>(std::min(m, n), 48);
+  std::vector<double> G1((size_t)(m * r)), G2((size_t)(n * r));
+  for (auto& x : G1) x = g.normal();
+  for (auto& x : G2) x = g.normal();
+  A.assign((size_t)(m * n), 0.0);
+  for (int64_t k = 0; k < r; ++k) {
+    const double sk = std::pow(10.0, -(double)k / 4.0);
+    for (int64_t j = 0; j < n; ++j) {
+      const double y = sk * G2[(size_t)(j + n * k)];
+      for (int64_t i = 0; i < m; ++i) A[(size_t)(i + m * j)] += G1[(size_t)(i + m * k)] * y;
+    }
+  }
+  for (auto& x : A) x += 1e-12 * g.normal();
+}
+
+}  // namespace
+
+int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_default, double* ms_tuned) {
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (ctx->rq) {  // plain launches: the calibration times the batched step kernel
+    int rc = ctx->rq->stop();
+    if (rc) return rc;
+  }
+  Engine& e = ctx->eng_ref();
+  const int32_t cands[] = {1, 96, 192, 320, 512, 768, 1024, 1536};
+  const int32_t dflt = 192;
+  // bucket size ranges (the smaller dimension) as in Engine::tune_bucket
+  const int64_t lo[6] = {8, 25, 49, 97, 161, 257}, hi[6] = {24, 48, 96, 160, 256, 320};
+  reps = std::max(1, reps);
+  double tot_def = 0.0, tot_best = 0.0;
+  int32_t table[Engine::TUNE_BUCKETS];
+  const bool timing = e.timing;
+  e.timing = true;
+  for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) {
+    const int size = bk / 2, elong = bk % 2;
+    TuneRng g{0x7a11ULL + (uint64_t)bk};
+    const int64_t nmat = (int64_t)e.num_sms;
+    std::vector<std::vector<double>> mats((size_t)nmat);
+    std::vector<int64_t> ms((size_t)nmat), ns((size_t)nmat);
+    for (int64_t q = 0; q < nmat; ++q) {
+      const int64_t s0 = lo[size] + (int64_t)(g.uniform() * (double)(hi[size] - lo[size] + 1));
+      int64_t m = s0, n = s0;
+      if (elong) {
+        if (q & 1)
+          n = 3 * s0;
+        else
+          m = 3 * s0;
+      }
+      ms[(size_t)q] = m;
+      ns[(size_t)q] = n;
+      tune_matrix(g, m, n, mats[(size_t)q]);
+    }
+    double best_t = 0.0, def_t = 0.0;
+    int32_t best_c = dflt;
+    for (int32_t c : cands) {
+      double tmin = 1e300;
+      for (int rep = 0; rep < reps + 1; ++rep) {  // first run warms up
+        std::vector<Req> rs((size_t)nmat);
+        std::vector<Req*> ptrs;
+        for (int64_t q = 0; q < nmat; ++q) {
+          Req& r = rs[(size_t)q];
+          r.t.kind = TCI_TASK_RRLU;
+          r.t.m = (int32_t)ms[(size_t)q];
+          r.t.n = (int32_t)ns[(size_t)q];
+          r.t.maxrank = r.t.kcap = (int32_t)std::min(ms[(size_t)q], ns[(size_t)q]);
+          r.t.reltol = 1e-10;
+          r.t.leftorth = 1;
+          r.t.post = TCI_POST_NONE;
+          r.t.tail_elems = c;
+          r.ain_host = mats[(size_t)q].data();
+          ptrs.push_back(&r);
+        }
+        const double k0 = e.stats.kernel_ms;
+        int rc = e.run_tasks(ptrs);
+        if (rc) {
+          e.timing = timing;
+          return rc;
+        }
+        if (rep > 0) tmin = std::min(tmin, e.stats.kernel_ms - k0);
+      }
+      if (c == dflt) def_t = tmin;
+      if (best_t == 0.0 || tmin < best_t) {
+        best_t = tmin;
+        best_c = c;
+      }
+    }
+    table[bk] = best_c;
+    tot_def += def_t;
+    tot_best += best_t;
+  }
+  e.timing = timing;
+  for (auto& eng : ctx->pool)
+    for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) eng->tail_table[bk] = table[bk];
+  if (speedup) *speedup = tot_best > 0 ? tot_def / tot_best : 1.0;
+  if (ms_default) *ms_default = tot_def;
+  if (ms_tuned) *ms_tuned = tot_best;
+  return 0;
+}
+
+int tci_autotune_table(tci_ctx* ctx, int32_t* table, int32_t* nbuckets, int32_t set) {
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  if (nbuckets) *nbuckets = Engine::TUNE_BUCKETS;
+  if (!table) return 0;
+  if (set) {
+    for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk)
+      if (table[bk] < 0) return fail(TCI_ERR_ARG, "tail sizes must be >= 0 (0: the kernel's default)");
+    for (auto& eng : ctx->pool)
+      for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) eng->tail_table[bk] = table[bk];
+  } else {
+    for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) table[bk] = ctx->eng_ref().tail_table[bk];
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------- tensor-train contraction
 }  // extern "C"
 

@@ -413,11 +413,13 @@ int Engine::launch() {
   std::vector<char> bad(nt, 0);
   std::vector<size_t> wel(nt, 0);
   bool anybad = false;
-  for (size_t i = 0; i < nt; ++i)
+  for (size_t i = 0; i < nt; ++i) {
+    apply_tuning(batch[i]->t);
     if (!plan_task(batch[i]->t, smem_bytes, wel[i])) {
       bad[i] = 1;
       anybad = true;
     }
+  }
   if (anybad) {
     std::vector<Req*> good;
     std::vector<Waiter> goodw, badw;
@@ -809,6 +811,7 @@ int Engine::submit() {
       Req& r = *batch[k];
       tci_task& t = r.t;
       size_t we = 0;
+      apply_tuning(t);
       if (!plan_task(t, res_smem_, we)) {
         rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
         break;

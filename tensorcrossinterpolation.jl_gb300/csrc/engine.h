@@ -296,6 +296,19 @@ class Engine {
   size_t smem_bytes = 0;
   int num_sms = 0;
   size_t hbm_budget = 0;
+  // Autotuned rrLU parameter per (rows, cols) bucket: the trailing-block size
+  // (elements) at which a factorization continues on one warp instead of the
+  // whole CTA; 0 = the kernel's default.  Filled by tci_autotune_rrlu.
+  static constexpr int TUNE_BUCKETS = 12;
+  int32_t tail_table[TUNE_BUCKETS] = {0};
+  static int tune_bucket(int64_t m, int64_t n) {
+    const int64_t s = m < n ? m : n, l = m < n ? n : m;
+    const int size = s <= 24 ? 0 : s <= 48 ? 1 : s <= 96 ? 2 : s <= 160 ? 3 : s <= 256 ? 4 : 5;
+    return 2 * size + (l > 2 * s ? 1 : 0);
+  }
+  void apply_tuning(tci_task& t) const {
+    if (t.kind == TCI_TASK_RRLU && t.tail_elems == 0) t.tail_elems = tail_table[tune_bucket(t.m, t.n)];
+  }
 
  private:
   struct Waiter {

@@ -952,7 +952,8 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   const bool leftorth = T.leftorth != 0;
   double* xy = nullptr;
   if (!T.smem_mode && (size_t)(cur.p - smem) + (size_t)(m + n) * 8 <= smem_bytes) xy = (double*)cur.take((size_t)(m + n) * 8);
-  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl, xy);
+  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl, xy,
+            T.tail_elems > 0 ? T.tail_elems : WARP_TAIL_RRLU);
   const int K = ctl.K;
   int nan = lu_has_nan(A, lda, m, n, K, ctl);
   if (T.post == TCI_POST_LEFT && !nan) post_left(A, lda, m, n, K, leftorth, rowperm, T.core_out);

@@ -65,6 +65,9 @@ typedef struct tci_task {
   uint64_t ticket;             // resident mode: host-ring ticket (the record's done word = ticket + 1)
   int32_t lut_full;            // lut holds the solve's tables over the whole range (no per-task build)
   int32_t lut_base0;           // the integer sum at table0[0] (table1 starts at 0)
+  int32_t tail_elems;          // RRLU: trailing blocks of at most this many elements finish on one
+                               // warp (0: the kernel's default); set from the autotuned table
+  int32_t pad_tail;
 } tci_task;
 
 // Result record: fixed header followed by per-task arrays.

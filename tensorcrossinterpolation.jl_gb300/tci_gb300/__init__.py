@@ -204,6 +204,9 @@ _SIGNATURES = {
     "tci_get_cores_batched": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p), F64P,
                                              I64P]),
     "tci_ctx_set_resident_limits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64]),
+    "tci_autotune_rrlu": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int32, F64P, F64P, F64P]),
+    "tci_autotune_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                          ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]),
     "tci_rrlu_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
                                         ctypes.c_double, ctypes.c_double, ctypes.c_int32, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -284,6 +287,27 @@ class Context:
         """Bounds of the resident kernel's waits: it leaves after idle_us with
         nothing to do, and a worker waits at most wait_us for its task."""
         _check(load_library().tci_ctx_set_resident_limits(self.h, int(idle_us), int(wait_us)))
+
+    def autotune_rrlu(self, reps=2):
+        """Time the rrLU tail-size candidates per (rows, cols) bucket on seeded
+        matrices and keep the fastest for this context's later tasks.  Returns
+        (speedup over the default, default ms, tuned ms)."""
+        out = np.zeros(3)
+        _check(load_library().tci_autotune_rrlu(self.h, int(reps), _p(out[0:], F64P), _p(out[1:], F64P),
+                                                _p(out[2:], F64P)))
+        return float(out[0]), float(out[1]), float(out[2])
+
+    def tune_table(self, table=None):
+        """The tuned tail sizes per bucket; with `table`, set them (0 = default)."""
+        lib = load_library()
+        nb = ctypes.c_int32()
+        _check(lib.tci_autotune_table(self.h, None, ctypes.byref(nb), 0))
+        if table is not None:
+            arr = (ctypes.c_int32 * nb.value)(*[int(x) for x in table])
+            _check(lib.tci_autotune_table(self.h, arr, ctypes.byref(nb), 1))
+        arr = (ctypes.c_int32 * nb.value)()
+        _check(lib.tci_autotune_table(self.h, arr, ctypes.byref(nb), 0))
+        return list(arr)
 
     def stats(self, reset=False):
         s = Stats()
