@@ -367,10 +367,10 @@ def single_solve_configs(T, ctx, with_cpu=True):
     rng = np.random.default_rng(55)
     bonds = [1] + [64] * 29 + [1]
     op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 8.0 for i in range(30)]
-    tz, res = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, ctx=ctx),
+    tz, res = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, method="LU", ctx=ctx),
                        reps=1)
     ctx.stats(reset=True)
-    tzs, res_s = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, ctx=ctx,
+    tzs, res_s = _best_of(lambda: T.contract(op, mps, algorithm="zipup", tolerance=1e-9, maxbonddim=512, method="LU", ctx=ctx,
                                               precision="tf32x3"), reps=1)
     st = ctx.stats(reset=True)
     pts = rng.integers(1, 5, size=(20, 30))

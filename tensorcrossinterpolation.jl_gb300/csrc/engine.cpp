@@ -18,7 +18,7 @@
 cudaError_t tci_step_configure();
 size_t tci_step_smem_bytes();
 cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
-                            int* counter_dev, int grid, cudaStream_t stream);
+                            int* counter_dev, int grid, double* cta_area, size_t cta_stride, cudaStream_t stream);
 cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
 size_t tci_resident_smem_bytes();
 size_t tci_rrlu_big_smem(int64_t m, int64_t n, int G);
@@ -407,8 +407,8 @@ int Engine::launch() {
   const size_t off_order = off;
   off = a16(off + nt * sizeof(int));
   std::vector<size_t> o_params(nt), o_rows(nt), o_cols(nt), o_prows(nt), o_cores(nt), o_ain(nt);
-  std::vector<size_t> o_res(nt), o_work(nt);
-  size_t res_total = 0, work_total = 0;
+  std::vector<size_t> o_res(nt);
+  size_t res_total = 0, work_total = 0, cta_stride = 0;
   // Plan every task; a task that cannot run fails its own waiter only.
   std::vector<char> bad(nt, 0);
   std::vector<size_t> wel(nt, 0);
@@ -466,11 +466,17 @@ int Engine::launch() {
     o_res[i] = res_total;
     r.res_bytes = result_bytes(r.t);
     res_total += r.res_bytes;
-    o_work[i] = work_total;
-    work_total += we;
-    if (r.t.lutcap0 > 0 && !r.t.lut_full) work_total += (size_t)r.t.lutcap0 + (size_t)std::max(r.t.lutcap1, 0);
+    // global-memory scratch (a matrix too large for shared memory, per-task f
+    // tables): one area per CTA, reused by the CTA's successive tasks, so the
+    // scratch stays hot in L2 instead of a fresh region per task
+    size_t need = we;
+    if (r.t.lutcap0 > 0 && !r.t.lut_full) need += (size_t)r.t.lutcap0 + (size_t)std::max(r.t.lutcap1, 0);
+    cta_stride = std::max(cta_stride, need);
   }
   const size_t blob_total = off;
+  const int grid = std::max(1, std::min<int>((int)nt, num_sms * TCI_CTAS_PER_SM));
+  cta_stride = (cta_stride + 31) / 32 * 32;  // 256-byte aligned areas
+  work_total = cta_stride * (size_t)grid;
   int rc = ensure(blob_total, res_total, work_total);
   if (rc) {
     std::vector<Waiter> ws;
@@ -492,8 +498,8 @@ int Engine::launch() {
     t.prows = (int64_t)o_prows[i];
     t.cores = r.ncores ? (int64_t)o_cores[i] : 0;
     t.res = (int64_t)o_res[i];
-    t.work = t.smem_mode ? nullptr : dwork_ + o_work[i];
-    if (!t.lut_full) t.lut = t.lutcap0 > 0 ? dwork_ + o_work[i] + wel[i] : nullptr;
+    t.work = nullptr;  // the kernel points it (and a per-task table) into its CTA's area
+    if (!t.lut_full) t.lut = nullptr;
     if (r.ain_host) t.ain = (const double*)(dblob_ + o_ain[i]);
     t.cost = task_cost(t);
     tasks[i] = t;
@@ -510,10 +516,9 @@ int Engine::launch() {
 
   // ---- upload, launch, download
   CUDA_TRY(cudaMemcpyAsync(dblob_, hblob_, blob_total, cudaMemcpyHostToDevice, stream_));
-  const int grid = std::max(1, std::min<int>((int)nt, num_sms * TCI_CTAS_PER_SM));
   if (timing) CUDA_TRY(cudaEventRecord(ev0_, stream_));
-  CUDA_TRY(tci_step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid,
-                           stream_));
+  CUDA_TRY(tci_step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid, dwork_,
+                           cta_stride, stream_));
   if (timing) CUDA_TRY(cudaEventRecord(ev1_, stream_));
   CUDA_TRY(cudaMemcpyAsync(hres_, dres_, res_total, cudaMemcpyDeviceToHost, stream_));
   CUDA_TRY(cudaEventRecord(done_, stream_));

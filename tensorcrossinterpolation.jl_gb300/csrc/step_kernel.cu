@@ -745,7 +745,33 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
       for (int j = K + tid; j < n; j += NT) ys[j] = A[(K - 1) + (size_t)j * lda];
       __syncthreads();
       int jj = tid / rows, ii = tid % rows;
-      for (long long e = tid; e < total; e += NT) {
+      long long e = tid;
+      // four elements per step with their global loads issued first; the keys
+      // still reach the tracker in increasing order
+      for (; e + 3LL * NT < total; e += 4LL * NT) {
+        int i4[4], j4[4];
+        double a4[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          i4[q] = K + ii;
+          j4[q] = K + jj;
+          ii += sr;
+          jj += sq;
+          if (ii >= rows) {
+            ii -= rows;
+            jj += 1;
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) a4[q] = A[i4[q] + (size_t)j4[q] * lda];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const double v = __dsub_rn(a4[q], __dmul_rn(xs[i4[q]], ys[j4[q]]));
+          A[i4[q] + (size_t)j4[q] * lda] = v;
+          at.push(v, pack_key(i4[q], j4[q]));
+        }
+      }
+      for (; e < total; e += NT) {
         const int i = K + ii, j = K + jj;
         double* col = A + (size_t)j * lda;
         const double v = __dsub_rn(col[i], __dmul_rn(xs[i], ys[j]));
@@ -909,11 +935,13 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   am.init();
   unsigned long long mx = 0;
   if (T.ain) {
+    // the input is read once: evict-first loads keep it from pushing the
+    // working matrices (re-read every pivot) out of L2
     for (int j = warp; j < n; j += NW) {
       const double* src = T.ain + (size_t)j * m;
       double* dst = A + (size_t)j * lda;
       for (int i = lane; i < m; i += 32) {
-        double v = src[i];
+        double v = __ldcs(src + i);
         dst[i] = v;
         am.push(v, pack_key(i, j));
         unsigned long long b = abs_bits(v);
@@ -1503,19 +1531,30 @@ __device__ void run_task(const tci_task& T, const char* blob, char* resb, char* 
   }
 }
 
+// cta_area: the global scratch of each CTA (cta_stride doubles apiece), reused
+// by the CTA's successive tasks: the working matrix of a task too large for
+// shared memory, then its per-task f tables (the host sized the stride for the
+// largest task).
 __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     tci_step_kernel(const char* __restrict__ blob, char* __restrict__ resb, const int* __restrict__ order,
-                    int ntasks, int* counter, size_t smem_bytes) {
+                    int ntasks, int* counter, size_t smem_bytes, double* cta_area, size_t cta_stride) {
   extern __shared__ __align__(16) char smem[];
   __shared__ Ctl ctl;
   const tci_task* tasks = (const tci_task*)blob;
+  double* const area = cta_area + (size_t)blockIdx.x * cta_stride;
   for (;;) {
     if (threadIdx.x == 0) ctl.task = atomicAdd(counter, 1);
     __syncthreads();
     const int ti = ctl.task;
     __syncthreads();
     if (ti >= ntasks) break;
-    const tci_task T = tasks[order[ti]];
+    tci_task T = tasks[order[ti]];
+    size_t we = 0;
+    if (!T.smem_mode) {
+      we = T.kind == TCI_TASK_RRLU ? (size_t)T.m * T.n : (T.kind == TCI_TASK_SITE ? (size_t)T.r * T.r : 0);
+      T.work = area;
+    }
+    if (!T.lut_full) T.lut = T.lutcap0 > 0 ? area + we : nullptr;
     const long long t0 = clock64();
     run_task(T, blob, resb, smem, ctl, smem_bytes);
     if (threadIdx.x == 0) ((tci_result_head*)(atw(resb, T.res)))->cycles = clock64() - t0;
@@ -2314,22 +2353,22 @@ cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_reside
 
 // Launch one step.  counter must be zero (the launcher clears it on the stream).
 cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
-                            int* counter_dev, int grid, cudaStream_t stream) {
+                            int* counter_dev, int grid, double* cta_area, size_t cta_stride, cudaStream_t stream) {
   cudaError_t e = cudaMemsetAsync(counter_dev, 0, sizeof(int), stream);
   if (e != cudaSuccess) return e;
   tci_step_kernel<<<grid, NT, tci_step_smem_bytes(), stream>>>(blob_dev, res_dev, order_dev, ntasks,
-                                                              counter_dev, tci_step_smem_bytes());
+                                                              counter_dev, tci_step_smem_bytes(), cta_area,
+                                                              cta_stride);
   return cudaGetLastError();
 }
 
 // ===================================================================== rrLU
 // without allocation (tci_rrlu_noalloc; no counterpart in the reference).
 //
-// Some callers cannot let the library allocate device memory: code that runs
-// while a stream is being captured into a CUDA graph, latency-critical serving
-// loops where a cudaMalloc/cudaFree would stall the device, and hosts that
-// own every device buffer through their own allocator (a Julia GPU array pool,
-// a framework arena).  This entry point runs the same rank-revealing LU as the
+// Some callers cannot let the library allocate device memory: latency-critical
+// serving loops where a cudaMalloc/cudaFree would stall the device, and hosts
+// that own every device buffer through their own allocator (a Julia GPU array
+// pool, a framework arena).  This entry point runs the same rank-revealing LU as the
 // step kernel's RRLU task on caller-owned device buffers and keeps its working
 // copy of the matrix, the factors and the result record in the fixed array
 // below.  The array lives in every GPU that loads the library until the

@@ -774,7 +774,7 @@ def _value_callback(f):
     return VALUE_FN(_call)
 
 
-def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU", ctx=None, f=None,
+def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method=None, ctx=None, f=None,
              initialpivots=10, precision="fp64", **kwargs):
     """contract(A, B; algorithm, tolerance, maxbonddim) (contraction.jl:515-560) of
     tensor trains with 4-leg cores (A's third leg against B's second), or of a
@@ -783,7 +783,10 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     `initialpivots` a count of random starts or a list of fused 1-based
     pivots, and crossinterpolate2 keywords in kwargs), "naive" or "zipup";
     factorizations use the rank-revealing LU (method "LU") or MatrixLUCI over it
-    (method "CI") -- the reference's SVD is not on the device.  precision
+    (method "CI").  The reference factorizes these two algorithms with
+    LinearAlgebra.svd (contraction.jl:369, :446), which is not on the device:
+    without an explicit method, an algorithm that factorizes (zipup, or naive
+    with truncation) raises instead of silently giving different factors.  precision
     "tf32x3" (zipup) runs the site contractions as TF32 hi/lo split products on
     the tensor cores; the result's `err_est` is the largest relative error of
     those products against FP64 at sampled entries.  Returns a TensorTrain."""
@@ -797,12 +800,21 @@ def contract(A, B, algorithm="TCI", tolerance=1e-12, maxbonddim=None, method="LU
     alg = {"naive": TCI_CONTRACT_NAIVE, "zipup": TCI_CONTRACT_ZIPUP}.get(algorithm)
     if alg is None:
         raise ArgumentError(TCI_ERR_ARG, f"Unknown algorithm {algorithm}.")
-    if method not in FACTORIZE:
+    if method not in FACTORIZE and method is not None:
         raise TCIError(TCI_ERR_GENERIC, f"method=:{method} is not available on the device (:LU, :CI)")
     a, a3 = _as_tt4(A, True)
     b, b3 = _as_tt4(B, False)
     if len(a) != len(b):
         raise ArgumentError(TCI_ERR_ARG, "Cannot contract tensor trains with different length.")
+    for n, (x, y) in enumerate(zip(a, b)):  # contraction.jl:43-46
+        if np.shape(x)[2] != np.shape(y)[1]:
+            raise TCIError(TCI_ERR_GENERIC, f"Tensor trains must share the identical index at n={n + 1}!")
+    if method is None:
+        if alg == TCI_CONTRACT_ZIPUP or tolerance > 0 or maxbonddim:
+            raise TCIError(TCI_ERR_GENERIC, f"contract(algorithm=:{algorithm}) factorizes with :SVD in the reference "
+                           "(contraction.jl:369, :446), which is not on the device: pass method='LU' or "
+                           "method='CI'")
+        method = "LU"  # nothing is factorized
     ctx = ctx or default_context()
     a, ad, ap = _tt4_args(a)
     b, bd, bp = _tt4_args(b)

@@ -1,7 +1,7 @@
 """Argument checks of the Python mirror that run before any device work, with the
 reference's exception types (no GPU): optimize!'s tolerance / pivottolerance rules
 (tensorci2.jl:724-741, test/test_tensorci2.jl:234-245), contract's algorithm and
-f rules (contraction.jl:515-545), compress!/_factorize methods
+f rules (contraction.jl:515-545) and its SVD default, compress!/_factorize methods
 (tensortrain.jl:94-137), sweep directions (tensorci2.jl:402-411) and pivot shapes
 (tensorci2.jl:197-199)."""
 import numpy as np
@@ -40,6 +40,15 @@ def test_contract_rules(T):
         T.contract(a, a[:1])  # algorithm=:TCI, contraction.jl:406-408
     with pytest.raises(T.ArgumentError, match="3 or all have 4 legs"):
         T.compress([np.zeros((1, 2, 1)), np.zeros((1, 2, 2, 1))])
+    # the reference factorizes zipup and truncated naive contractions with SVD
+    # (contraction.jl:369, :446): without an explicit method the call says so
+    with pytest.raises(T.TCIError, match="SVD"):
+        T.contract(a, a, algorithm="zipup")
+    with pytest.raises(T.TCIError, match="SVD"):
+        T.contract(a, a, algorithm="naive", tolerance=1e-10)
+    b = [rng.standard_normal((1, 3, 2, 1)), rng.standard_normal((1, 3, 2, 1))]
+    with pytest.raises(T.TCIError, match="identical index"):
+        T.contract(a, b, algorithm="zipup")
 
 
 def test_pivot_shapes(T):

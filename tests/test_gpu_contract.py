@@ -26,7 +26,7 @@ def test_mpo_mpo_bitwise(T, oracle, algorithm):
     rng = np.random.default_rng(11)
     a = _rand_tt(rng, [1, 2, 3, 2, 1], [2] * 4, [3] * 4)
     b = _rand_tt(rng, [1, 2, 3, 2, 1], [3] * 4, [2] * 4)
-    ab = T.contract(a, b, algorithm=algorithm, tolerance=1e-12)
+    ab = T.contract(a, b, algorithm=algorithm, tolerance=1e-12, method="LU")
     _same(ab, oracle.tt4_contract(a, b, algorithm, tolerance=1e-12))
     ref = oracle.tt4_full(a) @ oracle.tt4_full(b)
     assert np.allclose(oracle.tt4_full(ab.sitetensors), ref, rtol=1e-10, atol=1e-12 * np.abs(ref).max())
@@ -37,7 +37,7 @@ def test_zipup_truncation_bitwise(T, oracle, tol, maxbond):
     rng = np.random.default_rng(12)
     a = _rand_tt(rng, [1, 4, 6, 6, 4, 1], [2] * 5, [3] * 5)
     b = _rand_tt(rng, [1, 3, 5, 5, 3, 1], [3] * 5, [2] * 5)
-    ab = T.contract(a, b, algorithm="zipup", tolerance=tol, maxbonddim=maxbond)
+    ab = T.contract(a, b, algorithm="zipup", tolerance=tol, maxbonddim=maxbond, method="LU")
     _same(ab, oracle.tt4_contract(a, b, "zipup", tolerance=tol, maxbonddim=maxbond))
     if maxbond:
         assert max(c.shape[3] for c in ab.sitetensors) <= maxbond
@@ -47,7 +47,7 @@ def test_naive_with_compression_bitwise(T, oracle):
     rng = np.random.default_rng(13)
     a = _rand_tt(rng, [1, 4, 6, 6, 4, 1], [2] * 5, [2] * 5)
     b = _rand_tt(rng, [1, 3, 5, 5, 3, 1], [2] * 5, [2] * 5)
-    ab = T.contract(a, b, algorithm="naive", tolerance=1e-10)
+    ab = T.contract(a, b, algorithm="naive", tolerance=1e-10, method="LU")
     _same(ab, oracle.tt4_contract(a, b, "naive", tolerance=1e-10))
     assert [c.shape[3] for c in ab.sitetensors[:-1]] == [4, 16, 16, 4]
 
@@ -66,7 +66,7 @@ def test_mpo_mps(T, oracle, algorithm):
     rng = np.random.default_rng(15)
     a = _rand_tt(rng, [1, 2, 3, 2, 1], [3] * 4, [3] * 4)
     v = [rng.standard_normal((r0, 3, r1)) for r0, r1 in zip([1, 2, 3, 2], [2, 3, 2, 1])]
-    ab = T.contract(a, T.TensorTrain(v), algorithm=algorithm, tolerance=1e-12)
+    ab = T.contract(a, T.TensorTrain(v), algorithm=algorithm, tolerance=1e-12, method="LU")
     assert all(c.ndim == 3 for c in ab.sitetensors)
     v4 = [c.reshape(c.shape[0], 3, 1, c.shape[2], order="F") for c in v]
     ref = (oracle.tt4_full(a) @ oracle.tt4_full(v4))[:, 0]
@@ -81,7 +81,7 @@ def test_contract_with_tci_result(T, oracle):
     tci, _, _ = T.crossinterpolate2(float, T.DeviceFunction("qtt2d"), [4] * 6, tolerance=1e-9, maxbonddim=64)
     bonds = [1, 3, 3, 3, 3, 3, 1]
     op = [rng.standard_normal((bonds[i], 4, 4, bonds[i + 1])) / 2.0 for i in range(6)]
-    ab = T.contract(op, tci, algorithm="zipup", tolerance=1e-12)
+    ab = T.contract(op, tci, algorithm="zipup", tolerance=1e-12, method="LU")
     v4 = [c.reshape(c.shape[0], 4, 1, c.shape[2], order="F") for c in tci.sitetensors]
     ref = (oracle.tt4_full(op) @ oracle.tt4_full(v4))[:, 0]
     got = oracle.tt4_full([c.reshape(c.shape[0], c.shape[1], 1, c.shape[2], order="F") for c in ab.sitetensors])

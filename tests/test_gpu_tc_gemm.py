@@ -86,8 +86,9 @@ def test_zipup_split_mpo_mps_wide_bonds(T, oracle):
     L = 6
     op = [rng.standard_normal((r0, 4, 4, r1)) / 4.0 for r0, r1 in zip([1] + [16] * (L - 1), [16] * (L - 1) + [1])]
     v = [rng.standard_normal((r0, 4, r1)) / 3.5 for r0, r1 in zip([1] + [12] * (L - 1), [12] * (L - 1) + [1])]
-    tt_s = T.contract(op, T.TensorTrain(v), algorithm="zipup", tolerance=1e-14, maxbonddim=4096, precision="tf32x3")
-    tt_d = T.contract(op, T.TensorTrain(v), algorithm="zipup", tolerance=1e-14, maxbonddim=4096)
+    tt_s = T.contract(op, T.TensorTrain(v), algorithm="zipup", tolerance=1e-14, maxbonddim=4096, precision="tf32x3",
+                      method="LU")
+    tt_d = T.contract(op, T.TensorTrain(v), algorithm="zipup", tolerance=1e-14, maxbonddim=4096, method="LU")
     pts = rng.integers(1, 5, size=(2000, L))
     ys = tt_s.evaluate(pts)
     yd = tt_d.evaluate(pts)
