@@ -97,6 +97,22 @@ def oracle_solve(reqs, cores):
 SERVED_F_OPS = 39
 
 
+def served_ops(st):
+    """FP64 operations of a served batch from the engine's counters: the rank-1
+    updates (multiply + subtract), f from tables (one operation per element) and
+    f evaluated directly."""
+    return (2.0 * st["lu_updates"] + 1.0 * st["feval_tabulated"] +
+            SERVED_F_OPS * (st["feval"] - st["feval_tabulated"]))
+
+
+# DRAM bytes (read + write) per FP64 operation of the served task code: the sum of
+# dram__bytes_read.sum + dram__bytes_write.sum over all 1181 tci_step_kernel
+# launches of one 512-request served batch run as batched launches (TCI_RESIDENT=0):
+# 843.7 MB read + 3.3 MB written for 6.355e9 served_ops.  The resident kernel runs
+# the same task code.
+SERVED_DRAM_BYTES_PER_OP = 847.04e6 / 6.3547e9
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -598,6 +614,16 @@ def main():
     if args.only == "single":  # the single-solve configurations alone
         print(json.dumps(single_solve_configs(T, ctx, with_cpu=not args.no_cpu)))
         return
+    if args.only == "served-step":  # one served batch (the first timed step's list), nothing else
+        reqs = make_requests(args.batch, seed=step_seed(args.warmup, rank))
+        specs = [(T.DeviceFunction("served", r[2]), [r[1]] * r[0], dict(tolerance=r[3], maxbonddim=r[4]))
+                 for r in reqs]
+        ctx.stats(reset=True)
+        T.crossinterpolate2_batched(specs, max_live=args.live, ctx=ctx)
+        st = ctx.stats(reset=True)
+        print(json.dumps({"requests": len(specs), "fp64_ops": served_ops(st), "launches": st["launches"],
+                          "kernel_ms": st["kernel_ms"]}))
+        return
 
     def specs_for(step, tol_range=(-10.0, -6.0)):
         reqs = make_requests(args.batch, seed=step_seed(step, rank), tol_range=tol_range)
@@ -675,10 +701,7 @@ def main():
     total_dev_s, total_e2e_s = max_over_ranks([total_dev_s, sum(e2e_s)], dist)
     value = nsolves * world / total_dev_s
     e2e = nsolves * world / total_e2e_s
-    # FP64 operations: the rank-1 updates (multiply + subtract), f from tables
-    # (one operation per element) and f evaluated directly
-    ops = (2.0 * st["lu_updates"] + 1.0 * st["feval_tabulated"] +
-           SERVED_F_OPS * (st["feval"] - st["feval_tabulated"]))
+    ops = served_ops(st)
     # FP64 rate of the dominant kernel: the resident kernel's own lifetime
     # (CUDA events around each launch on its stream; one launch per batch)
     kern_s = kernel_ms / 1e3 if kernel_ms > 0 else total_dev_s
@@ -781,7 +804,11 @@ def main():
         "autotune": tune,
         "parity_sample": parity,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak if peak else None, "traffic": None,
+                     "frac": achieved / peak if peak else None,
+                     "traffic": (SERVED_DRAM_BYTES_PER_OP * ops / args.steps
+                                 if SERVED_DRAM_BYTES_PER_OP is not None else None),
+                     "traffic_unit": "bytes per launch (one resident-kernel launch per step), scaled by FP64 "
+                                     "operations from an ncu capture of the same task code as batched launches",
                      "peak_source": "measured FP64 mul+sub throughput (tci_fp64_peak), this run",
                      "fp64_fused_peak": peak_fma / 1e12},
         "kernel_ms_per_step": kernel_ms / args.steps,
