@@ -326,12 +326,17 @@ int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64_t maxrank,
  * barriers per pivot).  tci_autotune_rrlu picks T per (rows, cols) bucket
  * (12 buckets: the smaller dimension in <= 24, <= 48, <= 96, <= 160, <= 256,
  * > 256, times square-ish or more than 2:1) by timing the candidates
- * {1, 96, 192, 320, 512, 768, 1024, 1536} on seeded matrices of each bucket
- * (U diag(10^(-k/4)) V^T + 1e-12 noise, one per SM, reltol 1e-10), reps timed
- * runs each after one warm-up, with CUDA events around the step kernel; every
- * later rrLU and TCI task of the context uses the table.  *speedup = the sum of
- * the default's (T = 192) times over the sum of the best times; ms_default /
- * ms_tuned those sums (any may be NULL).  Pivots do not depend on T. */
+ * {1, 96, 192, 384, 768, 1536} with CUDA events around the step kernel on a
+ * seeded set of each bucket: about three matrices per CTA (at most 24 M
+ * elements), half low rank (U diag(10^(-k/4)) V^T + 1e-12 noise) and half
+ * graded full rank (pivots reaching reltol 1e-10 near 0.9 min(m, n)), one
+ * warm-up launch, then reps launches per candidate, interleaved.  A candidate
+ * replaces the default (T = 192) only if it is 2 % faster on that set and again
+ * on a fresh validation set of the bucket; every later rrLU and TCI task of the
+ * context uses the table.  *speedup = the sum of the default's times over the
+ * sum of the chosen ones (validation times where the choice changed);
+ * ms_default / ms_tuned those sums (any may be NULL).  Pivots do not depend
+ * on T. */
 int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_default, double* ms_tuned);
 /* Read (set = 0) or write (set = 1) the tuned table: nbuckets entries (0 = the
  * kernel's default); *nbuckets receives the count (pass table = NULL to query). */

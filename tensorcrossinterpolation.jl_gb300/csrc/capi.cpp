@@ -1301,7 +1301,15 @@ struct TuneRng {
   }
 };
 
-void tune_matrix(TuneRng& g, int64_t m, int64_t n, std::vector<double>& A) {
+// Calibration matrices of a bucket, two kinds in equal numbers:
+//  - low rank: U diag(10^(-k/4)) V^T + 1e-12 noise, rank <= 48 (a factorization
+//    stops near rank 40 and never reaches a small trailing block unless the
+//    matrix is small);
+//  - graded: u_ij 10^(-(p_i + q_j)/c), u uniform in [-1, 1] and p, q random
+//    permutations of the rows and columns, c = 0.18 min(m, n): the pivots
+//    decay like 10^(-2k/c) and reach reltol 1e-10 near k = 0.9 min(m, n), so
+//    the factorization ends in the trailing blocks the tail size acts on.
+void tune_matrix_lowrank(TuneRng& g, int64_t m, int64_t n, std::vector<double>& A) {
   const int64_t r = std::min<int64_t>(std::min(m, n), 48);
   std::vector<double> G1((size_t)(m * r)), G2((size_t)(n * r));
   for (auto& x : G1) x = g.normal();
@@ -1317,6 +1325,84 @@ void tune_matrix(TuneRng& g, int64_t m, int64_t n, std::vector<double>& A) {
   for (auto& x : A) x += 1e-12 * g.normal();
 }
 
+void tune_matrix_graded(TuneRng& g, int64_t m, int64_t n, std::vector<double>& A) {
+  const double c = std::max(1.0, 0.18 * (double)std::min(m, n));
+  auto scales = [&](int64_t k) {
+    std::vector<int64_t> p((size_t)k);
+    for (int64_t i = 0; i < k; ++i) p[(size_t)i] = i;
+    for (int64_t i = k - 1; i > 0; --i) std::swap(p[(size_t)i], p[(size_t)(g.next() % (uint64_t)(i + 1))]);
+    std::vector<double> s((size_t)k);
+    for (int64_t i = 0; i < k; ++i) s[(size_t)i] = std::pow(10.0, -(double)p[(size_t)i] / c);
+    return s;
+  };
+  const std::vector<double> rs = scales(m), cs = scales(n);
+  A.resize((size_t)(m * n));
+  for (int64_t j = 0; j < n; ++j)
+    for (int64_t i = 0; i < m; ++i) A[(size_t)(i + m * j)] = (2.0 * g.uniform() - 1.0) * rs[(size_t)i] * cs[(size_t)j];
+}
+
+struct TuneSet {
+  std::vector<std::vector<double>> mats;
+  std::vector<int64_t> ms, ns;
+};
+
+// Seeded calibration set of bucket bk: enough matrices for about three tasks per
+// CTA of the batched launch (capped at 24 M elements, at least one per CTA).
+TuneSet tune_set(int bk, uint64_t seed, int64_t grid) {
+  static const int64_t lo[6] = {8, 25, 49, 97, 161, 257}, hi[6] = {24, 48, 96, 160, 256, 320};
+  const int size = bk / 2, elong = bk % 2;
+  const double mid = 0.5 * (double)(lo[size] + hi[size]);
+  const double avg = mid * mid * (elong ? 3.0 : 1.0);
+  const int64_t nmat = std::max(grid, std::min<int64_t>(3 * grid, (int64_t)(24e6 / avg)));
+  TuneRng g{seed};
+  TuneSet S;
+  S.mats.resize((size_t)nmat);
+  S.ms.resize((size_t)nmat);
+  S.ns.resize((size_t)nmat);
+  for (int64_t q = 0; q < nmat; ++q) {
+    const int64_t s0 = lo[size] + (int64_t)(g.uniform() * (double)(hi[size] - lo[size] + 1));
+    int64_t m = s0, n = s0;
+    if (elong) {
+      if (q & 2)
+        n = 3 * s0;
+      else
+        m = 3 * s0;
+    }
+    S.ms[(size_t)q] = m;
+    S.ns[(size_t)q] = n;
+    if (q & 1)
+      tune_matrix_lowrank(g, m, n, S.mats[(size_t)q]);
+    else
+      tune_matrix_graded(g, m, n, S.mats[(size_t)q]);
+  }
+  return S;
+}
+
+// Kernel milliseconds of one batched launch of the set's factorizations with
+// tail size c (CUDA events around the step kernel).
+int tune_time(Engine& e, const TuneSet& S, int32_t c, double& ms) {
+  const size_t nmat = S.mats.size();
+  std::vector<Req> rs(nmat);
+  std::vector<Req*> ptrs;
+  for (size_t q = 0; q < nmat; ++q) {
+    Req& r = rs[q];
+    r.t.kind = TCI_TASK_RRLU;
+    r.t.m = (int32_t)S.ms[q];
+    r.t.n = (int32_t)S.ns[q];
+    r.t.maxrank = r.t.kcap = (int32_t)std::min(S.ms[q], S.ns[q]);
+    r.t.reltol = 1e-10;
+    r.t.leftorth = 1;
+    r.t.post = TCI_POST_NONE;
+    r.t.tail_elems = c;
+    r.ain_host = S.mats[q].data();
+    ptrs.push_back(&r);
+  }
+  const double k0 = e.stats.kernel_ms;
+  const int rc = e.run_tasks(ptrs);
+  ms = e.stats.kernel_ms - k0;
+  return rc;
+}
+
 }  // namespace
 
 int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_default, double* ms_tuned) {
@@ -1326,73 +1412,63 @@ int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_de
     if (rc) return rc;
   }
   Engine& e = ctx->eng_ref();
-  const int32_t cands[] = {1, 96, 192, 320, 512, 768, 1024, 1536};
+  const int32_t cands[] = {1, 96, 192, 384, 768, 1536};
   const int32_t dflt = 192;
-  // bucket size ranges (the smaller dimension) as in Engine::tune_bucket
-  const int64_t lo[6] = {8, 25, 49, 97, 161, 257}, hi[6] = {24, 48, 96, 160, 256, 320};
+  // a candidate replaces the default only if it is this much faster on the
+  // calibration set and again on a fresh validation set
+  const double margin = 0.98;
   reps = std::max(1, reps);
+  const int64_t grid = (int64_t)e.num_sms * TCI_CTAS_PER_SM;
   double tot_def = 0.0, tot_best = 0.0;
   int32_t table[Engine::TUNE_BUCKETS];
   const bool timing = e.timing;
   e.timing = true;
-  for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) {
-    const int size = bk / 2, elong = bk % 2;
-    TuneRng g{0x7a11ULL + (uint64_t)bk};
-    const int64_t nmat = (int64_t)e.num_sms;
-    std::vector<std::vector<double>> mats((size_t)nmat);
-    std::vector<int64_t> ms((size_t)nmat), ns((size_t)nmat);
-    for (int64_t q = 0; q < nmat; ++q) {
-      const int64_t s0 = lo[size] + (int64_t)(g.uniform() * (double)(hi[size] - lo[size] + 1));
-      int64_t m = s0, n = s0;
-      if (elong) {
-        if (q & 1)
-          n = 3 * s0;
-        else
-          m = 3 * s0;
+  int rc = 0;
+  for (int bk = 0; bk < Engine::TUNE_BUCKETS && !rc; ++bk) {
+    const TuneSet S = tune_set(bk, 0x7a11ULL + (uint64_t)bk, grid);
+    double warm = 0.0;
+    rc = tune_time(e, S, dflt, warm);  // first launch of the set warms up
+    std::vector<double> tmin(sizeof(cands) / sizeof(cands[0]), 1e300);
+    for (int rep = 0; rep < reps && !rc; ++rep)  // candidates interleaved per repetition
+      for (size_t ci = 0; ci < tmin.size() && !rc; ++ci) {
+        double t = 0.0;
+        rc = tune_time(e, S, cands[ci], t);
+        tmin[ci] = std::min(tmin[ci], t);
       }
-      ms[(size_t)q] = m;
-      ns[(size_t)q] = n;
-      tune_matrix(g, m, n, mats[(size_t)q]);
+    if (rc) break;
+    size_t best = 0, idef = 0;
+    for (size_t ci = 0; ci < tmin.size(); ++ci) {
+      if (tmin[ci] < tmin[best]) best = ci;
+      if (cands[ci] == dflt) idef = ci;
     }
-    double best_t = 0.0, def_t = 0.0;
-    int32_t best_c = dflt;
-    for (int32_t c : cands) {
-      double tmin = 1e300;
-      for (int rep = 0; rep < reps + 1; ++rep) {  // first run warms up
-        std::vector<Req> rs((size_t)nmat);
-        std::vector<Req*> ptrs;
-        for (int64_t q = 0; q < nmat; ++q) {
-          Req& r = rs[(size_t)q];
-          r.t.kind = TCI_TASK_RRLU;
-          r.t.m = (int32_t)ms[(size_t)q];
-          r.t.n = (int32_t)ns[(size_t)q];
-          r.t.maxrank = r.t.kcap = (int32_t)std::min(ms[(size_t)q], ns[(size_t)q]);
-          r.t.reltol = 1e-10;
-          r.t.leftorth = 1;
-          r.t.post = TCI_POST_NONE;
-          r.t.tail_elems = c;
-          r.ain_host = mats[(size_t)q].data();
-          ptrs.push_back(&r);
-        }
-        const double k0 = e.stats.kernel_ms;
-        int rc = e.run_tasks(ptrs);
-        if (rc) {
-          e.timing = timing;
-          return rc;
-        }
-        if (rep > 0) tmin = std::min(tmin, e.stats.kernel_ms - k0);
+    int32_t choice = dflt;
+    double t_def = tmin[idef], t_choice = tmin[idef];
+    if (best != idef && tmin[best] < margin * tmin[idef]) {
+      // confirm on a fresh set of the same bucket
+      const TuneSet V = tune_set(bk, 0x5eedULL + (uint64_t)bk, grid);
+      double vd = 1e300, vc = 1e300;
+      rc = tune_time(e, V, dflt, warm);
+      for (int rep = 0; rep < reps && !rc; ++rep) {
+        double t = 0.0;
+        rc = tune_time(e, V, dflt, t);
+        vd = std::min(vd, t);
+        if (!rc) rc = tune_time(e, V, cands[best], t);
+        vc = std::min(vc, t);
       }
-      if (c == dflt) def_t = tmin;
-      if (best_t == 0.0 || tmin < best_t) {
-        best_t = tmin;
-        best_c = c;
+      if (rc) break;
+      t_def = vd;
+      t_choice = vd;
+      if (vc < margin * vd) {
+        choice = cands[best];
+        t_choice = vc;
       }
     }
-    table[bk] = best_c;
-    tot_def += def_t;
-    tot_best += best_t;
+    table[bk] = choice;
+    tot_def += t_def;
+    tot_best += t_choice;
   }
   e.timing = timing;
+  if (rc) return rc;
   for (auto& eng : ctx->pool)
     for (int bk = 0; bk < Engine::TUNE_BUCKETS; ++bk) eng->tail_table[bk] = table[bk];
   if (speedup) *speedup = tot_best > 0 ? tot_def / tot_best : 1.0;

@@ -339,6 +339,36 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
   }
 }
 
+// Shared memory a planned task takes (plan_task's figure for the chosen mode), for
+// the kinds whose inputs the resident kernel may stage into the free top of
+// shared memory; 0 for the others (never staged).  A SITE task takes as many
+// row blocks as fit, so it keeps room for its planned count.
+static size_t staged_plan_bytes(const tci_task& t) {
+  const size_t m = (size_t)t.m, n = (size_t)t.n;
+  switch (t.kind) {
+    case TCI_TASK_RRLU: {
+      size_t rest = a16(m * 4) + a16(n * 4);
+      if (!t.ain) rest += 2 * a16(m * 8) + 2 * a16(n * 8);
+      return t.smem_mode ? a16(m * n * 8) + rest : rest + a16((m + n) * 8);
+    }
+    case TCI_TASK_SITE: {
+      const size_t r = (size_t)t.r;
+      const size_t rest = 2 * a16(r * 4) + 5 * a16(r * 8) + 2 * a16(m * 8);
+      const size_t want_rows = std::min<size_t>(std::max<size_t>(m, 1), 64);
+      return t.smem_mode ? a16(r * r * 8) + rest + want_rows * (r * 8 + 8) : rest + 8 * (r * 8 + 8);
+    }
+    case TCI_TASK_CORE:
+      return 2 * a16(m * 8) + 2 * a16(n * 8);
+    case TCI_TASK_SEARCH:
+      return a16((size_t)3 * (t.L + 1) * 4) + (size_t)t.n * 8;
+    default:
+      return 0;
+  }
+}
+
+// Inputs larger than this are read from the host record in place.
+static constexpr size_t STAGE_MAX_BYTES = 64 * 1024;
+
 static size_t result_bytes(const tci_task& t) {
   size_t h = sizeof(tci_result_head);
   switch (t.kind) {
@@ -808,6 +838,10 @@ int Engine::submit() {
   batch.swap(pending_);
   std::vector<Waiter> ws;
   ws.swap(waiters_);
+  // Staging shortens one task's critical path by a host round trip per dependent
+  // read; with many tasks in flight those reads already overlap other tasks'
+  // work and the copy would only add to each task, so stage in latency mode only.
+  const bool latency_mode = inflight_tasks_ + batch.size() < (size_t)num_sms;
   for (auto& w : ws) {
     Flight f;
     f.w = w;
@@ -875,6 +909,14 @@ int Engine::submit() {
         if (lut) t.lut = d + we;
       }
       t.cost = task_cost(t);
+      // small inputs are copied to shared memory in one parallel pass when the
+      // task starts: the task code then reads them on chip instead of making
+      // dependent round trips to host memory
+      t.stage_bytes = 0;
+      if (latency_mode && o_params == 0 && o_res > 0 && o_res <= STAGE_MAX_BYTES) {
+        const size_t plan = staged_plan_bytes(t);
+        if (plan > 0 && plan + o_res <= res_smem_) t.stage_bytes = (int32_t)o_res;
+      }
       stats.h2d_bytes += (int64_t)o_res;
       stats.d2h_bytes += (int64_t)r.res_bytes;
       rc = rq_->publish(t, r.ticket);
@@ -883,6 +925,7 @@ int Engine::submit() {
     if (rc) {
       if (!f.reqs.empty()) {  // some tasks are out: keep the blocks until they finish, then fail
         f.w.op->status = rc;
+        inflight_tasks_ += f.reqs.size();
         flights_.push_back(std::move(f));
         continue;
       }
@@ -892,6 +935,7 @@ int Engine::submit() {
       w.h.resume();  // whatever it enqueues is submitted on the next call
       continue;
     }
+    inflight_tasks_ += f.reqs.size();
     flights_.push_back(std::move(f));
   }
   return 0;
@@ -903,6 +947,7 @@ void Engine::abandon() {
     for (void* p : f.dblocks) spool_->free(p);
   }
   flights_.clear();
+  inflight_tasks_ = 0;
   pending_.clear();
   waiters_.clear();
 }
@@ -926,6 +971,7 @@ int Engine::poll(bool& progressed) {
     Flight g = std::move(f);
     if (i + 1 != flights_.size()) flights_[i] = std::move(flights_.back());
     flights_.pop_back();
+    inflight_tasks_ -= g.reqs.size();
     stats.tasks += (int64_t)g.reqs.size();
     for (Req* r : g.reqs) account(*r, r->t.smem_mode);
     const int status = g.w.op->status;  // nonzero: a task of this op could not be submitted

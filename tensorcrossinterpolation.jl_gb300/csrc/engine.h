@@ -334,6 +334,7 @@ class Engine {
   BlockPool* dpool_ = nullptr;
   size_t res_smem_ = 0;
   std::vector<Flight> flights_;
+  size_t inflight_tasks_ = 0;  // tasks of flights_
   std::vector<char> big_res_;  // host copy of the last multi-CTA rrLU's result record
   cudaStream_t stream_ = nullptr;
   cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;

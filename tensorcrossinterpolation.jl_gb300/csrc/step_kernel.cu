@@ -1713,6 +1713,45 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     if (tid < TASK_WORDS) ((uint64_t*)&Ts)[tid] = ((const volatile uint64_t*)&d->t)[tid];
     __syncthreads();
     if (tid == 0) st_release_gpu(&d->taken, (uint64_t)ticket + 1);
+    const long long t0 = clock64();
+    size_t task_smem = smem_bytes;
+    if (Ts.stage_bytes > 0) {
+      // The record's input part (params, index lists, core table; 16-byte
+      // multiple, 256-byte aligned block) to the top of shared memory, with
+      // every thread's loads issued before its stores; pointers into it are
+      // moved to the copy.
+      const size_t sb = (size_t)Ts.stage_bytes;
+      const char* base = (const char*)(uintptr_t)Ts.params;
+      char* dst = smem + (smem_bytes - sb);
+      const uint4* s4 = (const uint4*)base;
+      uint4* d4 = (uint4*)dst;
+      const int n4 = (int)(sb / 16);
+      for (int k0 = tid; k0 < n4; k0 += 4 * NT) {
+        uint4 v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k0 + q * NT < n4) v[q] = s4[k0 + q * NT];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (k0 + q * NT < n4) d4[k0 + q * NT] = v[q];
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const uintptr_t lo = (uintptr_t)base, hi = lo + sb;
+        auto move = [&](int64_t p) -> int64_t {
+          const uintptr_t q = (uintptr_t)p;
+          return (q >= lo && q < hi) ? (int64_t)(uintptr_t)(dst + (q - lo)) : p;
+        };
+        Ts.params = move(Ts.params);
+        Ts.rows = move(Ts.rows);
+        Ts.cols = move(Ts.cols);
+        Ts.prows = move(Ts.prows);
+        Ts.cores = move(Ts.cores);
+        Ts.ain = (const double*)(uintptr_t)move((int64_t)(uintptr_t)Ts.ain);
+      }
+      task_smem = smem_bytes - sb;
+      __syncthreads();
+    }
     if (Ts.nparams <= RES_MAX_PARAMS) {  // f parameters are read per element: keep them on chip
       const double* src = (const double*)(uintptr_t)Ts.params;
       for (int k = tid; k < Ts.nparams; k += NT) s_params[k] = src[k];
@@ -1720,8 +1759,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     __syncthreads();
     if (tid == 0 && Ts.nparams <= RES_MAX_PARAMS) Ts.params = (int64_t)(uintptr_t)s_params;
     __syncthreads();
-    const long long t0 = clock64();
-    run_task(Ts, nullptr, nullptr, smem, ctl, smem_bytes);
+    run_task(Ts, nullptr, nullptr, smem, ctl, task_smem);
     __syncthreads();
     if (tid == 0) {
       tci_result_head* h = (tci_result_head*)(uintptr_t)Ts.res;

@@ -67,7 +67,9 @@ typedef struct tci_task {
   int32_t lut_base0;           // the integer sum at table0[0] (table1 starts at 0)
   int32_t tail_elems;          // RRLU: trailing blocks of at most this many elements finish on one
                                // warp (0: the kernel's default); set from the autotuned table
-  int32_t pad_tail;
+  int32_t stage_bytes;         // resident mode: the first stage_bytes of the task's host record (its
+                               // inputs, starting at params) are copied to the top of shared memory
+                               // before the task runs (0: read in place)
 } tci_task;
 
 // Result record: fixed header followed by per-task arrays.

@@ -7,7 +7,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-CANDIDATES = {1, 96, 192, 320, 512, 768, 1024, 1536}
+CANDIDATES = {1, 96, 192, 384, 768, 1536}
 
 
 def test_autotune_table_and_identical_results(T, oracle):
