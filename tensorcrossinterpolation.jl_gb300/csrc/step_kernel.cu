@@ -1792,7 +1792,8 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
 
 struct BigBar {
   unsigned int count, gen;
-  int error, pad;
+  int error;
+  unsigned int arrived;  // partials published so far (G per pivot step; never reset)
 };
 struct BigPartial {
   unsigned long long A, B;
@@ -1858,6 +1859,9 @@ __device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
+}
+__device__ __forceinline__ void red_release_gpu_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 constexpr long long BIG_BAR_POLLS = 1LL << 24;  // bounded wait of one grid barrier (a few seconds)
@@ -1947,6 +1951,136 @@ __device__ void block_track(BigTrack& t, Ctl& ctl) {
   __syncthreads();
 }
 
+// Block reduction of every thread's BigTrack into thread 0's (the others keep
+// partial values).  One CTA barrier; the caller's next barrier orders the reuse
+// of the staging slots.
+__device__ void block_track_to0(BigTrack& t, Ctl& ctl) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t a = t.A, b = t.B;
+  uint32_t kk = t.k, ph = t.ph;
+  double v = t.v;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
+    const double v2 = __shfl_down_sync(FULL, v, off);
+    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
+  }
+  if (lane == 0) {
+    ctl.red_u[warp] = a;
+    ctl.red_b[warp] = b;
+    ctl.red_k[warp] = (int)kk;
+    ctl.red_p[warp] = ph;
+    ctl.red_s[warp] = v;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < NW ? ctl.red_u[lane] : 0ULL;
+    b = lane < NW ? ctl.red_b[lane] : 0ULL;
+    kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+    ph = lane < NW ? ctl.red_p[lane] : 0u;
+    v = lane < NW ? ctl.red_s[lane] : 0.0;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+      const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+      const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
+      const double v2 = __shfl_down_sync(FULL, v, off);
+      big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
+    }
+    t.A = a;
+    t.B = b;
+    t.k = kk;
+    t.ph = ph;
+    t.v = v;
+  }
+}
+
+// Publish this CTA's partial (one thread, after a CTA barrier that follows the
+// CTA's update): the fields, then one arrival on the grid's counter with release
+// semantics (cumulative: it also covers the other threads' update writes, which
+// the CTA barrier ordered before it), so that a CTA that sees the count with
+// acquire also sees the partial and the update.  The arrival is a reduction (no
+// round trip).
+__device__ __forceinline__ void big_publish(BigPartial& o, const BigTrack& t, BigBar* bar) {
+  o.A = t.A;
+  o.B = t.B;
+  o.k = t.k;
+  o.ph = t.ph;
+  o.v = t.v;
+  red_release_gpu_add_u32(&bar->arrived, 1u);
+}
+
+// Most partials one lane of the gathering warp handles (grids of up to 160 CTAs).
+constexpr int BIG_GATHER_Q = 5;
+
+// Warp 0: wait until `target` partials have arrived in all (lane 0 polls the
+// counter, bounded), then combine the G partials of this step, every lane
+// loading its share at once; every lane gets the result.  This wait is the pivot
+// step's only grid-wide synchronisation: a CTA publishes after its update, so
+// once all G are in, every update of the step is done and visible.  Returns
+// false if the wait hit its bound or another CTA has flagged an error (the flag
+// is then set).
+__device__ bool big_gather(const BigPartial* cur, int G, unsigned target, BigBar* bar, BigTrack& g) {
+  const int lane = threadIdx.x & 31;
+  g.init();
+  int ok = 1;
+  if (lane == 0) {
+    unsigned sleep_ns = 16;
+    for (long long it = 0; ld_acquire_gpu_u32(&bar->arrived) < target; ++it) {
+      if (it > BIG_BAR_POLLS || *(volatile int*)&bar->error) {
+        atomicExch(&bar->error, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(sleep_ns);
+      sleep_ns = sleep_ns < 64 ? sleep_ns * 2 : 64;
+    }
+  }
+  ok = __shfl_sync(FULL, ok, 0);
+  __syncwarp();  // lane 0's acquire orders the warp's loads below
+  if (ok) {
+    uint64_t qa[BIG_GATHER_Q], qb[BIG_GATHER_Q];
+    uint32_t qk[BIG_GATHER_Q], qp[BIG_GATHER_Q];
+    double qv[BIG_GATHER_Q];
+#pragma unroll
+    for (int q = 0; q < BIG_GATHER_Q; ++q) {
+      if (lane + 32 * q < G) {
+        const BigPartial* p = cur + lane + 32 * q;
+        qa[q] = __ldcg(&p->A);
+        qb[q] = __ldcg(&p->B);
+        qk[q] = __ldcg(&p->k);
+        qp[q] = __ldcg(&p->ph);
+        qv[q] = __ldcg(&p->v);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < BIG_GATHER_Q; ++q)
+      if (lane + 32 * q < G) big_combine(g.A, g.k, g.ph, g.B, g.v, qa[q], qk[q], qp[q], qb[q], qv[q]);
+  }
+  uint64_t a = g.A, b = g.B;
+  uint32_t kk = g.k, ph = g.ph;
+  double v = g.v;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
+    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
+    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
+    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
+    const double v2 = __shfl_down_sync(FULL, v, off);
+    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
+  }
+  g.A = __shfl_sync(FULL, a, 0);
+  g.B = __shfl_sync(FULL, b, 0);
+  g.k = __shfl_sync(FULL, kk, 0);
+  g.ph = __shfl_sync(FULL, ph, 0);
+  g.v = __shfl_sync(FULL, v, 0);
+  return ok != 0;
+}
+
 struct BigArgs {
   const double* ain;      // m x n input (column-major)
   double* A;              // m x n working copy (physical positions never change)
@@ -2003,52 +2137,92 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
     }
   }
   block_track(bt, ctl);
-  if (tid == 0) {
-    BigPartial& o = P.parts[b];  // buffer 0: read at pivot 0
-    o.A = bt.A;
-    o.B = bt.B;
-    o.k = bt.k;
-    o.ph = bt.ph;
-    o.v = bt.v;
-  }
-  bool ok = big_barrier(P.bar, G, gen, ctl);
+  if (tid == 0) big_publish(P.parts[b], bt, P.bar);  // buffer 0: read at pivot 0
+  bool ok = true;
   int K = 0;
   tci_result_head* head = (tci_result_head*)P.res;
   const int kcap = P.kcap;
   int* rowp = (int*)(P.res + sizeof(tci_result_head));
   int* colp = (int*)(P.res + sizeof(tci_result_head) + align_up((size_t)kcap * 4, 8));
   double* diag = (double*)(P.res + sizeof(tci_result_head) + 2 * align_up((size_t)kcap * 4, 8));
+  // Decision of pivot step K (every CTA takes the same one), by one thread: the
+  // error, the stopping rule, swaprow!(K, rl) / swapcol!(K, cl) on the maps, and
+  // the pivot row and column leaving this block's active sets.
+  auto decide = [&]() {
+    const unsigned key = (unsigned)ctl.K, ph = (unsigned)ctl.kmax;
+    const int rl = (int)(key & 0xffffu), cl = (int)(key >> 16);
+    const int R = (int)(ph & 0xffffu), Cc = (int)(ph >> 16);
+    const double piv = ctl.piv;
+    const double e = fabs(piv);
+    ctl.err = e;
+    ctl.stop = ((e < P.reltol * ctl.maxerror || e < P.abstol) && K > 0) ? 1 : 0;
+    if (!ctl.stop) {
+      ctl.maxerror = jmax(ctl.maxerror, e);
+      if (b == 0) {
+        diag[K] = e;
+        P.pivs[K] = piv;
+      }
+      // swaprow!(K, rl), swapcol!(K, cl) on the maps
+      const int sr = stor_r[K];
+      stor_r[K] = R;
+      stor_r[rl] = sr;
+      pos_r[R] = K;
+      pos_r[sr] = rl;
+      const int sc = stor_c[K];
+      stor_c[K] = Cc;
+      stor_c[cl] = sc;
+      pos_c[Cc] = K;
+      pos_c[sc] = cl;
+      // the pivot row and column leave this block's active sets
+      if (R >= r0 && R < r1) {
+        const int s = slot_r[R - r0], last = act_r[ctl.r - 1];
+        act_r[s] = last;
+        slot_r[last] = s;
+        ctl.r -= 1;
+      }
+      if (Cc >= c0 && Cc < c1) {
+        const int s = slot_c[Cc - c0], last = act_c[ctl.c - 1];
+        act_c[s] = last;
+        slot_c[last] = s;
+        ctl.c -= 1;
+      }
+    }
+  };
   while (ok) {
     // the partials of pivot K are in buffer K & 1: a CTA writes the next set to
     // the other buffer, so a fast CTA never overwrites what a slow one reads
     BigPartial* const cur = P.parts + (size_t)(K & 1) * G;
     // ---- the pivot: argmax of abs2 over the trailing block, from the G partials
-    {
+    // (warp 0 waits for them); unless the exact pass is needed, lane 0 also takes
+    // the decision
+    if (tid < 32) {
       BigTrack g;
-      g.init();
-      for (int t = tid; t < G; t += NT) {
-        const BigPartial* q = cur + t;
-        big_combine(g.A, g.k, g.ph, g.B, g.v, __ldcg(&q->A), __ldcg(&q->k), __ldcg(&q->ph), __ldcg(&q->B),
-                    __ldcg(&q->v));
-      }
-      block_track(g, ctl);
+      const bool got = big_gather(cur, G, (unsigned)(K + 1) * (unsigned)G, P.bar, g);
       if (tid == 0) {
-        const uint64_t Mstar = g.A ? g.A - 1 : 0;
-        const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
-        const bool close = g.B != 0 && (g.B - 1) + 16 >= Mstar;
-        ctl.red_u[NW] = Mstar;
-        ctl.need_exact = (g.A != 0 && !(safe && !close)) ? 1 : 0;
-        if (g.A == 0) {  // every element NaN: the scan keeps its start
-          ctl.kmax = (int)(((unsigned)stor_c[K] << 16) | (unsigned)stor_r[K]);
-          ctl.K = (K << 16) | K;
-          ctl.piv = __ldcg(&P.A[stor_r[K] + (size_t)stor_c[K] * m]);
-        } else {
-          ctl.kmax = (int)g.ph;
-          ctl.K = (int)g.k;
-          ctl.piv = g.v;
+        ctl.bar_err = got ? 0 : 1;
+        if (got) {
+          const uint64_t Mstar = g.A ? g.A - 1 : 0;
+          const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
+          const bool close = g.B != 0 && (g.B - 1) + 16 >= Mstar;
+          ctl.red_u[NW] = Mstar;
+          ctl.need_exact = (g.A != 0 && !(safe && !close)) ? 1 : 0;
+          if (g.A == 0) {  // every element NaN: the scan keeps its start
+            ctl.kmax = (int)(((unsigned)stor_c[K] << 16) | (unsigned)stor_r[K]);
+            ctl.K = (K << 16) | K;
+            ctl.piv = __ldcg(&P.A[stor_r[K] + (size_t)stor_c[K] * m]);
+          } else {
+            ctl.kmax = (int)g.ph;
+            ctl.K = (int)g.k;
+            ctl.piv = g.v;
+          }
+          if (!ctl.need_exact) decide();
         }
       }
-      __syncthreads();
+    }
+    __syncthreads();
+    if (ctl.bar_err) {
+      ok = false;
+      break;
     }
     if (ctl.need_exact) {  // squares of the elements near the maximum (rare)
       const uint64_t Mstar = ctl.red_u[NW];
@@ -2097,67 +2271,33 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
                     __ldcg(&q->v));
       }
       block_track(g, ctl);
-      if (tid == 0 && g.A) {
-        ctl.kmax = (int)g.ph;
-        ctl.K = (int)g.k;
-        ctl.piv = g.v;
+      if (tid == 0) {
+        if (g.A) {
+          ctl.kmax = (int)g.ph;
+          ctl.K = (int)g.k;
+          ctl.piv = g.v;
+        }
+        decide();
       }
       __syncthreads();
     }
-    // ---- decision (every CTA computes the same); thread 0 updates the maps
-    const unsigned key = (unsigned)ctl.K, ph = (unsigned)ctl.kmax;
-    const int rl = (int)(key & 0xffffu), cl = (int)(key >> 16);
-    const int R = (int)(ph & 0xffffu), Cc = (int)(ph >> 16);
+    const int R = (int)((unsigned)ctl.kmax & 0xffffu), Cc = (int)((unsigned)ctl.kmax >> 16);
     const double piv = ctl.piv;
-    if (tid == 0) {
-      const double e = fabs(piv);
-      ctl.err = e;
-      ctl.stop = ((e < P.reltol * ctl.maxerror || e < P.abstol) && K > 0) ? 1 : 0;
-      if (!ctl.stop) {
-        ctl.maxerror = jmax(ctl.maxerror, e);
-        if (b == 0) {
-          diag[K] = e;
-          P.pivs[K] = piv;
-        }
-        // swaprow!(K, rl), swapcol!(K, cl) on the maps
-        const int sr = stor_r[K];
-        stor_r[K] = R;
-        stor_r[rl] = sr;
-        pos_r[R] = K;
-        pos_r[sr] = rl;
-        const int sc = stor_c[K];
-        stor_c[K] = Cc;
-        stor_c[cl] = sc;
-        pos_c[Cc] = K;
-        pos_c[sc] = cl;
-        // the pivot row and column leave this block's active sets
-        if (R >= r0 && R < r1) {
-          const int s = slot_r[R - r0], last = act_r[ctl.r - 1];
-          act_r[s] = last;
-          slot_r[last] = s;
-          ctl.r -= 1;
-        }
-        if (Cc >= c0 && Cc < c1) {
-          const int s = slot_c[Cc - c0], last = act_c[ctl.c - 1];
-          act_c[s] = last;
-          slot_c[last] = s;
-          ctl.c -= 1;
-        }
-      }
-    }
-    __syncthreads();
     if (ctl.stop) break;
     ++K;
     if (K == P.kmax) break;  // the trailing update after the last pivot is not observable
     // ---- x (pivot column) for the active rows, y (pivot row) for the active columns
+    // (one element per thread: the x and y entries on different threads)
     const int nr = ctl.r, nc = ctl.c;
-    for (int t = tid; t < nr; t += NT) {
-      const double v = __ldcg(&P.A[r0 + act_r[t] + (size_t)Cc * m]);
-      xs[t] = leftorth ? __ddiv_rn(v, piv) : v;
-    }
-    for (int u = tid; u < nc; u += NT) {
-      const double v = __ldcg(&P.A[R + (size_t)(c0 + act_c[u]) * m]);
-      ys[u] = leftorth ? v : __ddiv_rn(v, piv);
+    for (int t = tid; t < nr + nc; t += NT) {
+      if (t < nr) {
+        const double v = __ldcg(&P.A[r0 + act_r[t] + (size_t)Cc * m]);
+        xs[t] = leftorth ? __ddiv_rn(v, piv) : v;
+      } else {
+        const int u = t - nr;
+        const double v = __ldcg(&P.A[R + (size_t)(c0 + act_c[u]) * m]);
+        ys[u] = leftorth ? v : __ddiv_rn(v, piv);
+      }
     }
     __syncthreads();
     // ---- rank-1 update of the block's active part, fused with its argmax.
@@ -2212,16 +2352,10 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
         }
       }
     }
-    block_track(bt, ctl);
-    if (tid == 0) {
-      BigPartial& o = P.parts[(size_t)(K & 1) * G + b];  // read at pivot K (already incremented)
-      o.A = bt.A;
-      o.B = bt.B;
-      o.k = bt.k;
-      o.ph = bt.ph;
-      o.v = bt.v;
-    }
-    ok = big_barrier(P.bar, G, gen, ctl);
+    block_track_to0(bt, ctl);
+    // read at pivot K (already incremented); no grid barrier: the next gather
+    // waits for every CTA's partial
+    if (tid == 0) big_publish(P.parts[(size_t)(K & 1) * G + b], bt, P.bar);
   }
   if (ok) ok = big_barrier(P.bar, G, gen, ctl);  // every pivot value is recorded
   if (!ok) {
@@ -2306,6 +2440,7 @@ struct BigGrid {
   int pr, pc, mb, nb;
 };
 BigGrid big_grid(int64_t m, int64_t n, int G) {
+  G = std::min(G, 32 * BIG_GATHER_Q);  // one gathering warp reads every partial
   BigGrid best{1, 1, (int)m, (int)n};
   double best_score = -1.0;
   for (int pr = 1; pr <= G; ++pr) {
