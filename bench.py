@@ -99,9 +99,11 @@ SERVED_F_OPS = 39
 
 def served_ops(st):
     """FP64 operations of a served batch from the engine's counters: the rank-1
-    updates (multiply + subtract), f from tables (one operation per element) and
+    updates of the factorizations (multiply + subtract), the triangular solves of
+    setsitetensor! and the train contractions of the global pivot search
+    (multiply + add or subtract), f from tables (one operation per element) and
     f evaluated directly."""
-    return (2.0 * st["lu_updates"] + 1.0 * st["feval_tabulated"] +
+    return (2.0 * st["lu_updates"] + 2.0 * st.get("dense_macs", 0) + 1.0 * st["feval_tabulated"] +
             SERVED_F_OPS * (st["feval"] - st["feval_tabulated"]))
 
 

@@ -371,6 +371,10 @@ typedef struct tci_stats {
   /* most solves live at once in a batched or serving run (admission by the
    * live cap and the HBM budget) */
   int64_t peak_live;
+  /* FP64 multiply-add (or multiply-subtract) pairs outside the rank-1 updates:
+   * the triangular solves of setsitetensor! (m r (r - 1) per SITE task) and the
+   * train contractions of the global pivot search and of evaluate */
+  int64_t dense_macs;
 } tci_stats;
 int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset);
 /* Bounds of the resident kernel's waits (no reference counterpart): it leaves

@@ -247,6 +247,7 @@ int tci_ctx_stats(tci_ctx* ctx, tci_stats* out, int32_t reset) {
     t.feval_tabulated += s.feval_tabulated;
     t.tc_ms += s.tc_ms;
     t.tc_flops += s.tc_flops;
+    t.dense_macs += s.dense_macs;
     if (reset) e->stats = tci_stats{};
   }
   t.peak_live = ctx->peak_live;

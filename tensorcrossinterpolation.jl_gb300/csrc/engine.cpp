@@ -584,6 +584,8 @@ void Engine::account(const Req& r, int smem_mode) {
     case TCI_TASK_SITE:
       stats.feval += (int64_t)t.r * t.r + (int64_t)t.m * t.r;
       for (int64_t k = 1; k < t.r; ++k) stats.lu_updates += (int64_t)(t.r - k) * (t.r - k);
+      // forward (unit lower) and backward substitution of every row
+      if (!(h->status & TCI_ST_SINGULAR)) stats.dense_macs += (int64_t)t.m * t.r * (t.r - 1);
       break;
     case TCI_TASK_CORE:
       stats.feval += (int64_t)t.m * t.n;
@@ -591,6 +593,17 @@ void Engine::account(const Req& r, int smem_mode) {
     case TCI_TASK_EVAL:
     case TCI_TASK_SEARCH:
       stats.feval += t.m;
+      if (r.cores) {
+        int64_t chain = 0, items = 0;  // sum of r0 r1 over the sites; sum of d (r0 r1 + r1)
+        for (int p = 0; p < r.ncores; ++p) {
+          const int64_t r0 = r.cores[p].r0, d = r.cores[p].d, r1 = r.cores[p].r1;
+          chain += r0 * r1;
+          items += d * (r0 * r1 + r1);
+        }
+        // EVAL: one left-to-right product per point; SEARCH: the left and right
+        // environments of the start point and the value at every one-site change
+        stats.dense_macs += t.kind == TCI_TASK_EVAL ? (int64_t)t.m * chain : 2 * chain + items;
+      }
       break;
     default:
       break;

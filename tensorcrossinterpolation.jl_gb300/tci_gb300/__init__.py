@@ -104,6 +104,7 @@ class Stats(ctypes.Structure):
         ("tc_ms", ctypes.c_double),
         ("tc_flops", ctypes.c_double),
         ("peak_live", ctypes.c_int64),
+        ("dense_macs", ctypes.c_int64),
     ]
 
 
