@@ -110,9 +110,9 @@ def served_ops(st):
 # DRAM bytes (read + write) per FP64 operation of the served task code: the sum of
 # dram__bytes_read.sum + dram__bytes_write.sum over all 1181 tci_step_kernel
 # launches of one 512-request served batch run as batched launches (TCI_RESIDENT=0):
-# 843.7 MB read + 3.3 MB written for 6.355e9 served_ops.  The resident kernel runs
+# 843.7 MB read + 3.3 MB written for 6.896e9 served_ops.  The resident kernel runs
 # the same task code.
-SERVED_DRAM_BYTES_PER_OP = 847.04e6 / 6.3547e9
+SERVED_DRAM_BYTES_PER_OP = 847.04e6 / 6.8957e9
 
 
 class ClockSampler:
