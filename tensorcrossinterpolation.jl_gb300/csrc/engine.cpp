@@ -331,9 +331,9 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
     case TCI_TASK_TABLE:
       t.smem_mode = 1;
       return t.lut != nullptr;
-    case TCI_TASK_SEARCH:  // t.n = sum of the left and right bond sizes
+    case TCI_TASK_SEARCH:  // t.n = sum of the left and right bond sizes; then the core table
       t.smem_mode = 1;
-      return a16((size_t)3 * (t.L + 1) * 4) + (size_t)t.n * 8 <= smem;
+      return a16((size_t)3 * (t.L + 1) * 4) + a16((size_t)t.n * 8) + (size_t)t.L * sizeof(tci_core_ref) <= smem;
     default:
       return false;
   }
@@ -360,7 +360,7 @@ static size_t staged_plan_bytes(const tci_task& t) {
     case TCI_TASK_CORE:
       return 2 * a16(m * 8) + 2 * a16(n * 8);
     case TCI_TASK_SEARCH:
-      return a16((size_t)3 * (t.L + 1) * 4) + (size_t)t.n * 8;
+      return a16((size_t)3 * (t.L + 1) * 4) + a16((size_t)t.n * 8) + a16((size_t)t.L * sizeof(tci_core_ref));
     default:
       return 0;
   }

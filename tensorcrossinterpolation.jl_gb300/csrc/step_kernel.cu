@@ -550,8 +550,12 @@ __device__ void rr_decide(Ctl& ctl, const double* A, int lda, int K, double relt
 // columns K/C, columns K/C outside rows K/R, and the corners -- and each pair is
 // read and written by one thread.  Ends with a barrier.
 // The body for threads t = 0, stride, ... of a group (no barrier).
+// nan: set when an entry of the new row K (columns >= K) or of the new column K
+// (rows >= K) is NaN -- the entries that join U and L at this pivot.  Every
+// other entry of L and U joined at an earlier pivot (swaps only move them), so
+// the flags of all pivots cover the NaN check of L and U (matrixlu.jl:162-169).
 __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n, int K, int R, int C, double piv,
-                                                bool leftorth, int t, int stride) {
+                                                bool leftorth, int t, int stride, bool& nan) {
   for (int w = t; w < n + m + 1; w += stride) {
     if (w < n) {  // row pair (K, j) <-> (R, j)
       const int j = w;
@@ -559,10 +563,14 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
       double* col = A + (size_t)j * lda;
       if (R != K) {
         const double a = col[K], b = col[R];
-        col[K] = (!leftorth && j > K) ? __ddiv_rn(b, piv) : b;
+        const double v = (!leftorth && j > K) ? __ddiv_rn(b, piv) : b;
+        col[K] = v;
         col[R] = a;
-      } else if (!leftorth && j > K) {
-        col[K] = __ddiv_rn(col[K], piv);
+        if (j > K && v != v) nan = true;
+      } else if (j > K) {
+        const double v = !leftorth ? __ddiv_rn(col[K], piv) : col[K];
+        col[K] = v;
+        if (v != v) nan = true;
       }
     } else if (w < n + m) {  // column pair (i, K) <-> (i, C)
       const int i = w - n;
@@ -571,10 +579,14 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
       if (C != K) {
         double* cc = A + (size_t)C * lda;
         const double a = ck[i], b = cc[i];
-        ck[i] = (leftorth && i > K) ? __ddiv_rn(b, piv) : b;
+        const double v = (leftorth && i > K) ? __ddiv_rn(b, piv) : b;
+        ck[i] = v;
         cc[i] = a;
-      } else if (leftorth && i > K) {
-        ck[i] = __ddiv_rn(ck[i], piv);
+        if (i > K && v != v) nan = true;
+      } else if (i > K) {
+        const double v = leftorth ? __ddiv_rn(ck[i], piv) : ck[i];
+        ck[i] = v;
+        if (v != v) nan = true;
       }
     } else {  // the corners (K, K), (K, C), (R, K), (R, C)
       const int rows[2] = {K, R}, cols[2] = {K, C};
@@ -590,12 +602,14 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
           const int i = rows[p], j = cols[q];
           if ((leftorth && j == K && i > K) || (!leftorth && i == K && j > K)) v = __ddiv_rn(v, piv);
           A[i + (size_t)j * lda] = v;
+          if ((i == K || j == K) && v != v) nan = true;
         }
     }
   }
 }
-__device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C, double piv, bool leftorth) {
-  swap_scale_body(A, lda, m, n, K, R, C, piv, leftorth, threadIdx.x, NT);
+__device__ void swap_scale(double* A, int lda, int m, int n, int K, int R, int C, double piv, bool leftorth,
+                           bool& nan) {
+  swap_scale_body(A, lda, m, n, K, R, C, piv, leftorth, threadIdx.x, NT, nan);
   __syncthreads();
 }
 
@@ -608,10 +622,10 @@ constexpr int WARP_TAIL_RRLU = 192;
 // only; same arithmetic and argmax as the CTA path.  Returns the final K on
 // every lane of warp 0.
 __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax, double reltol, double abstol,
-                              bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl) {
+                              bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl, bool& nan) {
   const int lane = threadIdx.x & 31;
   while (true) {
-    swap_scale_body(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth, lane, 32);
+    swap_scale_body(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth, lane, 32, nan);
     __syncwarp();
     ++K;
     if (K == kmax) break;
@@ -702,12 +716,14 @@ __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax,
 // whose resolving thread also takes the next decision -- three barriers.
 // xy: optional shared-memory copy (m + n doubles) of the pivot column and row
 // for a matrix in global memory, so that each element of the update costs one
-// load and one store.
-__device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
+// load and one store.  Returns this thread's part of the NaN check of L and U
+// (an OR over the CTA gives it).
+__device__ bool rrlu_loop(double* A, int lda, int m, int n, int maxrank, double reltol, double abstol,
                           bool leftorth, int* rowperm, int* colperm, double* diag_out, Ctl& ctl,
                           double* xy = nullptr, int warp_tail = WARP_TAIL_RRLU) {
   const int tid = threadIdx.x;
   const int kmax = min(maxrank, min(m, n));
+  bool nan = false;
   if (tid == 0) {
     ctl.K = 0;
     ctl.maxerror = 0.0;
@@ -725,7 +741,7 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
       tail = true;
       break;
     }
-    swap_scale(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth);
+    swap_scale(A, lda, m, n, K, ctl.r, ctl.c, ctl.piv, leftorth, nan);
     TCI_PHASE(3);
     ++K;
     if (K == kmax) break;  // the trailing update after the last pivot is not observable
@@ -808,27 +824,13 @@ __device__ void rrlu_loop(double* A, int lda, int m, int n, int maxrank, double 
     TCI_PHASE(6);
   }
   if (tail && tid < 32) K = rrlu_warp_tail(A, lda, m, n, K, kmax, reltol, abstol, leftorth, rowperm, colperm,
-                                           diag_out, ctl);
+                                           diag_out, ctl, nan);
   if (tid == 0) {
     ctl.K = K;
     if (K >= min(m, n)) ctl.err = 0.0;
   }
   __syncthreads();
-}
-
-// NaN scan of L = tril(A[:, 1:K]) and U = triu(A[1:K, :]) (matrixlu.jl:162-169).
-__device__ int lu_has_nan(const double* A, int lda, int m, int n, int K, Ctl& ctl) {
-  int bad = 0;
-  for (int j = threadIdx.x >> 5; j < n; j += NW) {
-    const double* col = A + (size_t)j * lda;
-    int i0 = j < K ? j : m;  // L part: rows >= j for j < K
-    for (int i = (threadIdx.x & 31); i < m; i += 32) {
-      bool inL = (j < K) && (i >= i0);
-      bool inU = (i < K) && (i <= j);
-      if ((inL || inU) && col[i] != col[i]) bad = 1;
-    }
-  }
-  return block_or(bad, ctl);
+  return nan;
 }
 
 // left(MatrixLUCI) for leftorthogonal (colstimespivotinv, matrixluci.jl:48-57):
@@ -980,10 +982,12 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   const bool leftorth = T.leftorth != 0;
   double* xy = nullptr;
   if (!T.smem_mode && (size_t)(cur.p - smem) + (size_t)(m + n) * 8 <= smem_bytes) xy = (double*)cur.take((size_t)(m + n) * 8);
-  rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag, ctl, xy,
-            T.tail_elems > 0 ? T.tail_elems : WARP_TAIL_RRLU);
+  const bool nan_part = rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag,
+                                  ctl, xy, T.tail_elems > 0 ? T.tail_elems : WARP_TAIL_RRLU);
   const int K = ctl.K;
-  int nan = lu_has_nan(A, lda, m, n, K, ctl);
+  // NaN check of L = tril(A[:, 1:K]) and U = triu(A[1:K, :]) (matrixlu.jl:162-169),
+  // gathered while the pivots were taken
+  int nan = block_or(nan_part ? 1 : 0, ctl);
   if (T.post == TCI_POST_LEFT && !nan) post_left(A, lda, m, n, K, leftorth, rowperm, T.core_out);
   if (T.post == TCI_POST_RIGHT && !nan) post_right(A, lda, m, n, K, leftorth, colperm, T.core_out);
   if (T.post == TCI_POST_FACTORS)
@@ -1377,7 +1381,6 @@ __device__ void task_search(const tci_task& T, const char* blob, char* resb, cha
   const int L = T.L, tid = threadIdx.x;
   const double* prm = (const double*)at(blob, T.params);
   const uint8_t* st = (const uint8_t*)at(blob, T.rows);
-  const tci_core_ref* cr = (const tci_core_ref*)at(blob, T.cores);
   char* base = atw(resb, T.res);
   double* fout = (double*)(base + sizeof(tci_result_head));
   double* tout = fout + T.m;
@@ -1386,6 +1389,16 @@ __device__ void task_search(const tci_task& T, const char* blob, char* resb, cha
   int* roff = loff + (L + 1);
   int* ioff = roff + (L + 1);  // first item of site p
   double* env = (double*)(smem + align_up((size_t)(3 * (L + 1)) * 4, 16));
+  // the core table on chip: every site step below reads it, and in resident
+  // mode the task's copy is in host memory (one round trip here instead of one
+  // per read)
+  tci_core_ref* cr = (tci_core_ref*)(smem + align_up((size_t)(3 * (L + 1)) * 4, 16) +
+                                     align_up((size_t)T.n * 8, 16));
+  {
+    const tci_core_ref* src = (const tci_core_ref*)at(blob, T.cores);
+    for (int p = tid; p < L; p += NT) cr[p] = src[p];
+  }
+  __syncthreads();
   if (tid == 0) {
     int a = 0, b = 0, c = 0;
     for (int p = 0; p < L; ++p) {

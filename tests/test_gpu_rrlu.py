@@ -183,3 +183,29 @@ def test_multi_cta_nan(T, oracle):
     assert e.value.code == T.TCI_ERR_NAN
     with pytest.raises(oracle.OracleError):
         oracle.rrlu(A)
+
+
+@pytest.mark.parametrize("seed", [99, 100, 101])
+def test_nan_inf_planted(T, oracle, seed):
+    """NaN and +-Inf planted at random positions: the GPU raises "lu.L contains
+    NaNs" exactly when the oracle does (the check is gathered pivot by pivot as
+    the entries join L and U), and otherwise matches it bit for bit."""
+    rng = np.random.default_rng(seed)
+    raised = 0
+    for trial in range(40):
+        m = int(rng.integers(2, 160))
+        n = int(rng.integers(2, 160))
+        A = rng.standard_normal((m, n))
+        for _ in range(int(rng.integers(1, 5))):
+            A[rng.integers(m), rng.integers(n)] = rng.choice([np.nan, np.inf, -np.inf])
+        kw = dict(leftorthogonal=bool(trial % 2), maxrank=int(rng.integers(1, min(m, n) + 1)))
+        try:
+            ref = oracle.rrlu(A, **kw)
+        except oracle.OracleError:
+            raised += 1
+            with pytest.raises(T.TCIError) as e:
+                T.rrlu(A, **kw)
+            assert e.value.code == T.TCI_ERR_NAN
+            continue
+        _same(T.rrlu(A, **kw), ref)
+    assert 0 < raised < 40  # both outcomes occur
