@@ -124,6 +124,30 @@ __device__ __forceinline__ void track_combine(uint64_t& A, uint32_t& k, uint64_t
   }
 }
 
+// Warp-wide versions with the hardware reductions (redux.sync) instead of a
+// shuffle tree; every lane gets the result.  warp_track gives what folding
+// track_combine over the lanes gives in any order: the largest A, the smallest
+// key among the lanes that hold it, and B = the largest value below A held
+// anywhere (a lane below the maximum offers its A, a lane at it its B).
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t x) {
+  const unsigned hi = __reduce_max_sync(FULL, (unsigned)(x >> 32));
+  const unsigned lo = __reduce_max_sync(FULL, (unsigned)(x >> 32) == hi ? (unsigned)x : 0u);
+  return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ void warp_track(uint64_t& A, uint32_t& k, uint64_t& B) {
+  const uint64_t Am = warp_max_u64(A);
+  const uint32_t km = __reduce_min_sync(FULL, A == Am ? k : 0xffffffffu);
+  B = warp_max_u64(A == Am ? B : A);
+  A = Am;
+  k = km;
+}
+// The largest s and the smallest key among the lanes that hold it.
+__device__ __forceinline__ void warp_best(uint64_t& s, uint32_t& key) {
+  const uint64_t sm = warp_max_u64(s);
+  key = __reduce_min_sync(FULL, s == sm ? key : 0xffffffffu);
+  s = sm;
+}
+
 // Exact candidate of the second pass: abs2 = v*v (never NaN here, >= +0), so
 // its bit pattern orders like its value; ties go to the smaller key.
 struct ArgBest {
@@ -153,15 +177,7 @@ __device__ void block_argmax(const ArgBest& a, Ctl& ctl, uint64_t& out_s, uint32
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t s = a.s;
   uint32_t key = a.key;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t os = __shfl_down_sync(FULL, s, off);
-    const uint32_t ok = __shfl_down_sync(FULL, key, off);
-    if (os > s || (os == s && ok < key)) {
-      s = os;
-      key = ok;
-    }
-  }
+  warp_best(s, key);
   if (lane == 0) {
     ctl.red_u[warp] = s;
     ctl.red_k[warp] = (int)key;
@@ -170,15 +186,7 @@ __device__ void block_argmax(const ArgBest& a, Ctl& ctl, uint64_t& out_s, uint32
   if (warp == 0) {
     s = lane < NW ? ctl.red_u[lane] : 0ULL;
     key = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t os = __shfl_down_sync(FULL, s, off);
-      const uint32_t ok = __shfl_down_sync(FULL, key, off);
-      if (os > s || (os == s && ok < key)) {
-        s = os;
-        key = ok;
-      }
-    }
+    warp_best(s, key);
     if (lane == 0) {
       ctl.red_u[NW] = s;
       ctl.red_k[NW] = (int)key;
@@ -258,13 +266,7 @@ __device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t a = t.A, b = t.B;
   uint32_t k = t.k;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-    const uint32_t k2 = __shfl_down_sync(FULL, k, off);
-    track_combine(a, k, b, a2, k2, b2);
-  }
+  warp_track(a, k, b);
   if (lane == 0) {
     ctl.red_u[warp] = a;
     ctl.red_b[warp] = b;
@@ -275,13 +277,7 @@ __device__ void argmax_resolve(const ArgTrack& t, const double* A, int lda, int 
     a = lane < NW ? ctl.red_u[lane] : 0ULL;
     b = lane < NW ? ctl.red_b[lane] : 0ULL;
     k = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-      const uint32_t k2 = __shfl_down_sync(FULL, k, off);
-      track_combine(a, k, b, a2, k2, b2);
-    }
+    warp_track(a, k, b);
     if (lane == 0) {
       const uint64_t Mstar = a ? a - 1 : 0;
       const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
@@ -653,16 +649,7 @@ __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax,
     }
     uint64_t a = at.A, b = at.B;
     uint32_t k = at.k;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-      const uint32_t k2 = __shfl_down_sync(FULL, k, off);
-      track_combine(a, k, b, a2, k2, b2);
-    }
-    a = __shfl_sync(FULL, a, 0);
-    b = __shfl_sync(FULL, b, 0);
-    k = __shfl_sync(FULL, k, 0);
+    warp_track(a, k, b);
     __syncwarp();  // every lane's update is in place before the exact pass / decision
     const uint64_t Mstar = a ? a - 1 : 0;
     const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
@@ -685,17 +672,7 @@ __device__ int rrlu_warp_tail(double* A, int lda, int m, int n, int K, int kmax,
       }
       uint64_t sv = ab.s;
       uint32_t key = ab.key;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const uint64_t os = __shfl_down_sync(FULL, sv, off);
-        const uint32_t ok = __shfl_down_sync(FULL, key, off);
-        if (os > sv || (os == sv && ok < key)) {
-          sv = os;
-          key = ok;
-        }
-      }
-      sv = __shfl_sync(FULL, sv, 0);
-      key = __shfl_sync(FULL, key, 0);
+      warp_best(sv, key);
       r = sv ? (int)(key & 0xffffu) : K;
       c = sv ? (int)(key >> 16) : K;
     }
@@ -1868,6 +1845,20 @@ __device__ __forceinline__ void big_combine(uint64_t& A, uint32_t& k, uint32_t& 
   }
 }
 
+// warp_track with the winner's physical position and value (from the first lane
+// that holds the winning key); every lane gets the result.  Same result as
+// folding big_combine over the lanes.
+__device__ __forceinline__ void warp_track5(uint64_t& A, uint32_t& k, uint32_t& ph, uint64_t& B, double& v) {
+  const uint64_t Am = warp_max_u64(A);
+  const uint32_t km = __reduce_min_sync(FULL, A == Am ? k : 0xffffffffu);
+  const int src = __ffs(__ballot_sync(FULL, A == Am && k == km)) - 1;
+  B = warp_max_u64(A == Am ? B : A);
+  ph = __shfl_sync(FULL, ph, src);
+  v = __shfl_sync(FULL, v, src);
+  A = Am;
+  k = km;
+}
+
 __device__ __forceinline__ unsigned ld_acquire_gpu_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -1915,15 +1906,7 @@ __device__ void block_track(BigTrack& t, Ctl& ctl) {
   uint64_t a = t.A, b = t.B;
   uint32_t kk = t.k, ph = t.ph;
   double v = t.v;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
-    const double v2 = __shfl_down_sync(FULL, v, off);
-    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
-  }
+  warp_track5(a, kk, ph, b, v);
   if (lane == 0) {
     ctl.red_u[warp] = a;
     ctl.red_b[warp] = b;
@@ -1938,15 +1921,7 @@ __device__ void block_track(BigTrack& t, Ctl& ctl) {
     kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
     ph = lane < NW ? ctl.red_p[lane] : 0u;
     v = lane < NW ? ctl.red_s[lane] : 0.0;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-      const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-      const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
-      const double v2 = __shfl_down_sync(FULL, v, off);
-      big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
-    }
+    warp_track5(a, kk, ph, b, v);
     if (lane == 0) {
       ctl.red_u[NW] = a;
       ctl.red_b[NW] = b;
@@ -1972,15 +1947,7 @@ __device__ void block_track_to0(BigTrack& t, Ctl& ctl) {
   uint64_t a = t.A, b = t.B;
   uint32_t kk = t.k, ph = t.ph;
   double v = t.v;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
-    const double v2 = __shfl_down_sync(FULL, v, off);
-    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
-  }
+  warp_track5(a, kk, ph, b, v);
   if (lane == 0) {
     ctl.red_u[warp] = a;
     ctl.red_b[warp] = b;
@@ -1995,15 +1962,7 @@ __device__ void block_track_to0(BigTrack& t, Ctl& ctl) {
     kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
     ph = lane < NW ? ctl.red_p[lane] : 0u;
     v = lane < NW ? ctl.red_s[lane] : 0.0;
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-      const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-      const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-      const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
-      const double v2 = __shfl_down_sync(FULL, v, off);
-      big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
-    }
+    warp_track5(a, kk, ph, b, v);
     t.A = a;
     t.B = b;
     t.k = kk;
@@ -2077,15 +2036,7 @@ __device__ bool big_gather(const BigPartial* cur, int G, unsigned target, BigBar
   uint64_t a = g.A, b = g.B;
   uint32_t kk = g.k, ph = g.ph;
   double v = g.v;
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const uint64_t a2 = __shfl_down_sync(FULL, a, off);
-    const uint64_t b2 = __shfl_down_sync(FULL, b, off);
-    const uint32_t k2 = __shfl_down_sync(FULL, kk, off);
-    const uint32_t p2 = __shfl_down_sync(FULL, ph, off);
-    const double v2 = __shfl_down_sync(FULL, v, off);
-    big_combine(a, kk, ph, b, v, a2, k2, p2, b2, v2);
-  }
+  warp_track5(a, kk, ph, b, v);
   g.A = __shfl_sync(FULL, a, 0);
   g.B = __shfl_sync(FULL, b, 0);
   g.k = __shfl_sync(FULL, kk, 0);
