@@ -197,6 +197,11 @@ int Engine::init() {
   CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
   CUDA_TRY(tci_step_configure());
   smem_bytes = tci_step_smem_bytes();
+  // TCI_PLAN_SMEM=<bytes> plans tasks against a smaller shared-memory budget (the
+  // kernel keeps its own), so that tests reach the global-memory layouts with
+  // small matrices; results do not depend on the layout.
+  if (const char* s = std::getenv("TCI_PLAN_SMEM")) plan_limit_ = (size_t)std::max(1024L, std::atol(s));
+  smem_bytes = std::min(smem_bytes, plan_limit_);
   CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device_));
   CUDA_TRY(cudaMalloc(&dcounter_, 64));
   cudaMemPool_t pool;
@@ -287,8 +292,9 @@ int Engine::ensure(size_t blob, size_t res, size_t work) {
 }
 
 // Shared-memory plan of a task; mirrors the SmemCursor use in step_kernel.cu.
-// Returns false if the task cannot run.
-static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
+// has_input: the RRLU matrix is given (t.ain, or a host matrix packed later), so
+// no f states are needed.  Returns false if the task cannot run.
+static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_input) {
   const size_t m = (size_t)t.m, n = (size_t)t.n;
   work_elems = 0;
   // argmax keys pack (column << 16) | row
@@ -296,27 +302,35 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems) {
     return false;
   switch (t.kind) {
     case TCI_TASK_RRLU: {
-      size_t rest = a16(m * 4) + a16(n * 4);
-      if (!t.ain) rest += 2 * a16(m * 8) + 2 * a16(n * 8);
-      if (a16(m * n * 8) + rest <= smem) {
+      const size_t perms = a16(m * 4) + a16(n * 4);
+      const size_t states = has_input ? 0 : 2 * a16(m * 8) + 2 * a16(n * 8);
+      if (a16(m * n * 8) + perms + states <= smem) {
         t.smem_mode = 1;
-        return true;
+      } else if (perms + states <= smem) {
+        t.smem_mode = 0;
+      } else if (perms <= smem && !has_input) {
+        t.smem_mode = 2;  // the f states beside the matrix in global scratch
+      } else {
+        return false;
       }
-      t.smem_mode = 0;
-      work_elems = m * n;
-      return rest <= smem;
+      work_elems = tci_work_elems(&t);
+      return true;
     }
     case TCI_TASK_SITE: {
       const size_t r = (size_t)t.r;
-      size_t rest = 2 * a16(r * 4) + 5 * a16(r * 8) + 2 * a16(m * 8);
+      const size_t small = 2 * a16(r * 4) + 5 * a16(r * 8), rowstates = 2 * a16(m * 8);
       size_t want_rows = std::min<size_t>(std::max<size_t>(m, 1), 64);
-      if (a16(r * r * 8) + rest + want_rows * (r * 8 + 8) <= smem) {
+      if (a16(r * r * 8) + small + rowstates + want_rows * (r * 8 + 8) <= smem) {
         t.smem_mode = 1;
-        return true;
+      } else if (small + rowstates + (r * 8 + 8) <= smem) {
+        t.smem_mode = 0;
+      } else if (small + (r * 8 + 8) <= smem) {
+        t.smem_mode = 2;  // the row f states beside P in global scratch
+      } else {
+        return false;
       }
-      t.smem_mode = 0;
-      work_elems = r * r;
-      return rest + (r * 8 + 8) <= smem;
+      work_elems = tci_work_elems(&t);
+      return true;
     }
     case TCI_TASK_CORE:
       t.smem_mode = 1;
@@ -347,15 +361,15 @@ static size_t staged_plan_bytes(const tci_task& t) {
   const size_t m = (size_t)t.m, n = (size_t)t.n;
   switch (t.kind) {
     case TCI_TASK_RRLU: {
-      size_t rest = a16(m * 4) + a16(n * 4);
-      if (!t.ain) rest += 2 * a16(m * 8) + 2 * a16(n * 8);
-      return t.smem_mode ? a16(m * n * 8) + rest : rest + a16((m + n) * 8);
+      const size_t perms = a16(m * 4) + a16(n * 4);
+      const size_t states = (t.ain || t.smem_mode == 2) ? 0 : 2 * a16(m * 8) + 2 * a16(n * 8);
+      return t.smem_mode == 1 ? a16(m * n * 8) + perms + states : perms + states + a16((m + n) * 8);
     }
     case TCI_TASK_SITE: {
       const size_t r = (size_t)t.r;
-      const size_t rest = 2 * a16(r * 4) + 5 * a16(r * 8) + 2 * a16(m * 8);
+      const size_t rest = 2 * a16(r * 4) + 5 * a16(r * 8) + (t.smem_mode == 2 ? 0 : 2 * a16(m * 8));
       const size_t want_rows = std::min<size_t>(std::max<size_t>(m, 1), 64);
-      return t.smem_mode ? a16(r * r * 8) + rest + want_rows * (r * 8 + 8) : rest + 8 * (r * 8 + 8);
+      return t.smem_mode == 1 ? a16(r * r * 8) + rest + want_rows * (r * 8 + 8) : rest + 8 * (r * 8 + 8);
     }
     case TCI_TASK_CORE:
       return 2 * a16(m * 8) + 2 * a16(n * 8);
@@ -445,7 +459,7 @@ int Engine::launch() {
   bool anybad = false;
   for (size_t i = 0; i < nt; ++i) {
     apply_tuning(batch[i]->t);
-    if (!plan_task(batch[i]->t, smem_bytes, wel[i])) {
+    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host)) {
       bad[i] = 1;
       anybad = true;
     }
@@ -841,7 +855,7 @@ void Engine::set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scr
   rq_ = q;
   hpool_ = host_pool;
   spool_ = scratch_pool;
-  res_smem_ = tci_resident_smem_bytes();
+  res_smem_ = std::min(tci_resident_smem_bytes(), plan_limit_);
 }
 
 int Engine::submit() {
@@ -864,7 +878,7 @@ int Engine::submit() {
       tci_task& t = r.t;
       size_t we = 0;
       apply_tuning(t);
-      if (!plan_task(t, res_smem_, we)) {
+      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host)) {
         rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
         break;
       }
@@ -918,7 +932,7 @@ int Engine::submit() {
           break;
         }
         f.dblocks.push_back(d);
-        if (!t.smem_mode) t.work = d;
+        if (t.smem_mode != 1) t.work = d;
         if (lut) t.lut = d + we;
       }
       t.cost = task_cost(t);

@@ -333,6 +333,7 @@ class Engine {
   BlockPool* spool_ = nullptr;  // device scratch of this engine's tasks (this thread only)
   BlockPool* dpool_ = nullptr;
   size_t res_smem_ = 0;
+  size_t plan_limit_ = SIZE_MAX;  // TCI_PLAN_SMEM
   std::vector<Flight> flights_;
   size_t inflight_tasks_ = 0;  // tasks of flights_
   std::vector<char> big_res_;  // host copy of the last multi-CTA rrLU's result record

@@ -903,7 +903,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   const int m = T.m, n = T.n, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   ResPtrs rp = res_ptrs(resb, T);
   SmemCursor cur{smem};
-  double* A = T.smem_mode ? (double*)cur.take((size_t)m * n * 8) : T.work;
+  double* A = T.smem_mode == 1 ? (double*)cur.take((size_t)m * n * 8) : T.work;
   const int lda = m;
   int* rowperm = (int*)cur.take((size_t)m * 4);
   int* colperm = (int*)cur.take((size_t)n * 4);
@@ -929,10 +929,12 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
     }
   } else {
     const double* prm = (const double*)at(blob, T.params);
-    double* rs0 = (double*)cur.take((size_t)m * 8);
-    double* rs1 = (double*)cur.take((size_t)m * 8);
-    double* cs0 = (double*)cur.take((size_t)n * 8);
-    double* cs1 = (double*)cur.take((size_t)n * 8);
+    // the row / column f states: on chip, or after the matrix in global scratch
+    double* const st = T.smem_mode == 2 ? T.work + (size_t)m * n : nullptr;
+    double* rs0 = st ? st : (double*)cur.take((size_t)m * 8);
+    double* rs1 = st ? st + m : (double*)cur.take((size_t)m * 8);
+    double* cs0 = st ? st + 2 * (size_t)m : (double*)cur.take((size_t)n * 8);
+    double* cs1 = st ? st + 2 * (size_t)m + n : (double*)cur.take((size_t)n * 8);
     compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
     compute_states(T, prm, (const uint8_t*)at(blob, T.cols), n, T.nr, T.nl, cs0, cs1);
     __syncthreads();
@@ -958,7 +960,7 @@ __device__ void task_rrlu(const tci_task& T, const char* blob, char* resb, char*
   argmax_resolve(am, A, lda, 0, m, 0, n, ctl);
   const bool leftorth = T.leftorth != 0;
   double* xy = nullptr;
-  if (!T.smem_mode && (size_t)(cur.p - smem) + (size_t)(m + n) * 8 <= smem_bytes) xy = (double*)cur.take((size_t)(m + n) * 8);
+  if (T.smem_mode != 1 && (size_t)(cur.p - smem) + (size_t)(m + n) * 8 <= smem_bytes) xy = (double*)cur.take((size_t)(m + n) * 8);
   const bool nan_part = rrlu_loop(A, lda, m, n, T.maxrank, T.reltol, T.abstol, leftorth, rowperm, colperm, rp.diag,
                                   ctl, xy, T.tail_elems > 0 ? T.tail_elems : WARP_TAIL_RRLU);
   const int K = ctl.K;
@@ -1143,15 +1145,16 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
   ResPtrs rp = res_ptrs(resb, T);
   const double* prm = (const double*)at(blob, T.params);
   SmemCursor cur{smem};
-  double* A = T.smem_mode ? (double*)cur.take((size_t)r * r * 8) : T.work;
+  double* A = T.smem_mode == 1 ? (double*)cur.take((size_t)r * r * 8) : T.work;
   int* ipiv = (int*)cur.take((size_t)r * 4);
   (void)cur.take((size_t)r * 4);  // unused slot (keeps the host's shared-memory plan)
   double* ps0 = (double*)cur.take((size_t)r * 8);
   double* ps1 = (double*)cur.take((size_t)r * 8);
   double* cs0 = (double*)cur.take((size_t)r * 8);
   double* cs1 = (double*)cur.take((size_t)r * 8);
-  double* rs0 = (double*)cur.take((size_t)m * 8);
-  double* rs1 = (double*)cur.take((size_t)m * 8);
+  // the row f states: on chip, or after P in global scratch
+  double* rs0 = T.smem_mode == 2 ? T.work + (size_t)r * r : (double*)cur.take((size_t)m * 8);
+  double* rs1 = T.smem_mode == 2 ? T.work + (size_t)r * r + m : (double*)cur.take((size_t)m * 8);
   compute_states(T, prm, (const uint8_t*)at(blob, T.prows), r, T.nl, 0, ps0, ps1);
   compute_states(T, prm, (const uint8_t*)at(blob, T.cols), r, T.nr, T.nl, cs0, cs1);
   compute_states(T, prm, (const uint8_t*)at(blob, T.rows), m, T.nl, 0, rs0, rs1);
@@ -1540,8 +1543,8 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM)
     if (ti >= ntasks) break;
     tci_task T = tasks[order[ti]];
     size_t we = 0;
-    if (!T.smem_mode) {
-      we = T.kind == TCI_TASK_RRLU ? (size_t)T.m * T.n : (T.kind == TCI_TASK_SITE ? (size_t)T.r * T.r : 0);
+    if (T.smem_mode != 1) {
+      we = tci_work_elems(&T);
       T.work = area;
     }
     if (!T.lut_full) T.lut = T.lutcap0 > 0 ? area + we : nullptr;
@@ -1986,8 +1989,10 @@ __device__ __forceinline__ void big_publish(BigPartial& o, const BigTrack& t, Bi
   red_release_gpu_add_u32(&bar->arrived, 1u);
 }
 
-// Most partials one lane of the gathering warp handles (grids of up to 160 CTAs).
+// Partials one lane of the gathering warp loads at once, and the most it handles
+// (grids of up to 320 CTAs).
 constexpr int BIG_GATHER_Q = 5;
+constexpr int BIG_GATHER_MAX = 2 * BIG_GATHER_Q;
 
 // Warp 0: wait until `target` partials have arrived in all (lane 0 polls the
 // counter, bounded), then combine the G partials of this step, every lane
@@ -2014,14 +2019,14 @@ __device__ bool big_gather(const BigPartial* cur, int G, unsigned target, BigBar
   }
   ok = __shfl_sync(FULL, ok, 0);
   __syncwarp();  // lane 0's acquire orders the warp's loads below
-  if (ok) {
+  for (int base = 0; ok && base < G; base += 32 * BIG_GATHER_Q) {
     uint64_t qa[BIG_GATHER_Q], qb[BIG_GATHER_Q];
     uint32_t qk[BIG_GATHER_Q], qp[BIG_GATHER_Q];
     double qv[BIG_GATHER_Q];
 #pragma unroll
     for (int q = 0; q < BIG_GATHER_Q; ++q) {
-      if (lane + 32 * q < G) {
-        const BigPartial* p = cur + lane + 32 * q;
+      if (base + lane + 32 * q < G) {
+        const BigPartial* p = cur + base + lane + 32 * q;
         qa[q] = __ldcg(&p->A);
         qb[q] = __ldcg(&p->B);
         qk[q] = __ldcg(&p->k);
@@ -2031,7 +2036,7 @@ __device__ bool big_gather(const BigPartial* cur, int G, unsigned target, BigBar
     }
 #pragma unroll
     for (int q = 0; q < BIG_GATHER_Q; ++q)
-      if (lane + 32 * q < G) big_combine(g.A, g.k, g.ph, g.B, g.v, qa[q], qk[q], qp[q], qb[q], qv[q]);
+      if (base + lane + 32 * q < G) big_combine(g.A, g.k, g.ph, g.B, g.v, qa[q], qk[q], qp[q], qb[q], qv[q]);
   }
   uint64_t a = g.A, b = g.B;
   uint32_t kk = g.k, ph = g.ph;
@@ -2404,7 +2409,7 @@ struct BigGrid {
   int pr, pc, mb, nb;
 };
 BigGrid big_grid(int64_t m, int64_t n, int G) {
-  G = std::min(G, 32 * BIG_GATHER_Q);  // one gathering warp reads every partial
+  G = std::min(G, 32 * BIG_GATHER_MAX);  // one gathering warp reads every partial
   BigGrid best{1, 1, (int)m, (int)n};
   double best_score = -1.0;
   for (int pr = 1; pr <= G; ++pr) {

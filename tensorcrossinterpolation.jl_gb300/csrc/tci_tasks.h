@@ -14,6 +14,7 @@
 // record's `done` word.  The offsets are then absolute addresses (the base
 // pointers passed to the kernel are zero).
 #pragma once
+#include <stddef.h>
 #include <stdint.h>
 
 enum {
@@ -58,7 +59,8 @@ typedef struct tci_task {
   double* core_out;           // LEFT/RIGHT/FACTORS, SITE and CORE output
   double* work;               // global scratch (matrix too large for shared memory)
   int64_t cost;               // scheduling weight
-  int32_t smem_mode;           // 1: matrix held in shared memory
+  int32_t smem_mode;           // 1: matrix held in shared memory; 0: matrix in `work`; 2: matrix
+                               // and the row / column f states in `work` (tci_work_elems)
   int32_t kcap;                // pivot capacity of the result record
   double* lut;                 // scratch for tabulated f parts (lutcap0 + lutcap1 doubles)
   int32_t lutcap0, lutcap1;    // table capacities (0: evaluate f directly)
@@ -71,6 +73,18 @@ typedef struct tci_task {
                                // inputs, starting at params) are copied to the top of shared memory
                                // before the task runs (0: read in place)
 } tci_task;
+
+// Doubles of global scratch a planned task uses at `work` (its f tables follow).
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+static inline size_t tci_work_elems(const tci_task* t) {
+  const size_t m = (size_t)t->m, n = (size_t)t->n, r = (size_t)t->r;
+  if (t->smem_mode == 1) return 0;
+  if (t->kind == TCI_TASK_RRLU) return m * n + (t->smem_mode == 2 ? 2 * (m + n) : 0);
+  if (t->kind == TCI_TASK_SITE) return r * r + (t->smem_mode == 2 ? 2 * m : 0);
+  return 0;
+}
 
 // Result record: fixed header followed by per-task arrays.
 typedef struct tci_result_head {
@@ -121,9 +135,14 @@ typedef struct tci_resident_state {
 } tci_resident_state;
 
 // Threads of one task CTA, and CTAs resident per SM (the shared-memory budget of
-// a CTA is the SM's divided among them).
-#define TCI_STEP_THREADS 512
+// a CTA is the SM's divided among them).  Two 256-thread CTAs per SM: while one
+// task waits on a pivot's latency chain (division, reductions, decision,
+// barriers) the other's rank-1 update keeps the FP64 pipe busy.  Measured on a
+// 10 000-request served step: 550 ms of kernel time against 630 ms with one
+// 512-thread CTA per SM, although Π above ~114 rows then no longer fits in
+// shared memory and is factored in the L2-resident per-CTA scratch.
+#define TCI_STEP_THREADS 256
 // EVAL tasks whose bonds are at most this run one thread per point, the running
 // vector in 2 x TCI_EVAL_THREAD_RMAX x TCI_STEP_THREADS doubles of shared memory.
 #define TCI_EVAL_THREAD_RMAX 16
-#define TCI_CTAS_PER_SM 1
+#define TCI_CTAS_PER_SM 2
