@@ -197,11 +197,10 @@ int Engine::init() {
   CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
   CUDA_TRY(tci_step_configure());
   smem_bytes = tci_step_smem_bytes();
-  // TCI_PLAN_SMEM=<bytes> plans tasks against a smaller shared-memory budget (the
-  // kernel keeps its own), so that tests reach the global-memory layouts with
-  // small matrices; results do not depend on the layout.
+  // TCI_PLAN_SMEM=<bytes> plans RRLU and SITE tasks against a smaller
+  // shared-memory budget (the kernel keeps its own), so that tests reach the
+  // global-memory layouts with small matrices; results do not depend on the layout.
   if (const char* s = std::getenv("TCI_PLAN_SMEM")) plan_limit_ = (size_t)std::max(1024L, std::atol(s));
-  smem_bytes = std::min(smem_bytes, plan_limit_);
   CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device_));
   CUDA_TRY(cudaMalloc(&dcounter_, 64));
   cudaMemPool_t pool;
@@ -293,10 +292,12 @@ int Engine::ensure(size_t blob, size_t res, size_t work) {
 
 // Shared-memory plan of a task; mirrors the SmemCursor use in step_kernel.cu.
 // has_input: the RRLU matrix is given (t.ain, or a host matrix packed later), so
-// no f states are needed.  Returns false if the task cannot run.
-static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_input) {
+// no f states are needed.  mat_limit caps the shared memory that RRLU and SITE
+// plans may use (TCI_PLAN_SMEM).  Returns false if the task cannot run.
+static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_input, size_t mat_limit = SIZE_MAX) {
   const size_t m = (size_t)t.m, n = (size_t)t.n;
   work_elems = 0;
+  if (t.kind == TCI_TASK_RRLU || t.kind == TCI_TASK_SITE) smem = std::min(smem, mat_limit);
   // argmax keys pack (column << 16) | row
   if ((t.kind == TCI_TASK_RRLU && (m > 65535 || n > 65535)) || (t.kind == TCI_TASK_SITE && t.r > 65535))
     return false;
@@ -459,7 +460,7 @@ int Engine::launch() {
   bool anybad = false;
   for (size_t i = 0; i < nt; ++i) {
     apply_tuning(batch[i]->t);
-    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host)) {
+    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host, plan_limit_)) {
       bad[i] = 1;
       anybad = true;
     }
@@ -855,7 +856,7 @@ void Engine::set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scr
   rq_ = q;
   hpool_ = host_pool;
   spool_ = scratch_pool;
-  res_smem_ = std::min(tci_resident_smem_bytes(), plan_limit_);
+  res_smem_ = tci_resident_smem_bytes();
 }
 
 int Engine::submit() {
@@ -878,7 +879,7 @@ int Engine::submit() {
       tci_task& t = r.t;
       size_t we = 0;
       apply_tuning(t);
-      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host)) {
+      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host, plan_limit_)) {
         rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
         break;
       }
@@ -1189,6 +1190,7 @@ int Engine::run_resident(CoTask& t) {
   while (!t.h.done()) {
     rc = submit();
     if (rc) break;
+    if (t.h.done()) break;  // a task that could not be submitted failed the solve
     bool progressed = false;
     rc = poll(progressed);
     if (rc) break;

@@ -59,3 +59,23 @@ def test_global_layouts_batched_equal_default(T, small_plan_ctx):
             assert np.array_equal(a.sets(s)[0], b.sets(s)[0])
             assert np.array_equal(a.sets(s)[1], b.sets(s)[1])
             assert np.array_equal(a.sitetensor(s), b.sitetensor(s))
+
+
+def test_task_beyond_the_plan_fails_cleanly(T):
+    """A Π whose permutations alone exceed the (here artificially small) budget:
+    the solve fails with the plan error, and the context keeps working."""
+    old = os.environ.get("TCI_PLAN_SMEM")
+    os.environ["TCI_PLAN_SMEM"] = "1024"
+    try:
+        ctx = T.Context(0)
+    finally:
+        if old is None:
+            del os.environ["TCI_PLAN_SMEM"]
+        else:
+            os.environ["TCI_PLAN_SMEM"] = old
+    rng = np.random.default_rng(79)
+    prm = _served(rng, 6, 12)
+    with pytest.raises(T.TCIError, match="on-chip plan"):
+        T.crossinterpolate2(float, T.DeviceFunction("served", prm), [12] * 6, tolerance=1e-10, maxbonddim=64, ctx=ctx)
+    tci, ranks, _ = T.crossinterpolate2(float, T.DeviceFunction("lorentz"), [4] * 4, tolerance=1e-8, ctx=ctx)
+    assert max(ranks) >= 1
