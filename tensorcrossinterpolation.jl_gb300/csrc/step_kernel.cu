@@ -2466,18 +2466,23 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
   a.nb = g.nb;
   a.reltol = reltol;
   a.abstol = abstol;
-  // most of the SM's on-chip memory as L1: the CTA's block of the working
-  // matrix is re-read every pivot (the attribute is a hint; the shared memory
-  // the launch asks for is always granted)
-  static bool carve = false;
-  if (!carve) {
-    e = cudaFuncSetAttribute((const void*)rrlu_big_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 25);
+  // Most of the SM's on-chip memory as L1 (the CTA's block of the working matrix
+  // is re-read every pivot), but enough shared memory for the CTAs that share
+  // an SM: the carveout is what the occupancy of a cooperative launch is
+  // computed with.
+  const size_t smem = tci_rrlu_big_smem(m, n, grid);
+  const int per_sm = (g.pr * g.pc + grid / TCI_CTAS_PER_SM - 1) / (grid / TCI_CTAS_PER_SM);
+  const double need = (double)per_sm * (double)(smem + 3 * 1024) / (228.0 * 1024.0);
+  const int pct = std::min(100, std::max(25, (int)std::ceil(100.0 * need)));
+  static int carve = -1;
+  if (pct != carve) {
+    e = cudaFuncSetAttribute((const void*)rrlu_big_kernel, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
-    carve = true;
+    carve = pct;
   }
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(NT), args,
-                                     tci_rrlu_big_smem(m, n, grid), stream);
+  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(NT), args, smem,
+                                     stream);
 }
 
 // Launch the resident kernel: one CTA per SM, all resident at once

@@ -209,3 +209,14 @@ def test_nan_inf_planted(T, oracle, seed):
             continue
         _same(T.rrlu(A, **kw), ref)
     assert 0 < raised < 40  # both outcomes occur
+
+
+def test_multi_cta_long_maps(T, oracle):
+    """A tall matrix whose permutation maps take tens of KB of shared memory per
+    CTA (two CTAs share an SM): the launch sizes its shared-memory carveout for
+    them, and the result stays bit-exact."""
+    rng = np.random.default_rng(12)
+    m, n, r = 4000, 600, 30
+    A = rng.standard_normal((m, r)) @ rng.standard_normal((r, n)) + 1e-10 * rng.standard_normal((m, n))
+    _same(T.rrlu(A, maxrank=40), oracle.rrlu(A, maxrank=40))
+    _same(T.rrlu(A.T.copy(), maxrank=40, leftorthogonal=False), oracle.rrlu(A.T.copy(), maxrank=40, leftorthogonal=False))
