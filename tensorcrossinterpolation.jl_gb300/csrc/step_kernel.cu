@@ -46,18 +46,24 @@ constexpr uint64_t NAN_FLOOR = 0x7ff0000000000000ULL;  // bits above this are Na
 constexpr uint64_t SQ_SMALL = (uint64_t)(1023 - 500) << 52;  // below: squares may be subnormal
 constexpr uint64_t SQ_BIG = (uint64_t)(1023 + 500) << 52;    // above: squares may overflow
 
-struct Ctl {
+template <int W>
+struct CtlT {
   int task;
   int r, c, K, stop, kmax, need_exact, bar_err;
   int status;
   double piv, maxerror, err;
-  double red_s[NW + 1];
-  int red_k[NW + 1];
-  unsigned long long red_u[NW + 1];
-  unsigned long long red_b[NW + 1];
-  unsigned red_p[NW + 1];
-  long long red4[4][NW + 1];
+  double red_s[W + 1];
+  int red_k[W + 1];
+  unsigned long long red_u[W + 1];
+  unsigned long long red_b[W + 1];
+  unsigned red_p[W + 1];
+  long long red4[4][W + 1];
 };
+using Ctl = CtlT<NW>;
+// The multi-CTA rrLU runs one 512-thread CTA per SM whatever the task CTAs are.
+constexpr int BIG_NT = 512;
+constexpr int BIG_NW = BIG_NT / 32;
+using BigCtl = CtlT<BIG_NW>;
 
 __device__ __forceinline__ double jmax(double a, double b) {
   if (a != a || b != b) return __longlong_as_double(0x7ff8000000000000LL);
@@ -1875,7 +1881,7 @@ constexpr long long BIG_BAR_POLLS = 1LL << 24;  // bounded wait of one grid barr
 
 // Grid-wide barrier (sense by generation).  Returns false once any CTA has hit
 // the wait bound; every CTA then leaves the factorization.
-__device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, Ctl& ctl) {
+__device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, BigCtl& ctl) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1904,7 +1910,7 @@ __device__ bool big_barrier(BigBar* bar, unsigned nblocks, unsigned& gen, Ctl& c
 
 // Block reduction of every thread's BigTrack; every thread gets the result.
 // Ends with a barrier.
-__device__ void block_track(BigTrack& t, Ctl& ctl) {
+__device__ void block_track(BigTrack& t, BigCtl& ctl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t a = t.A, b = t.B;
   uint32_t kk = t.k, ph = t.ph;
@@ -1919,33 +1925,33 @@ __device__ void block_track(BigTrack& t, Ctl& ctl) {
   }
   __syncthreads();
   if (warp == 0) {
-    a = lane < NW ? ctl.red_u[lane] : 0ULL;
-    b = lane < NW ? ctl.red_b[lane] : 0ULL;
-    kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
-    ph = lane < NW ? ctl.red_p[lane] : 0u;
-    v = lane < NW ? ctl.red_s[lane] : 0.0;
+    a = lane < BIG_NW ? ctl.red_u[lane] : 0ULL;
+    b = lane < BIG_NW ? ctl.red_b[lane] : 0ULL;
+    kk = lane < BIG_NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+    ph = lane < BIG_NW ? ctl.red_p[lane] : 0u;
+    v = lane < BIG_NW ? ctl.red_s[lane] : 0.0;
     warp_track5(a, kk, ph, b, v);
     if (lane == 0) {
-      ctl.red_u[NW] = a;
-      ctl.red_b[NW] = b;
-      ctl.red_k[NW] = (int)kk;
-      ctl.red_p[NW] = ph;
-      ctl.red_s[NW] = v;
+      ctl.red_u[BIG_NW] = a;
+      ctl.red_b[BIG_NW] = b;
+      ctl.red_k[BIG_NW] = (int)kk;
+      ctl.red_p[BIG_NW] = ph;
+      ctl.red_s[BIG_NW] = v;
     }
   }
   __syncthreads();
-  t.A = ctl.red_u[NW];
-  t.B = ctl.red_b[NW];
-  t.k = (uint32_t)ctl.red_k[NW];
-  t.ph = ctl.red_p[NW];
-  t.v = ctl.red_s[NW];
+  t.A = ctl.red_u[BIG_NW];
+  t.B = ctl.red_b[BIG_NW];
+  t.k = (uint32_t)ctl.red_k[BIG_NW];
+  t.ph = ctl.red_p[BIG_NW];
+  t.v = ctl.red_s[BIG_NW];
   __syncthreads();
 }
 
 // Block reduction of every thread's BigTrack into thread 0's (the others keep
 // partial values).  One CTA barrier; the caller's next barrier orders the reuse
 // of the staging slots.
-__device__ void block_track_to0(BigTrack& t, Ctl& ctl) {
+__device__ void block_track_to0(BigTrack& t, BigCtl& ctl) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint64_t a = t.A, b = t.B;
   uint32_t kk = t.k, ph = t.ph;
@@ -1960,11 +1966,11 @@ __device__ void block_track_to0(BigTrack& t, Ctl& ctl) {
   }
   __syncthreads();
   if (warp == 0) {
-    a = lane < NW ? ctl.red_u[lane] : 0ULL;
-    b = lane < NW ? ctl.red_b[lane] : 0ULL;
-    kk = lane < NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
-    ph = lane < NW ? ctl.red_p[lane] : 0u;
-    v = lane < NW ? ctl.red_s[lane] : 0.0;
+    a = lane < BIG_NW ? ctl.red_u[lane] : 0ULL;
+    b = lane < BIG_NW ? ctl.red_b[lane] : 0ULL;
+    kk = lane < BIG_NW ? (uint32_t)ctl.red_k[lane] : 0xffffffffu;
+    ph = lane < BIG_NW ? ctl.red_p[lane] : 0u;
+    v = lane < BIG_NW ? ctl.red_s[lane] : 0.0;
     warp_track5(a, kk, ph, b, v);
     t.A = a;
     t.B = b;
@@ -2063,9 +2069,9 @@ struct BigArgs {
   double reltol, abstol;
 };
 
-__global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P) {
+__global__ void __launch_bounds__(BIG_NT, 1) rrlu_big_kernel(BigArgs P) {
   extern __shared__ __align__(16) char smem[];
-  __shared__ Ctl ctl;
+  __shared__ BigCtl ctl;
   const int tid = threadIdx.x, G = gridDim.x, b = blockIdx.x, m = P.m, n = P.n;
   const bool leftorth = P.leftorth != 0;
   const int r0 = (b / P.pc) * P.mb, c0 = (b % P.pc) * P.nb;
@@ -2082,10 +2088,10 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   int* act_c = slot_r + P.mb;          // (nb each)
   int* slot_c = act_c + P.nb;
   unsigned gen = 0;
-  for (int i = tid; i < m; i += NT) pos_r[i] = stor_r[i] = i;
-  for (int j = tid; j < n; j += NT) pos_c[j] = stor_c[j] = j;
-  for (int t = tid; t < nrb; t += NT) act_r[t] = slot_r[t] = t;  // local indices
-  for (int u = tid; u < ncb; u += NT) act_c[u] = slot_c[u] = u;
+  for (int i = tid; i < m; i += BIG_NT) pos_r[i] = stor_r[i] = i;
+  for (int j = tid; j < n; j += BIG_NT) pos_c[j] = stor_c[j] = j;
+  for (int t = tid; t < nrb; t += BIG_NT) act_r[t] = slot_r[t] = t;  // local indices
+  for (int u = tid; u < ncb; u += BIG_NT) act_c[u] = slot_c[u] = u;
   if (tid == 0) {
     ctl.maxerror = 0.0;
     ctl.err = __longlong_as_double(0x7ff8000000000000LL);
@@ -2098,7 +2104,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   bt.init();
   {
     const long long tot = (long long)nrb * ncb;
-    for (long long e = tid; e < tot; e += NT) {
+    for (long long e = tid; e < tot; e += BIG_NT) {
       const int i = r0 + (int)(e % nrb), j = c0 + (int)(e / nrb);
       const double v = P.ain[i + (size_t)j * m];
       P.A[i + (size_t)j * m] = v;
@@ -2173,7 +2179,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
           const uint64_t Mstar = g.A ? g.A - 1 : 0;
           const bool safe = Mstar >= SQ_SMALL && Mstar < SQ_BIG;
           const bool close = g.B != 0 && (g.B - 1) + 16 >= Mstar;
-          ctl.red_u[NW] = Mstar;
+          ctl.red_u[BIG_NW] = Mstar;
           ctl.need_exact = (g.A != 0 && !(safe && !close)) ? 1 : 0;
           if (g.A == 0) {  // every element NaN: the scan keeps its start
             ctl.kmax = (int)(((unsigned)stor_c[K] << 16) | (unsigned)stor_r[K]);
@@ -2194,12 +2200,12 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
       break;
     }
     if (ctl.need_exact) {  // squares of the elements near the maximum (rare)
-      const uint64_t Mstar = ctl.red_u[NW];
+      const uint64_t Mstar = ctl.red_u[BIG_NW];
       const int nr = ctl.r, nc = ctl.c;
       ArgBest ab;
       ab.init();
       uint32_t abph = 0;
-      for (long long e = tid; e < (long long)nr * nc; e += NT) {
+      for (long long e = tid; e < (long long)nr * nc; e += BIG_NT) {
         const int i = r0 + act_r[(int)(e % nr)], j = c0 + act_c[(int)(e / nr)];
         const double v = P.A[i + (size_t)j * m];
         if (near_max(abs_bits(v), Mstar)) {
@@ -2234,7 +2240,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
       if (!ok) break;
       BigTrack g;
       g.init();
-      for (int t = tid; t < G; t += NT) {
+      for (int t = tid; t < G; t += BIG_NT) {
         const BigPartial* q = cur + t;
         big_combine(g.A, g.k, g.ph, g.B, g.v, __ldcg(&q->A), __ldcg(&q->k), __ldcg(&q->ph), __ldcg(&q->B),
                     __ldcg(&q->v));
@@ -2258,7 +2264,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
     // ---- x (pivot column) for the active rows, y (pivot row) for the active columns
     // (one element per thread: the x and y entries on different threads)
     const int nr = ctl.r, nc = ctl.c;
-    for (int t = tid; t < nr + nc; t += NT) {
+    for (int t = tid; t < nr + nc; t += BIG_NT) {
       if (t < nr) {
         const double v = __ldcg(&P.A[r0 + act_r[t] + (size_t)Cc * m]);
         xs[t] = leftorth ? __ddiv_rn(v, piv) : v;
@@ -2276,11 +2282,11 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
     bt.init();
     if (nr > 0 && nc > 0) {
       const long long tot = (long long)nr * nc;
-      const int sq = NT / nr, sr = NT % nr;
+      const int sq = BIG_NT / nr, sr = BIG_NT % nr;
       const bool rev = (K & 1) != 0;
       int tt = tid % nr, uu = tid / nr;
       long long e = tid;
-      for (; e + 3LL * NT < tot; e += 4LL * NT) {
+      for (; e + 3LL * BIG_NT < tot; e += 4LL * BIG_NT) {
         int ti[4], ui[4];
         double* ap[4];
         double av[4];
@@ -2306,7 +2312,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
           bt.push(v, pack_key(pos_r[i], pos_c[j]), pack_key(i, j));
         }
       }
-      for (; e < tot; e += NT) {
+      for (; e < tot; e += BIG_NT) {
         const int u = rev ? nc - 1 - uu : uu;
         const int i = r0 + act_r[tt], j = c0 + act_c[u];
         double* a = P.A + i + (size_t)j * m;
@@ -2336,7 +2342,7 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   int bad = 0;
   {
     const long long tot = (long long)nrb * ncb;
-    for (long long e = tid; e < tot; e += NT) {
+    for (long long e = tid; e < tot; e += BIG_NT) {
       const int i = r0 + (int)(e % nrb), j = c0 + (int)(e / nrb);
       const int lr = pos_r[i], lc = pos_c[j];
       double v = P.A[i + (size_t)j * m];
@@ -2357,12 +2363,12 @@ __global__ void __launch_bounds__(NT, TCI_CTAS_PER_SM) rrlu_big_kernel(BigArgs P
   }
   if (b == 0) {
     int nan = 0;
-    for (int t = tid; t < G; t += NT) nan |= (int)__ldcg(&P.parts[t].nan);
+    for (int t = tid; t < G; t += BIG_NT) nan |= (int)__ldcg(&P.parts[t].nan);
     nan = __syncthreads_or(nan);
     int* fr = (int*)(P.fact + (size_t)m * n);
-    for (int i = tid; i < m; i += NT) fr[i] = stor_r[i];
-    for (int j = tid; j < n; j += NT) fr[m + j] = stor_c[j];
-    for (int q = tid; q < K; q += NT) {
+    for (int i = tid; i < m; i += BIG_NT) fr[i] = stor_r[i];
+    for (int j = tid; j < n; j += BIG_NT) fr[m + j] = stor_c[j];
+    for (int q = tid; q < K; q += BIG_NT) {
       rowp[q] = stor_r[q];
       colp[q] = stor_c[q];
     }
@@ -2389,6 +2395,9 @@ size_t tci_step_smem_bytes() {
 // the task record and the f parameters as well).
 size_t tci_resident_smem_bytes() { return tci_step_smem_bytes(); }
 
+// Dynamic shared memory of one multi-CTA rrLU CTA (one per SM).
+size_t tci_big_smem_limit() { return (size_t)(228 * 1024) - 3 * 1024; }
+
 cudaError_t tci_step_configure() {
   cudaError_t e = cudaFuncSetAttribute(tci_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)tci_step_smem_bytes());
@@ -2397,7 +2406,7 @@ cudaError_t tci_step_configure() {
                            (int)tci_resident_smem_bytes());
   if (e != cudaSuccess) return e;
   return cudaFuncSetAttribute(rrlu_big_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tci_step_smem_bytes());
+                              (int)tci_big_smem_limit());
 }
 
 // Multi-CTA rrLU (rrlu_big_kernel).  The CTA grid: pr x pc <= G CTAs with the
@@ -2408,7 +2417,10 @@ namespace {
 struct BigGrid {
   int pr, pc, mb, nb;
 };
+// G: the task kernels' grid (TCI_CTAS_PER_SM per SM); the multi-CTA rrLU runs
+// one CTA per SM.
 BigGrid big_grid(int64_t m, int64_t n, int G) {
+  G = std::max(1, G / TCI_CTAS_PER_SM);
   G = std::min(G, 32 * BIG_GATHER_MAX);  // one gathering warp reads every partial
   BigGrid best{1, 1, (int)m, (int)n};
   double best_score = -1.0;
@@ -2431,7 +2443,7 @@ size_t tci_rrlu_big_smem(int64_t m, int64_t n, int G) {
   return (size_t)(8 * (m + n) + 16 * ((int64_t)g.mb + g.nb) + 64);
 }
 bool tci_rrlu_big_fits(int64_t m, int64_t n, int G) {
-  return m >= 1 && n >= 1 && m <= 65535 && n <= 65535 && tci_rrlu_big_smem(m, n, G) <= tci_step_smem_bytes();
+  return m >= 1 && n >= 1 && m <= 65535 && n <= 65535 && tci_rrlu_big_smem(m, n, G) <= tci_big_smem_limit();
 }
 size_t tci_rrlu_big_scratch_bytes(int grid, int kmax) {
   return 64 + 2 * (size_t)grid * sizeof(BigPartial) + (size_t)std::max(kmax, 1) * sizeof(double);
@@ -2471,7 +2483,8 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
   // an SM: the carveout is what the occupancy of a cooperative launch is
   // computed with.
   const size_t smem = tci_rrlu_big_smem(m, n, grid);
-  const int per_sm = (g.pr * g.pc + grid / TCI_CTAS_PER_SM - 1) / (grid / TCI_CTAS_PER_SM);
+  const int nsm = std::max(1, grid / TCI_CTAS_PER_SM);
+  const int per_sm = (g.pr * g.pc + nsm - 1) / nsm;
   const double need = (double)per_sm * (double)(smem + 3 * 1024) / (228.0 * 1024.0);
   const int pct = std::min(100, std::max(25, (int)std::ceil(100.0 * need)));
   static int carve = -1;
@@ -2481,7 +2494,7 @@ cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, c
     carve = pct;
   }
   void* args[] = {(void*)&a};
-  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(NT), args, smem,
+  return cudaLaunchCooperativeKernel((const void*)rrlu_big_kernel, dim3(g.pr * g.pc), dim3(BIG_NT), args, smem,
                                      stream);
 }
 
