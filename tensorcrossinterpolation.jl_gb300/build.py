@@ -23,16 +23,21 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # Kernels whose arithmetic must not be contracted into FMA (bit-exact pivots and
 # function values) are built with -fmad=false.
-CU_SOURCES = {
-    "step_kernel.cu": ["-fmad=false"],
-    "contract.cu": ["-fmad=false"],
-    "peak.cu": [],
-    "gather.cu": [],
-    "fcache.cu": [],
-    "tc_gemm.cu": [],
-}
+# (source, object, flags): step_kernel.cu is built twice, as the throughput
+# variant (two 256-thread task CTAs per SM) and the latency variant (one
+# 512-thread CTA per SM), in separate namespaces (csrc/kernels.h).
+CU_SOURCES = [
+    ("step_kernel.cu", "step_kernel.cu.o", ["-fmad=false"]),
+    ("step_kernel.cu", "step_kernel_k512.cu.o",
+     ["-fmad=false", "-DTCI_KNS=tci_k512", "-DTCI_STEP_THREADS=512", "-DTCI_CTAS_PER_SM=1", "-DTCI_SECONDARY"]),
+    ("contract.cu", "contract.cu.o", ["-fmad=false"]),
+    ("peak.cu", "peak.cu.o", []),
+    ("gather.cu", "gather.cu.o", []),
+    ("fcache.cu", "fcache.cu.o", []),
+    ("tc_gemm.cu", "tc_gemm.cu.o", []),
+]
 CXX_SOURCES = ["engine.cpp", "capi.cpp", "contract.cpp", "fcache.cpp", "contract_tci.cpp", "pivotsearch.cpp"]
-HEADERS = ["tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h", "tc_gemm.h"]
+HEADERS = ["kernels.h", "tci_tasks.h", "tci_functions.h", "tci_math.h", "tci_rng.h", "engine.h", "contract.h", "contract_tci.h", "fcache.h", "fc_slot.h", "tc_gemm.h"]
 
 
 def _newer(target, deps):
@@ -54,9 +59,9 @@ def build(verbose=False, force=False):
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(HERE, "..", "include", "tci_gb300.h")]
     jobs = []
     objs = []
-    for src, extra in CU_SOURCES.items():
+    for src, obj, extra in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(BUILD, obj)
         objs.append(o)
         if force or _newer(o, [s] + hdrs):
             jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

@@ -935,7 +935,7 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
     }
   };
   if (ctx->rq) {
-    int rc = ctx->rq->start();
+    int rc = ctx->rq->start(&tci_k256::kernels);
     if (rc) return rc;
     for (int g = 0; g < G; ++g) pool[g]->set_resident(ctx->rq.get(), ctx->hpools[g].get(), ctx->spools[g].get());
   }
@@ -1423,7 +1423,7 @@ int tci_autotune_rrlu(tci_ctx* ctx, int32_t reps, double* speedup, double* ms_de
   // calibration set and again on a fresh validation set
   const double margin = 0.98;
   reps = std::max(1, reps);
-  const int64_t grid = (int64_t)e.num_sms * TCI_CTAS_PER_SM;
+  const int64_t grid = (int64_t)e.num_sms * tci_k256::kernels.ctas_per_sm;
   double tot_def = 0.0, tot_best = 0.0;
   int32_t table[Engine::TUNE_BUCKETS];
   const bool timing = e.timing;

@@ -15,20 +15,10 @@
 #include <numeric>
 #include <thread>
 
-cudaError_t tci_step_configure();
-size_t tci_step_smem_bytes();
-cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* order_dev, int ntasks,
-                            int* counter_dev, int grid, double* cta_area, size_t cta_stride, cudaStream_t stream);
 cudaError_t tci_gather_launch(const void* table_dev, int n, double* dst_dev, int grid, cudaStream_t stream);
-size_t tci_resident_smem_bytes();
-size_t tci_rrlu_big_smem(int64_t m, int64_t n, int G);
-bool tci_rrlu_big_fits(int64_t m, int64_t n, int G);
-size_t tci_rrlu_big_scratch_bytes(int grid, int kmax);
-cudaError_t tci_rrlu_big_launch(const double* ain, double* work, double* fact, char* res, void* scratch, int m,
-                                int n, int kmax, int kcap, int leftorth, double reltol, double abstol, int grid,
-                                cudaStream_t stream);
-cudaError_t tci_resident_launch(tci_queue_slot* slots, uint32_t mask, tci_resident_state* st, tci_queue_ctl* qc,
-                                int grid, unsigned long long wait_ns, cudaStream_t stream);
+using tci_k256::tci_rrlu_big_fits;
+using tci_k256::tci_rrlu_big_launch;
+using tci_k256::tci_rrlu_big_scratch_bytes;
 
 namespace tci {
 
@@ -195,8 +185,9 @@ int Engine::init() {
   CUDA_TRY(cudaEventCreate(&ev0_));
   CUDA_TRY(cudaEventCreate(&ev1_));
   CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
-  CUDA_TRY(tci_step_configure());
-  smem_bytes = tci_step_smem_bytes();
+  CUDA_TRY(tci_k256::kernels.configure());
+  CUDA_TRY(tci_k512::kernels.configure());
+  smem_bytes = ks_->step_smem_bytes();
   // TCI_PLAN_SMEM=<bytes> plans RRLU and SITE tasks against a smaller
   // shared-memory budget (the kernel keeps its own), so that tests reach the
   // global-memory layouts with small matrices; results do not depend on the layout.
@@ -294,7 +285,8 @@ int Engine::ensure(size_t blob, size_t res, size_t work) {
 // has_input: the RRLU matrix is given (t.ain, or a host matrix packed later), so
 // no f states are needed.  mat_limit caps the shared memory that RRLU and SITE
 // plans may use (TCI_PLAN_SMEM).  Returns false if the task cannot run.
-static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_input, size_t mat_limit = SIZE_MAX) {
+static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_input, int threads,
+                      size_t mat_limit = SIZE_MAX) {
   const size_t m = (size_t)t.m, n = (size_t)t.n;
   work_elems = 0;
   if (t.kind == TCI_TASK_RRLU || t.kind == TCI_TASK_SITE) smem = std::min(smem, mat_limit);
@@ -338,8 +330,8 @@ static bool plan_task(tci_task& t, size_t smem, size_t& work_elems, bool has_inp
       return 2 * a16(m * 8) + 2 * a16(n * 8) <= smem;
     case TCI_TASK_EVAL:
       t.smem_mode = 1;
-      if (t.r <= TCI_EVAL_THREAD_RMAX) return (size_t)2 * TCI_EVAL_THREAD_RMAX * TCI_STEP_THREADS * 8 <= smem;
-      return (size_t)(TCI_STEP_THREADS / 32) * 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
+      if (t.r <= TCI_EVAL_THREAD_RMAX) return (size_t)2 * TCI_EVAL_THREAD_RMAX * threads * 8 <= smem;
+      return (size_t)(threads / 32) * 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
     case TCI_TASK_SUM:
       t.smem_mode = 1;
       return 2 * (size_t)std::max(t.r, 1) * 8 <= smem;
@@ -460,7 +452,8 @@ int Engine::launch() {
   bool anybad = false;
   for (size_t i = 0; i < nt; ++i) {
     apply_tuning(batch[i]->t);
-    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host, plan_limit_)) {
+    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host, ks_->threads,
+                   plan_limit_)) {
       bad[i] = 1;
       anybad = true;
     }
@@ -519,7 +512,7 @@ int Engine::launch() {
     cta_stride = std::max(cta_stride, need);
   }
   const size_t blob_total = off;
-  const int grid = std::max(1, std::min<int>((int)nt, num_sms * TCI_CTAS_PER_SM));
+  const int grid = std::max(1, std::min<int>((int)nt, num_sms * ks_->ctas_per_sm));
   cta_stride = (cta_stride + 31) / 32 * 32;  // 256-byte aligned areas
   work_total = cta_stride * (size_t)grid;
   int rc = ensure(blob_total, res_total, work_total);
@@ -562,7 +555,7 @@ int Engine::launch() {
   // ---- upload, launch, download
   CUDA_TRY(cudaMemcpyAsync(dblob_, hblob_, blob_total, cudaMemcpyHostToDevice, stream_));
   if (timing) CUDA_TRY(cudaEventRecord(ev0_, stream_));
-  CUDA_TRY(tci_step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid, dwork_,
+  CUDA_TRY(ks_->step_launch(dblob_, dres_, (const int*)(dblob_ + off_order), (int)nt, dcounter_, grid, dwork_,
                            cta_stride, stream_));
   if (timing) CUDA_TRY(cudaEventRecord(ev1_, stream_));
   CUDA_TRY(cudaMemcpyAsync(hres_, dres_, res_total, cudaMemcpyDeviceToHost, stream_));
@@ -746,7 +739,8 @@ void BlockPool::free(void* p) {
 // ---------------------------------------------------------------- resident ring
 int ResidentQueue::init(int dev, int num_sms, int idle_us) {
   device = dev;
-  grid = num_sms * TCI_CTAS_PER_SM;
+  this->num_sms = num_sms;
+  grid = num_sms * ks->ctas_per_sm;
   nslots = 1u << 15;
   mask = nslots - 1;
   CUDA_TRY(cudaSetDevice(dev));
@@ -776,12 +770,14 @@ ResidentQueue::~ResidentQueue() {
   if (slots) cudaFreeHost(slots);
 }
 
-int ResidentQueue::start() {
+int ResidentQueue::start(const tci_kernel_set* k) {
   std::lock_guard<std::mutex> lk(mu);
-  if (running) return 0;
+  if (running) return k == ks ? 0 : fail(TCI_ERR_GENERIC, "resident kernel already running in another variant");
+  ks = k;
+  grid = num_sms * ks->ctas_per_sm;
   std::atomic_ref<int32_t>(qc->stop).store(0, std::memory_order_release);
   CUDA_TRY(cudaEventRecord(ev0, stream));
-  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
+  CUDA_TRY(ks->resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
   CUDA_TRY(cudaEventRecord(ev1, stream));
   running = true;
   ++launches;
@@ -806,7 +802,7 @@ int ResidentQueue::ensure_alive() {
     return fail(TCI_ERR_TIMEOUT, "resident kernel: a wait for a task hit its limit");
   }
   CUDA_TRY(cudaEventRecord(ev0, stream));
-  CUDA_TRY(tci_resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
+  CUDA_TRY(ks->resident_launch(slots, mask, st_dev, qc, grid, wait_ns, stream));
   CUDA_TRY(cudaEventRecord(ev1, stream));
   ++launches;
   return 0;
@@ -856,7 +852,7 @@ void Engine::set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scr
   rq_ = q;
   hpool_ = host_pool;
   spool_ = scratch_pool;
-  res_smem_ = tci_resident_smem_bytes();
+  res_smem_ = q ? q->ks->resident_smem_bytes() : 0;
 }
 
 int Engine::submit() {
@@ -879,7 +875,7 @@ int Engine::submit() {
       tci_task& t = r.t;
       size_t we = 0;
       apply_tuning(t);
-      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host, plan_limit_)) {
+      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host, rq_->ks->threads, plan_limit_)) {
         rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
         break;
       }
@@ -1125,7 +1121,7 @@ static bool big_eligible(const Req& r, bool resident, int grid) {
 int Engine::run_big(Req& r) {
   tci_task& t = r.t;
   const int64_t m = t.m, n = t.n;
-  const int grid = num_sms * TCI_CTAS_PER_SM;
+  const int grid = num_sms * tci_k256::kernels.ctas_per_sm;
   const size_t rb = result_bytes(t);
   const size_t scratch = tci_rrlu_big_scratch_bytes(grid, t.maxrank);
   // one device block: result record, scratch, input copy (if host), working matrix
@@ -1175,13 +1171,14 @@ int Engine::run_big(Req& r) {
 
 int Engine::run_tasks(std::vector<Req*>& reqs) {
   if (fc_callback_depth()) return reentry();
-  if (reqs.size() == 1 && big_eligible(*reqs[0], resident(), num_sms * TCI_CTAS_PER_SM)) return run_big(*reqs[0]);
+  if (reqs.size() == 1 && big_eligible(*reqs[0], resident(), num_sms * tci_k256::kernels.ctas_per_sm))
+    return run_big(*reqs[0]);
   CoTask t = co_tasks(*this, reqs);
   return run(t, false);
 }
 
 int Engine::run_resident(CoTask& t) {
-  int rc = att_rq_->start();
+  int rc = att_rq_->start(&tci_k512::kernels);  // one solve: its tasks run one at a time
   if (rc) return rc;
   set_resident(att_rq_, att_h_, att_s_);
   t.h.resume();

@@ -16,6 +16,7 @@
 
 #include "../../include/tci_gb300.h"
 #include "fcache.h"
+#include "kernels.h"
 #include "tci_rng.h"
 #include "tci_tasks.h"
 
@@ -165,7 +166,8 @@ class BlockPool {
 // The ring of the resident kernel, shared by the engines of a context.
 struct ResidentQueue {
   int device = 0;
-  int grid = 0;
+  int grid = 0, num_sms = 0;
+  const tci_kernel_set* ks = &tci_k256::kernels;  // the variant of the running (or last) launch
   uint32_t nslots = 0, mask = 0;
   tci_queue_slot* slots = nullptr;       // mapped pinned host memory
   tci_queue_ctl* qc = nullptr;           // mapped pinned host memory
@@ -180,7 +182,9 @@ struct ResidentQueue {
   unsigned long long wait_ns = 60ull * 1000000000ull;  // a worker's longest wait for its ticket
   int init(int device, int num_sms, int idle_us);
   ~ResidentQueue();
-  int start();        // launch the kernel unless it is running
+  // launch the kernel unless it is running: the throughput variant (k256) for
+  // batched and served solves, the latency variant (k512) for a single solve
+  int start(const tci_kernel_set* k);
   int ensure_alive(); // relaunch it if every CTA has left (idle limit)
   int stop();         // ask the CTAs to leave once the ring is drained; wait
   int publish(const tci_task& t, uint64_t& ticket);
@@ -294,6 +298,7 @@ class Engine {
   tci_stats stats{};
   bool timing = true;
   size_t smem_bytes = 0;
+  const tci_kernel_set* ks_ = &tci_k256::kernels;  // batched launches: the throughput variant
   int num_sms = 0;
   size_t hbm_budget = 0;
   // Autotuned rrLU parameter per (rows, cols) bucket: the trailing-block size

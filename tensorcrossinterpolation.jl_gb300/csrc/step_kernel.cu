@@ -29,14 +29,24 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "kernels.h"
 #include "tci_functions.h"
 #include "tci_tasks.h"
+
+// The variant this translation unit builds (kernels.h): the threads of one task
+// CTA and the task CTAs per SM, and the namespace of its kernels and launchers.
+#ifndef TCI_KNS
+#define TCI_KNS tci_k256
+#define TCI_STEP_THREADS 256
+#define TCI_CTAS_PER_SM 2
+#endif
 
 // Optional per-phase timing hook (defined by an instrumented build; no-op here).
 #ifndef TCI_PHASE
 #define TCI_PHASE(id) ((void)0)
 #endif
 
+namespace TCI_KNS {
 namespace {
 
 constexpr int NT = TCI_STEP_THREADS;
@@ -2522,6 +2532,15 @@ cudaError_t tci_step_launch(const char* blob_dev, char* res_dev, const int* orde
   return cudaGetLastError();
 }
 
+extern const tci_kernel_set kernels = {TCI_STEP_THREADS, TCI_CTAS_PER_SM, tci_step_smem_bytes,
+                                       tci_resident_smem_bytes, tci_step_configure, tci_step_launch,
+                                       tci_resident_launch};
+
+}  // namespace TCI_KNS
+
+// The entry point without allocation is built once (in the throughput variant).
+#ifndef TCI_SECONDARY
+
 // ===================================================================== rrLU
 // without allocation (tci_rrlu_noalloc; no counterpart in the reference).
 //
@@ -2549,6 +2568,7 @@ namespace tci {
 void set_error(int code, const std::string& msg);
 }
 
+namespace TCI_KNS {
 namespace {
 
 constexpr int64_t NOALLOC_MAX_ELEMS = (int64_t)1 << 19;  // m * n
@@ -2592,6 +2612,7 @@ struct NoallocDevice {
 };
 
 }  // namespace
+}  // namespace TCI_KNS
 
 // See include/tci_gb300.h.  The first call on a device resolves the device
 // address of the scratch array (cudaGetSymbolAddress) and raises the kernel's
@@ -2603,6 +2624,7 @@ extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64
                                 double abstol, int32_t leftorthogonal, int32_t* rowperm_dev, int32_t* colperm_dev,
                                 int32_t* npivot_dev, double* error_dev, int32_t* status_dev, double* factors_dev,
                                 uintptr_t stream_u) {
+  using namespace TCI_KNS;
   static std::mutex mu;
   static NoallocDevice devs[64];
   if (m < 1 || n < 1 || m > NOALLOC_MAX_DIM || n > NOALLOC_MAX_DIM || m * n > NOALLOC_MAX_ELEMS) {
@@ -2683,3 +2705,4 @@ extern "C" int tci_rrlu_noalloc(const double* A_dev, int64_t m, int64_t n, int64
   }
   return 0;
 }
+#endif  // TCI_SECONDARY

@@ -134,15 +134,6 @@ typedef struct tci_resident_state {
   tci_queue_slot ring[TCI_DRING];
 } tci_resident_state;
 
-// Threads of one task CTA, and CTAs resident per SM (the shared-memory budget of
-// a CTA is the SM's divided among them).  Two 256-thread CTAs per SM: while one
-// task waits on a pivot's latency chain (division, reductions, decision,
-// barriers) the other's rank-1 update keeps the FP64 pipe busy.  Measured on a
-// 10 000-request served step: 550 ms of kernel time against 630 ms with one
-// 512-thread CTA per SM, although Π above ~114 rows then no longer fits in
-// shared memory and is factored in the L2-resident per-CTA scratch.
-#define TCI_STEP_THREADS 256
 // EVAL tasks whose bonds are at most this run one thread per point, the running
-// vector in 2 x TCI_EVAL_THREAD_RMAX x TCI_STEP_THREADS doubles of shared memory.
+// vector in 2 x TCI_EVAL_THREAD_RMAX x (task CTA threads) doubles of shared memory.
 #define TCI_EVAL_THREAD_RMAX 16
-#define TCI_CTAS_PER_SM 2
