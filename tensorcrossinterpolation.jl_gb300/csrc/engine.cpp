@@ -438,6 +438,9 @@ int Engine::launch() {
   waiters.clear();
   waiters.swap(waiters_);
   const size_t nt = batch.size();
+  // fewer tasks than SMs: each gets a whole SM (latency variant); else two
+  // task CTAs share an SM (throughput variant)
+  ks_ = nt < (size_t)num_sms ? &tci_k512::kernels : &tci_k256::kernels;
 
   // ---- layout
   size_t off = a16(nt * sizeof(tci_task));
@@ -452,8 +455,8 @@ int Engine::launch() {
   bool anybad = false;
   for (size_t i = 0; i < nt; ++i) {
     apply_tuning(batch[i]->t);
-    if (!plan_task(batch[i]->t, smem_bytes, wel[i], batch[i]->t.ain || batch[i]->ain_host, ks_->threads,
-                   plan_limit_)) {
+    if (!plan_task(batch[i]->t, ks_->step_smem_bytes(), wel[i], batch[i]->t.ain || batch[i]->ain_host,
+                   ks_->threads, plan_limit_)) {
       bad[i] = 1;
       anybad = true;
     }
