@@ -358,8 +358,8 @@ typedef struct tci_stats {
    * resuming the solves after them (summed over the engines' threads) */
   double host_launch_ms, host_wait_ms, host_resume_ms;
   /* SM clock cycles spent inside tasks, summed over all tasks (each task runs
-   * on one CTA, one CTA per SM): divided by SMs x clock x wall time it gives
-   * the fraction of the device kept busy */
+   * on one CTA; one or two task CTAs per SM): divided by task CTAs x clock x
+   * wall time it gives the fraction of the task slots kept busy */
   int64_t task_cycles;
   /* elements of feval computed from tables of the factored f parts (one FP64
    * operation each) rather than by evaluating f */
