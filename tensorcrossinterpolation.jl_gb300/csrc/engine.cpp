@@ -856,6 +856,7 @@ void Engine::set_resident(ResidentQueue* q, BlockPool* host_pool, BlockPool* scr
   hpool_ = host_pool;
   spool_ = scratch_pool;
   res_smem_ = q ? q->ks->resident_smem_bytes() : 0;
+  res_threads_ = q ? q->ks->threads : 0;
 }
 
 int Engine::submit() {
@@ -878,7 +879,7 @@ int Engine::submit() {
       tci_task& t = r.t;
       size_t we = 0;
       apply_tuning(t);
-      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host, rq_->ks->threads, plan_limit_)) {
+      if (!plan_task(t, res_smem_, we, t.ain || r.ain_host, res_threads_, plan_limit_)) {
         rc = fail(TCI_ERR_TOO_LARGE, "a matrix exceeds the step kernel's on-chip plan");
         break;
       }

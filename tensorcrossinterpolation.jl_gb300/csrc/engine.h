@@ -338,6 +338,7 @@ class Engine {
   BlockPool* spool_ = nullptr;  // device scratch of this engine's tasks (this thread only)
   BlockPool* dpool_ = nullptr;
   size_t res_smem_ = 0;
+  int res_threads_ = 0;  // tasks are planned for this variant's budget (it fits the other one too)
   size_t plan_limit_ = SIZE_MAX;  // TCI_PLAN_SMEM
   std::vector<Flight> flights_;
   size_t inflight_tasks_ = 0;  // tasks of flights_
