@@ -187,7 +187,6 @@ int Engine::init() {
   CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
   CUDA_TRY(tci_k256::kernels.configure());
   CUDA_TRY(tci_k512::kernels.configure());
-  smem_bytes = ks_->step_smem_bytes();
   // TCI_PLAN_SMEM=<bytes> plans RRLU and SITE tasks against a smaller
   // shared-memory budget (the kernel keeps its own), so that tests reach the
   // global-memory layouts with small matrices; results do not depend on the layout.

@@ -297,7 +297,6 @@ class Engine {
 
   tci_stats stats{};
   bool timing = true;
-  size_t smem_bytes = 0;
   const tci_kernel_set* ks_ = &tci_k256::kernels;  // the variant of the current / last batched launch
   int num_sms = 0;
   size_t hbm_budget = 0;
