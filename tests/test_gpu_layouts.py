@@ -79,3 +79,25 @@ def test_task_beyond_the_plan_fails_cleanly(T):
         T.crossinterpolate2(float, T.DeviceFunction("served", prm), [12] * 6, tolerance=1e-10, maxbonddim=64, ctx=ctx)
     tci, ranks, _ = T.crossinterpolate2(float, T.DeviceFunction("lorentz"), [4] * 4, tolerance=1e-8, ctx=ctx)
     assert max(ranks) >= 1
+
+
+def test_throughput_variant_matches_oracle(T, oracle):
+    """Enough live solves that the resident kernel runs two 256-thread task CTAs
+    per SM (the throughput variant) for most of the batch: pivots and site
+    tensors still equal the oracle's."""
+    rng = np.random.default_rng(80)
+    specs, raw = [], []
+    for _ in range(400):
+        L = int(rng.integers(4, 8))
+        d = int(rng.integers(2, 9))
+        prm = _served(rng, L, d)
+        kw = dict(tolerance=10 ** rng.uniform(-10, -6), maxbonddim=32)
+        specs.append((T.DeviceFunction("served", prm), [d] * L, kw))
+        raw.append((L, d, prm, kw))
+    res = T.crossinterpolate2_batched(specs, max_live=400)
+    for i in range(0, 400, 20):
+        L, d, prm, kw = raw[i]
+        ref, _, _ = oracle.crossinterpolate2([d] * L, oracle.F_SERVED, prm, None, **kw)
+        _same_sets(res[i], ref)
+        for b in range(1, L + 1):
+            assert np.array_equal(res[i].sitetensor(b), ref.core(b)), f"solve {i} site tensor {b} differs"
