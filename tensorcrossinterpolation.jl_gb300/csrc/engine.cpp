@@ -66,13 +66,15 @@ bool IndexSet::contains(const uint8_t* v) const {
 IndexSet kron_right(const IndexSet& I, int d) {
   IndexSet o;
   o.len = I.len + 1;
-  o.data.reserve(I.n * d * o.len);
-  std::vector<uint8_t> buf(o.len);
+  o.n = I.n * (size_t)d;
+  o.data.resize(o.n * (size_t)o.len);
+  uint8_t* dst = o.data.data();
+  const size_t il = (size_t)I.len;
   for (int j = 0; j < d; ++j)
     for (size_t i = 0; i < I.n; ++i) {
-      if (I.len) std::memcpy(buf.data(), I.at(i), I.len);
-      buf[I.len] = (uint8_t)j;
-      o.push(buf.data());
+      if (il) std::memcpy(dst, I.data.data() + i * il, il);
+      dst[il] = (uint8_t)j;
+      dst += o.len;
     }
   return o;
 }
@@ -80,16 +82,83 @@ IndexSet kron_right(const IndexSet& I, int d) {
 IndexSet kron_left(int d, const IndexSet& J) {
   IndexSet o;
   o.len = J.len + 1;
-  o.data.reserve(J.n * d * o.len);
-  std::vector<uint8_t> buf(o.len);
+  o.n = J.n * (size_t)d;
+  o.data.resize(o.n * (size_t)o.len);
+  uint8_t* dst = o.data.data();
+  const size_t jl = (size_t)J.len;
   for (size_t j = 0; j < J.n; ++j)
     for (int i = 0; i < d; ++i) {
-      buf[0] = (uint8_t)i;
-      if (J.len) std::memcpy(buf.data() + 1, J.at(j), J.len);
-      o.push(buf.data());
+      dst[0] = (uint8_t)i;
+      if (jl) std::memcpy(dst + 1, J.data.data() + j * jl, jl);
+      dst += o.len;
     }
   return o;
 }
+
+namespace {
+// Multi-indices of up to 16 bytes as two integers (bytes in order, zero padded):
+// equal keys <=> equal multi-indices of one length.
+struct Key16 {
+  uint64_t lo, hi;
+  bool operator==(const Key16& o) const { return lo == o.lo && hi == o.hi; }
+};
+inline uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+inline Key16 key16(const uint8_t* v, int len) {
+  Key16 k{0, 0};
+  for (int q = 0; q < len && q < 8; ++q) k.lo |= (uint64_t)v[q] << (8 * q);
+  for (int q = 8; q < len; ++q) k.hi |= (uint64_t)v[q] << (8 * (q - 8));
+  return k;
+}
+
+// Base.union for lengths up to 16: open addressing over packed keys, in a table
+// kept per thread (slots hold entry + 1; 0 = empty).
+IndexSet union_small(const IndexSet& a, const IndexSet& b) {
+  thread_local std::vector<uint32_t> table;
+  thread_local std::vector<Key16> keys;
+  IndexSet o;
+  o.len = a.len;
+  const size_t nmax = a.n + b.n;
+  size_t cap = 16;
+  while (cap < 2 * nmax + 1) cap <<= 1;
+  if (table.size() < cap) table.resize(cap);
+  if (keys.size() < nmax) keys.resize(nmax);
+  uint32_t* const tab = table.data();  // (thread-local lookups hoisted out of the loop)
+  Key16* const ks = keys.data();
+  std::memset(tab, 0, cap * sizeof(uint32_t));
+  o.data.resize(nmax * (size_t)a.len);
+  uint8_t* dst = o.data.data();
+  size_t cnt = 0;
+  const size_t mask = cap - 1;
+  for (const IndexSet* src : {&a, &b})
+    for (size_t i = 0; i < src->n; ++i) {
+      const uint8_t* v = src->data.data() + i * (size_t)a.len;
+      const Key16 k = key16(v, a.len);
+      size_t h = mix64(k.lo * 0x9e3779b97f4a7c15ULL ^ mix64(k.hi)) & mask;
+      bool found = false;
+      while (tab[h]) {
+        if (ks[tab[h] - 1] == k) {
+          found = true;
+          break;
+        }
+        h = (h + 1) & mask;
+      }
+      if (!found) {
+        tab[h] = (uint32_t)(cnt + 1);
+        ks[cnt] = k;
+        for (int q = 0; q < a.len; ++q) dst[q] = v[q];
+        dst += a.len;
+        ++cnt;
+      }
+    }
+  o.n = cnt;
+  o.data.resize(cnt * (size_t)a.len);
+  return o;
+}
+}  // namespace
 
 IndexSet set_union(const IndexSet& a, const IndexSet& b) {
   IndexSet o;
@@ -98,6 +167,7 @@ IndexSet set_union(const IndexSet& a, const IndexSet& b) {
     if (a.n + b.n > 0) o.n = 1;
     return o;
   }
+  if (a.len <= 16 && a.n + b.n < ((size_t)1 << 31)) return union_small(a, b);
   size_t cap = 16;
   while (cap < 2 * (a.n + b.n) + 1) cap <<= 1;
   std::vector<int64_t> table(cap, -1);
@@ -129,8 +199,10 @@ IndexSet select(const IndexSet& s, const int32_t* idx, int k) {
     o.n = (size_t)k;
     return o;
   }
-  o.data.reserve((size_t)k * s.len);
-  for (int i = 0; i < k; ++i) o.push(s.at((size_t)idx[i]));
+  o.n = (size_t)k;
+  o.data.resize((size_t)k * s.len);
+  uint8_t* dst = o.data.data();
+  for (int i = 0; i < k; ++i, dst += s.len) std::memcpy(dst, s.at((size_t)idx[i]), (size_t)s.len);
   return o;
 }
 
