@@ -458,6 +458,14 @@ class TensorCI2:
                                     _p(piv, I64P), piv.shape[0], ctypes.byref(h)))
         self.h = h
 
+    @classmethod
+    def _wrap(cls, f, localdims, ctx, handle):
+        """A solve the library created (batched entry points)."""
+        t = cls.__new__(cls)
+        t.ctx, t.f, t.h = ctx, f, handle
+        t.localdims = [int(d) for d in localdims]
+        return t
+
     def __del__(self):
         try:
             if self.h:
@@ -1014,15 +1022,91 @@ def make_requests(specs):
     return arr, keep
 
 
+_REQ_DTYPE = None
+
+
+def _req_dtype():
+    """numpy mirror of Request (pointers as uint64, opts flattened), built from the
+    ctypes field offsets."""
+    global _REQ_DTYPE
+    if _REQ_DTYPE is None:
+        def np_type(ct):
+            if ct in (I64P, F64P):
+                return np.uint64
+            return {ctypes.c_int32: np.int32, ctypes.c_int64: np.int64, ctypes.c_double: np.float64,
+                    ctypes.c_uint64: np.uint64}[ct]
+
+        names, formats, offsets = [], [], []
+        for nm, ct in Request._fields_:
+            if ct is Opts:
+                for onm, oct_ in Opts._fields_:
+                    names.append("opts_" + onm)
+                    formats.append(np_type(oct_))
+                    offsets.append(Request.opts.offset + getattr(Opts, onm).offset)
+            else:
+                names.append(nm)
+                formats.append(np_type(ct))
+                offsets.append(getattr(Request, nm).offset)
+        _REQ_DTYPE = np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                               "itemsize": ctypes.sizeof(Request)})
+    return _REQ_DTYPE
+
+
+def pack_requests(specs):
+    """The same requests as make_requests, packed with whole-array operations: all
+    local dims and f parameters in two arrays, the option structs from one
+    make_opts per distinct set of keyword arguments besides tolerance and
+    maxbonddim.  Returns (POINTER(Request), buffers to keep alive)."""
+    n = len(specs)
+    rec = np.zeros(max(n, 1), _req_dtype())
+    if n == 0:
+        return rec.ctypes.data_as(ctypes.POINTER(Request)), [rec]
+    Ls = np.fromiter((len(ld) for _, ld, _ in specs), np.int64, n)
+    dims = np.ascontiguousarray(np.concatenate([np.asarray(ld, dtype=np.int64).ravel() for _, ld, _ in specs]))
+    plist = [f.params for f, _, _ in specs]
+    npar = np.fromiter((p.size for p in plist), np.int64, n)
+    prm = np.ascontiguousarray(np.concatenate(plist).astype(np.float64)) if npar.sum() else np.zeros(1)
+    doff = np.concatenate([[0], np.cumsum(Ls)[:-1]]).astype(np.uint64)
+    poff = np.concatenate([[0], np.cumsum(npar)[:-1]]).astype(np.uint64)
+    rec["L"] = Ls
+    rec["fid"] = np.fromiter((f.fid for f, _, _ in specs), np.int32, n)
+    rec["localdims"] = np.uint64(dims.ctypes.data) + np.uint64(8) * doff
+    rec["fparams"] = np.where(npar > 0, np.uint64(prm.ctypes.data) + np.uint64(8) * poff, np.uint64(0))
+    rec["nparams"] = npar
+    fields = [nm for nm, _ in Opts._fields_]
+    groups, tol, mbd, single = {}, np.empty(n), np.empty(n, np.int64), []
+    for i, (_, _, kw) in enumerate(specs):
+        if "pivottolerance" in kw:  # its consistency check with tolerance is per request
+            single.append(i)
+            continue
+        rest = tuple(sorted((k, v) for k, v in kw.items() if k not in ("tolerance", "maxbonddim")))
+        groups.setdefault(rest, []).append(i)
+        t = kw.get("tolerance")
+        tol[i] = 1e-8 if t is None else float(t)
+        b = kw.get("maxbonddim")
+        mbd[i] = 0 if b is None else int(b)
+    for rest, idx in groups.items():
+        o = make_opts(**dict(rest))
+        idx = np.asarray(idx, np.int64)
+        for nm in fields:
+            rec["opts_" + nm][idx] = getattr(o, nm)
+        rec["opts_tolerance"][idx] = tol[idx]
+        rec["opts_maxbonddim"][idx] = mbd[idx]
+    for i in single:
+        o = make_opts(**specs[i][2])
+        for nm in fields:
+            rec["opts_" + nm][i] = getattr(o, nm)
+    return rec.ctypes.data_as(ctypes.POINTER(Request)), [rec, dims, prm, specs]
+
+
 def crossinterpolate2_batched(specs, max_live=0, ctx=None):
     """Solve many crossinterpolate2 problems together (one launch per step for all)."""
     ctx = ctx or default_context()
-    arr, keep = make_requests(specs)
+    arr, keep = pack_requests(specs)
     out = (ctypes.c_void_p * len(specs))()
     rc = load_library().tci_crossinterpolate2_batched(ctx.h, len(specs), arr, int(max_live), out)
-    res = []
-    for i, (f, localdims, _) in enumerate(specs):
-        res.append(TensorCI2(f, localdims, ctx=ctx, _handle=ctypes.c_void_p(out[i])) if out[i] else None)
+    wrap = TensorCI2._wrap
+    res = [wrap(f, ld, ctx, ctypes.c_void_p(h)) if h else None for (f, ld, _), h in zip(specs, out)]
     _check(rc)
     return res
 
@@ -1073,7 +1157,7 @@ def tensortrains(tcis, ctx=None):
 def serve(specs, arrival, max_live=0, ctx=None):
     """Continuous-batching server over a request stream -> (latency, rank, wall)."""
     ctx = ctx or default_context()
-    arr, keep = make_requests(specs)
+    arr, keep = pack_requests(specs)
     arrival = np.ascontiguousarray(arrival, dtype=np.float64)
     lat = np.zeros(len(specs))
     rank = np.zeros(len(specs), np.int64)
