@@ -810,9 +810,9 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
     double last_progress = now_s(), last_done = last_progress;
     double last_switch = now_s();
     for (;;) {
-      // Kernel variant by load (worker 0): with fewer live solves than half the
-      // SMs and no admission waiting, every task gets a whole SM (k512); from
-      // one live solve per SM on, two task CTAs share an SM (k256).  Tasks are
+      // Kernel variant by load (worker 0): with fewer live solves than SMs and no
+      // admission waiting, every task gets a whole SM (k512); from two live
+      // solves per SM on, two task CTAs share an SM (k256).  Tasks are
       // planned for k256's budget, which k512 satisfies, so a switch only
       // relaunches the kernel; tasks published meanwhile wait in the ring.
       if (g == 0 && ctx->rq) {
@@ -827,8 +827,8 @@ int drive(tci_ctx* ctx, std::deque<Job>& jobs, bool use_arrival, int64_t max_liv
         const tci_kernel_set* cur = ctx->rq->ks;
         const int nsm = ctx->rq->num_sms;
         const tci_kernel_set* want = cur;
-        if (cur == &tci_k256::kernels && live > 0 && 2 * live < nsm && !admit_waiting) want = &tci_k512::kernels;
-        if (cur == &tci_k512::kernels && live >= nsm) want = &tci_k256::kernels;
+        if (cur == &tci_k256::kernels && live > 0 && live < nsm && !admit_waiting) want = &tci_k512::kernels;
+        if (cur == &tci_k512::kernels && live >= 2 * nsm) want = &tci_k256::kernels;
         if (want != cur && now_s() - last_switch > 0.02) {
           last_switch = now_s();
           int rc = ctx->rq->stop();
