@@ -89,6 +89,9 @@ __device__ __forceinline__ uint64_t abs_bits(double v) {
   asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(v));
   return ((uint64_t)(hi & 0x7fffffffu) << 32) | (uint64_t)lo;
 }
+// v is NaN, tested on the integer pipe (an FP64 self-comparison would take the
+// slow FP64 pipe).
+__device__ __forceinline__ bool is_nan_bits(double v) { return abs_bits(v) > 0x7ff0000000000000ULL; }
 
 // Argmax of abs2 with first-in-column-major tie breaking, without squaring on
 // the FP64 pipe in the common case: while updating, each thread tracks the
@@ -578,11 +581,11 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
         const double v = (!leftorth && j > K) ? __ddiv_rn(b, piv) : b;
         col[K] = v;
         col[R] = a;
-        if (j > K && v != v) nan = true;
+        if (j > K && is_nan_bits(v)) nan = true;
       } else if (j > K) {
         const double v = !leftorth ? __ddiv_rn(col[K], piv) : col[K];
         col[K] = v;
-        if (v != v) nan = true;
+        if (is_nan_bits(v)) nan = true;
       }
     } else if (w < n + m) {  // column pair (i, K) <-> (i, C)
       const int i = w - n;
@@ -594,11 +597,11 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
         const double v = (leftorth && i > K) ? __ddiv_rn(b, piv) : b;
         ck[i] = v;
         cc[i] = a;
-        if (i > K && v != v) nan = true;
+        if (i > K && is_nan_bits(v)) nan = true;
       } else if (i > K) {
         const double v = leftorth ? __ddiv_rn(ck[i], piv) : ck[i];
         ck[i] = v;
-        if (v != v) nan = true;
+        if (is_nan_bits(v)) nan = true;
       }
     } else {  // the corners (K, K), (K, C), (R, K), (R, C)
       const int rows[2] = {K, R}, cols[2] = {K, C};
@@ -614,7 +617,7 @@ __device__ __forceinline__ void swap_scale_body(double* A, int lda, int m, int n
           const int i = rows[p], j = cols[q];
           if ((leftorth && j == K && i > K) || (!leftorth && i == K && j > K)) v = __ddiv_rn(v, piv);
           A[i + (size_t)j * lda] = v;
-          if ((i == K || j == K) && v != v) nan = true;
+          if ((i == K || j == K) && is_nan_bits(v)) nan = true;
         }
     }
   }
@@ -1228,7 +1231,7 @@ __device__ void task_site(const tci_task& T, const char* blob, char* resb, char*
     for (int e = tid; e < rows_here * r; e += NT) {
       int rr = e % rows_here, q = e / rows_here;
       double v = W[rr + (size_t)q * RB];
-      if (v != v) nanflag = 1;
+      if (is_nan_bits(v)) nanflag = 1;
       T.core_out[(base + rr) + (size_t)q * m] = v;
     }
     __syncthreads();
@@ -2360,7 +2363,7 @@ __global__ void __launch_bounds__(BIG_NT, 1) rrlu_big_kernel(BigArgs P) {
       if (!leftorth && lr < K && lc > lr) v = __ddiv_rn(v, __ldcg(&P.pivs[lr]));
       const bool inL = lc < K && lr >= lc;
       const bool inU = lr < K && lr <= lc;
-      if ((inL || inU) && v != v) bad = 1;
+      if ((inL || inU) && is_nan_bits(v)) bad = 1;
       P.fact[lr + (size_t)lc * m] = v;
     }
   }
