@@ -1,7 +1,8 @@
 """Host logic of the engine on the CPU through the library's own C++ symbols,
 built into small checkers linked against libtci_gpu.so: the index-set
-operations (kronecker, union, select, pushunique!; tests/host/indexset_check.cpp)
-and the key layout of the device value cache (tests/host/fcache_keys_check.cpp)."""
+operations (kronecker, union, select, pushunique!; tests/host/indexset_check.cpp and,
+on randomized inputs, tests/host/indexset_random_check.cpp) and the key layout of
+the device value cache (tests/host/fcache_keys_check.cpp)."""
 import os
 import shutil
 import subprocess
@@ -35,3 +36,10 @@ def test_index_sets(T, tmp_path):
 
 def test_fcache_keys(T, tmp_path):
     _run_checker(T, tmp_path, "fcache_keys_check")
+
+
+def test_index_sets_randomized(T, tmp_path):
+    """kronecker / union / select against direct restatements on randomized
+    inputs (both union paths, many duplicates), and the task layouts' global
+    scratch sizes."""
+    _run_checker(T, tmp_path, "indexset_random_check")
