@@ -10,7 +10,8 @@ library.  The tests call it through the C ABI and check it
 
   - against the allocating entry point tci_rrlu, bit for bit, on two calls in a
     row (the second larger than shared memory, so the fixed array holds the
-    working matrix) and at the two limit shapes (16384 x 32 and m*n = 2^19);
+    working matrix), at the two limit shapes (16384 x 32 and m*n = 2^19) and
+    when captured into a CUDA graph and replayed on new inputs;
   - against the CPU oracle directly on the reference's own rrLU test matrices
     (test/test_matrixlu.jl), and on a matrix whose L holds a NaN, where the
     status output must carry TCI_ERR_NAN (the reference's "lu.L contains NaNs",
@@ -26,27 +27,46 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
+def _buffers(torch, m, n):
+    dev = torch.device("cuda:0")
+    return dict(a=torch.empty(m * n, dtype=torch.float64, device=dev),
+                rowp=torch.full((m,), -1, dtype=torch.int32, device=dev),
+                colp=torch.full((n,), -1, dtype=torch.int32, device=dev),
+                npiv=torch.full((1,), -1, dtype=torch.int32, device=dev),
+                err=torch.full((1,), -1.0, dtype=torch.float64, device=dev),
+                status=torch.full((1,), -1, dtype=torch.int32, device=dev),
+                fac=torch.empty(m * n, dtype=torch.float64, device=dev))
+
+
+def _load(torch, b, A):
+    b["a"].copy_(torch.from_numpy(np.asfortranarray(A).reshape(-1, order="F").copy()))
+
+
+def _enqueue(T, b, m, n, stream, **kw):
+    """Only enqueues (no synchronisation), so it can run inside a stream capture."""
+    rc = T.load_library().tci_rrlu_noalloc(
+        ctypes.c_void_p(b["a"].data_ptr()), m, n, int(kw.get("maxrank") or 0), kw.get("reltol", 1e-14),
+        kw.get("abstol", 0.0), int(kw.get("leftorthogonal", True)), ctypes.c_void_p(b["rowp"].data_ptr()),
+        ctypes.c_void_p(b["colp"].data_ptr()), ctypes.c_void_p(b["npiv"].data_ptr()),
+        ctypes.c_void_p(b["err"].data_ptr()), ctypes.c_void_p(b["status"].data_ptr()),
+        ctypes.c_void_p(b["fac"].data_ptr()), stream)
+    assert rc == 0, T.load_library().tci_last_error()
+
+
+def _collect(b, m, n):
+    F = b["fac"].cpu().numpy().reshape((m, n), order="F")
+    return dict(rowperm=b["rowp"].cpu().numpy(), colperm=b["colp"].cpu().numpy(), npivot=int(b["npiv"].item()),
+                error=float(b["err"].item()), status=int(b["status"].item()), F=F)
+
+
 def _noalloc(T, torch, A, **kw):
     m, n = A.shape
     dev = torch.device("cuda:0")
-    a = torch.from_numpy(np.asfortranarray(A).reshape(-1, order="F").copy()).to(dev)
-    rowp = torch.full((m,), -1, dtype=torch.int32, device=dev)
-    colp = torch.full((n,), -1, dtype=torch.int32, device=dev)
-    npiv = torch.full((1,), -1, dtype=torch.int32, device=dev)
-    err = torch.full((1,), -1.0, dtype=torch.float64, device=dev)
-    status = torch.full((1,), -1, dtype=torch.int32, device=dev)
-    fac = torch.empty(m * n, dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev).cuda_stream
-    rc = T.load_library().tci_rrlu_noalloc(
-        ctypes.c_void_p(a.data_ptr()), m, n, int(kw.get("maxrank") or 0), kw.get("reltol", 1e-14),
-        kw.get("abstol", 0.0), int(kw.get("leftorthogonal", True)), ctypes.c_void_p(rowp.data_ptr()),
-        ctypes.c_void_p(colp.data_ptr()), ctypes.c_void_p(npiv.data_ptr()), ctypes.c_void_p(err.data_ptr()),
-        ctypes.c_void_p(status.data_ptr()), ctypes.c_void_p(fac.data_ptr()), stream)
-    assert rc == 0, T.load_library().tci_last_error()
+    b = _buffers(torch, m, n)
+    _load(torch, b, A)
+    _enqueue(T, b, m, n, torch.cuda.current_stream(dev).cuda_stream, **kw)
     torch.cuda.synchronize(dev)
-    F = fac.cpu().numpy().reshape((m, n), order="F")
-    return dict(rowperm=rowp.cpu().numpy(), colperm=colp.cpu().numpy(), npivot=int(npiv.item()),
-                error=float(err.item()), status=int(status.item()), F=F)
+    return _collect(b, m, n)
 
 
 def _factors(r, leftorthogonal):
@@ -61,8 +81,9 @@ def _factors(r, leftorthogonal):
     return L, U
 
 
-def _check_against_allocating(T, torch, A, **kw):
-    r = _noalloc(T, torch, A, **kw)
+def _check_against_allocating(T, torch, A, r=None, **kw):
+    if r is None:
+        r = _noalloc(T, torch, A, **kw)
     ref = T.rrlu(A, **kw)
     assert r["status"] == 0
     assert r["npivot"] == ref.npivot
@@ -110,6 +131,39 @@ def test_noalloc_limit_shapes(T, shape):
     k = 20
     A = rng.standard_normal((m, k)) @ rng.standard_normal((k, n)) + 1e-12 * rng.standard_normal((m, n))
     _check_against_allocating(T, torch, A, reltol=1e-10, maxrank=24)
+
+
+def test_noalloc_in_cuda_graph(T):
+    """The call captured into a CUDA graph after a warm-up call (which does the
+    per-device set-up outside the capture), then replayed on new contents of the
+    same input buffer: every replay matches tci_rrlu bit for bit.  The matrix is
+    larger than shared memory, so the replays also reuse the fixed array."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(77)
+    m, n, k = 200, 150, 18
+    kw = dict(reltol=1e-10, maxrank=32)
+
+    def matrix():
+        return rng.standard_normal((m, k)) @ rng.standard_normal((k, n)) + 1e-12 * rng.standard_normal((m, n))
+
+    dev = torch.device("cuda:0")
+    b = _buffers(torch, m, n)
+    A = matrix()
+    _load(torch, b, A)
+    _enqueue(T, b, m, n, torch.cuda.current_stream(dev).cuda_stream, **kw)
+    torch.cuda.synchronize(dev)
+    _check_against_allocating(T, torch, A, r=_collect(b, m, n), **kw)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="thread_local"):
+        _enqueue(T, b, m, n, torch.cuda.current_stream(dev).cuda_stream, **kw)
+    for _ in range(3):
+        A = matrix()
+        _load(torch, b, A)
+        for key in ("rowp", "colp", "npiv", "status"):
+            b[key].fill_(-1)
+        g.replay()
+        torch.cuda.synchronize(dev)
+        _check_against_allocating(T, torch, A, r=_collect(b, m, n), **kw)
 
 
 def test_noalloc_reference_matrices_against_oracle(T, oracle, golden):
