@@ -64,6 +64,35 @@ def test_luci_colstimespivotinv(oracle, golden):
     assert np.allclose(left @ right, A[:, J] @ np.linalg.inv(P) @ A[I, :], rtol=1e-9, atol=1e-12)
 
 
+def test_luci_exact_lowrank(oracle, golden):
+    """test_matrixluci.jl:48-74: MatrixLUCI of an exact rank-3 product has 3
+    pivots, left * right reproduces it, and the first npivots rows of colmatrix
+    (left when leftorthogonal is false, matrixluci.jl:40-42) are well conditioned."""
+    g = golden["rrlu_lowrank"]
+    A = np.array(g["p"]) @ np.array(g["q"])
+    for leftorth in (True, False):
+        left, right = oracle.luci(A, leftorthogonal=leftorth)
+        assert left.shape == (A.shape[0], 3) and right.shape == (3, A.shape[1])
+        assert np.allclose(left @ right, A, rtol=1e-10, atol=1e-12)
+    colmatrix, _ = oracle.luci(A, leftorthogonal=False)
+    res = oracle.rrlu(A)
+    assert np.allclose(colmatrix, A[:, res["colpermutation"][:3]], rtol=1e-10, atol=1e-12)
+    assert np.linalg.cond(colmatrix[:3, :]) < 1e12
+
+
+def test_luci_near_duplicate_columns(oracle, golden):
+    """test_matrixluci.jl:39-45: the 8 x 6 matrix beside a copy perturbed by
+    1e-3 (seeded here in place of rand): at reltol 1e-2 fewer pivots than rows
+    and columns, and left * right within 1e-2 of the matrix everywhere."""
+    A = np.array(golden["luci"]["A"])
+    A = np.hstack([A, A + 1e-3 * np.random.default_rng(7).random(A.shape)])
+    left, right = oracle.luci(A, reltol=1e-2)
+    res = oracle.rrlu(A, reltol=1e-2)
+    assert res["npivot"] < A.shape[0] and res["npivot"] < A.shape[1]
+    assert left.shape == (A.shape[0], res["npivot"])
+    assert np.max(np.abs(left @ right - A)) < 1e-2
+
+
 def test_argmax_first_in_column_major(oracle):
     """submatrixargmax keeps the first maximum of abs2 in column-major order
     (matrixlu.jl:16-31): with ties the earliest column, then the earliest row."""
