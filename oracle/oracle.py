@@ -339,6 +339,29 @@ class OracleTCI:
         _check(lib().orc_tci_addglobalpivots1sitesweep(self.h, _p(piv, I64P), piv.shape[0], reltol, abstol,
                                                        0 if maxbonddim is None else maxbonddim))
 
+    def addglobalpivots2sitesweep(self, f, pivots, tolerance=1e-8, normalizeerror=True, maxbonddim=None,
+                                  ntry=10, strictlynested=False):
+        """addglobalpivots2sitesweep! (tensorci2.jl:243-288), f = (fid, params):
+        add the pivots, run two 2-site sweeps at abstol = tolerance (times
+        maxsamplevalue when normalizeerror), then keep the requested pivots whose
+        |tt - f| is still above abstol and try again with those, at most ntry
+        times; returns how many remain."""
+        rows = [np.asarray(p, dtype=np.int64).ravel() for p in pivots]
+        if any(r.size != self.L for r in rows):  # tensorci2.jl:255-257
+            raise OracleError(2, "Please specify a pivot as one index per leg of the MPS.")
+        piv = np.ascontiguousarray(np.array(rows, dtype=np.int64).reshape(-1, self.L))
+        fvals = feval(f[0], f[1], piv) if piv.shape[0] else np.zeros(0)
+        cur = piv
+        for _ in range(ntry):
+            abstol = tolerance * (self.maxsamplevalue if normalizeerror else 1.0)
+            self.addglobalpivots(cur)
+            self.sweep2site(2, abstol=abstol, maxbonddim=maxbonddim, strictlynested=strictlynested)
+            new = piv[np.abs(self.evaluate(piv) - fvals) > abstol] if piv.shape[0] else piv
+            if new.shape[0] == 0 or {tuple(p) for p in new} == {tuple(p) for p in cur}:
+                return int(new.shape[0])
+            cur = new
+        return int(cur.shape[0])
+
     @property
     def maxsamplevalue(self):
         return lib().orc_tci_maxsample(self.h)

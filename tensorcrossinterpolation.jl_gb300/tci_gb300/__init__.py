@@ -516,6 +516,38 @@ class TensorCI2:
         _check(load_library().tci_addglobalpivots1sitesweep(self.h, _p(piv, I64P), piv.shape[0], reltol, abstol,
                                                             0 if maxbonddim is None else int(maxbonddim)))
 
+    def addglobalpivots2sitesweep(self, pivots, tolerance=1e-8, normalizeerror=True, maxbonddim=None,
+                                  pivotsearch="full", verbosity=0, ntry=10, strictlynested=False):
+        """addglobalpivots2sitesweep! (tensorci2.jl:243-288): add the pivots, run
+        two 2-site sweeps at abstol = tolerance (times maxsamplevalue when
+        normalizeerror), then keep the requested pivots whose |tt - f| is still
+        above abstol and try again with those, at most ntry times, stopping early
+        when the remaining set repeats.  Returns how many pivots remain."""
+        if pivotsearch != "full":
+            raise ArgumentError(TCI_ERR_ARG, "only pivotsearch=:full is implemented on the device")
+        piv = _pivots_array(pivots, len(self))
+        fvals = self._fvalues(piv)
+        cur = piv
+        for _ in range(ntry):
+            abstol = tolerance * (self.maxsamplevalue if normalizeerror else 1.0)
+            self.addglobalpivots(cur)
+            self.sweep2site(2, abstol=abstol, maxbonddim=maxbonddim, strictlynested=strictlynested)
+            new = piv[np.abs(self.evaluate(piv) - fvals) > abstol] if piv.shape[0] else piv
+            if verbosity > 0:
+                print(f"Trying to add {cur.shape[0]} global pivots, {new.shape[0]} still remain.")
+            if new.shape[0] == 0 or {tuple(p) for p in new} == {tuple(p) for p in cur}:
+                return int(new.shape[0])
+            cur = new
+        return int(cur.shape[0])
+
+    def _fvalues(self, points):
+        """f at points (n x L, 1-based): the device function, or the caller's f."""
+        if points.shape[0] == 0:
+            return np.zeros(0)
+        if isinstance(self.f, BatchFunction):
+            return np.ascontiguousarray(self.f.f(points.copy()), dtype=np.float64).reshape(-1)
+        return feval(self.f, self.localdims, points, ctx=self.ctx)
+
     # ---- state
     def linkdims(self):
         out = np.zeros(len(self) - 1, np.int64)
