@@ -64,3 +64,30 @@ def test_pivot_length_mismatch(T):
     with pytest.raises(T.ArgumentError):
         tci.addglobalpivots2sitesweep([[1, 1, 1, 1]], pivotsearch="rook")
     assert tci.addglobalpivots2sitesweep([]) == 0
+
+
+def test_globalsearch_nasty_function(T, oracle):
+    """test_tensorci2.jl:433-459 on the device: from optfirstpivot of a random
+    start, with 10 global-pivot searches per iteration, the same first pivot,
+    ranks and errors as the oracle, and the last error below 1e-10."""
+    n = 10
+
+    def f(p):
+        x = _x(p)
+        return np.exp(-10 * x) * np.sin(2 * np.pi * 100 * x**1.1)
+
+    start = np.random.default_rng(1234).integers(1, 3, size=n)
+    ofid = oracle.register_fn(f)
+    ofirst = oracle.optfirstpivot(ofid, (), [2] * n, start.copy())
+    kw = dict(tolerance=1e-12, maxbonddim=100, maxiter=100, nsearchglobalpivot=10, strictlynested=False)
+    _, rranks, rerrors = oracle.crossinterpolate2([2] * n, ofid, (), [ofirst], **kw)
+    bf = T.BatchFunction(f)
+    try:
+        first = T.optfirstpivot(bf, [2] * n, start)
+        assert list(first) == list(ofirst)
+        _, ranks, errors = T.crossinterpolate2(float, bf, [2] * n, [first], **kw)
+    finally:
+        bf.close()
+    assert list(ranks) == list(rranks)
+    assert np.array_equal(errors, rerrors)
+    assert errors[-1] < 1e-10

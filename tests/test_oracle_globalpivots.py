@@ -63,3 +63,21 @@ def test_pivot_length_mismatch(oracle):
         tci.addglobalpivots2sitesweep((oracle.F_LORENTZ, ()), np.ones((1, 3), np.int64))
     assert e.value.code == 2
     assert tci.addglobalpivots2sitesweep((oracle.F_LORENTZ, ()), np.zeros((0, 4), np.int64)) == 0
+
+
+def _nasty(p):
+    x = _x(p)
+    return np.exp(-10 * x) * np.sin(2 * np.pi * 100 * x**1.1)
+
+
+def test_globalsearch_nasty_function(oracle):
+    """test_tensorci2.jl:433-459: a 10-bit quantics function that oscillates
+    100 times, from optfirstpivot of a random start, with 10 global-pivot
+    searches per iteration: the last error is below 1e-10."""
+    n = 10
+    fid = oracle.register_fn(_nasty)
+    start = np.random.default_rng(1234).integers(1, 3, size=n)
+    first = oracle.optfirstpivot(fid, (), [2] * n, start)
+    _, ranks, errors = oracle.crossinterpolate2([2] * n, fid, (), [first], tolerance=1e-12, maxbonddim=100,
+                                                maxiter=100, nsearchglobalpivot=10, strictlynested=False)
+    assert errors[-1] < 1e-10
